@@ -1,0 +1,193 @@
+"""Generate the golden fixtures in this folder by running the reference package.
+
+Run in a container that has the reference checkout and its compiled extension
+(``oracle/build_ref.sh``)::
+
+    python tests/golden/make_golden.py
+
+Every fixture holds the seeded inputs and the reference's outputs for one
+small case shaped like one of the benchmark configurations (P1 Laplace, P2
+anisotropic diffusion on a jittered cube, Nedelec N1 Maxwell on a relabelled
+cube, vector-P1 elasticity / neo-Hookean pieces, linear forms, geometry and
+edge topology).  The fixtures are what pins the CPU oracle and the GPU path.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import reference_loader  # noqa: E402
+
+
+def jitter(p, h, amp, rng):
+    """Move interior vertices by U(-amp*h, amp*h)^3 (boundary vertices stay)."""
+    p = p.copy()
+    interior = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+    p[:, interior] += rng.uniform(-amp * h, amp * h, size=(3, int(interior.sum())))
+    return p
+
+
+def spd_tensors(E, rng):
+    """A = Q diag(exp(N(0, 0.5^2))) Q^T with Q a sign-fixed QR of a Gaussian."""
+    G = rng.standard_normal((E, 3, 3))
+    Q, R = np.linalg.qr(G)
+    Q = Q * np.sign(np.diagonal(R, axis1=1, axis2=2))[:, None, :]
+    lam = np.exp(rng.normal(0.0, 0.5, size=(E, 3)))
+    return np.einsum("eij,ej,ekj->eik", Q, lam, Q)
+
+
+def csr_parts(K):
+    K = K.tocsr()
+    return dict(indptr=np.asarray(K.indptr, np.int64), indices=np.asarray(K.indices, np.int64),
+                data=np.asarray(K.data, np.float64), shape=np.asarray(K.shape, np.int64))
+
+
+def main():
+    sk = reference_loader.load()
+    from skfemntv.forms import ddot, dot, grad, mul  # type: ignore
+    out = {}
+
+    # --- P1 Laplace, 1-point rule, coefficient 1 and a per-element kappa ---
+    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3)
+    X1, W1 = np.array([[.25], [.25], [.25]]), np.array([1 / 6])
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X1, W1))
+
+    @sk.BilinearForm
+    def lap(u, v, w):
+        return ddot(grad(u), grad(v))
+
+    @sk.BilinearForm
+    def klap(u, v, w):
+        return w.kappa * ddot(grad(u), grad(v))
+
+    rng = np.random.default_rng(np.random.SeedSequence(1))
+    kappa = np.exp(rng.normal(0, 1, size=m.nelements))
+    K = sk.asm(lap, b)
+    Kk = sk.asm(klap, b, kappa=kappa[:, None])
+    out["p1_laplace"] = dict(p=m.p, t=m.t, X=X1, W=W1, kappa=kappa, **csr_parts(K),
+                             kdata=np.asarray(Kk.data).copy())
+
+    # --- P1 default 4-point rule: mass + stiffness with per-(E,Q) coefficients ---
+    b4 = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1))
+
+    @sk.BilinearForm
+    def helm(u, v, w):
+        return w.c * ddot(grad(u), grad(v)) + w.s * dot(u, v)
+
+    cq = np.exp(rng.normal(0, 0.3, size=b4.dx.shape))
+    sq = rng.uniform(0.5, 2.0, size=b4.dx.shape)
+    K4 = sk.asm(helm, b4, c=cq, s=sq)
+    out["p1_helmholtz"] = dict(p=m.p, t=m.t, X=b4.X, W=b4.W, c=cq, s=sq, **csr_parts(K4),
+                               dx=b4.dx, grads=b4.tabulated_gradients)
+
+    # --- P2 anisotropic diffusion, 3^3 x 6 jittered cube, 4-point rule ---
+    n = 3
+    m0 = sk.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    rng = np.random.default_rng(np.random.SeedSequence(2))
+    pj = jitter(m0.p, 1.0 / n, 0.2, rng)
+    mj = sk.MeshTet(pj, m0.t)
+    m2 = sk.MeshTet2.from_mesh(mj)
+    X4, W4 = b4.X, b4.W
+    b2 = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(X4, W4))
+    A = spd_tensors(m2.nelements, rng)  # (E,3,3)
+    Apub = np.broadcast_to(np.moveaxis(A, (1, 2), (0, 1))[:, :, :, None], (3, 3, m2.nelements, len(W4)))
+
+    @sk.BilinearForm
+    def aniso(u, v, w):
+        return dot(mul(w.A, grad(u)), grad(v))
+
+    K2 = sk.asm(aniso, b2, A=np.ascontiguousarray(Apub))
+    out["p2_aniso"] = dict(p0=m0.p, pj=pj, t0=m0.t, p=m2.p, t=m2.t, X=X4, W=W4, A=A,
+                           **csr_parts(K2), dx=b2.dx, grads=b2.tabulated_gradients,
+                           det=b2._geometry_determinants, cond=b2._geometry_condition_numbers,
+                           xq=b2.global_coordinates)
+
+    # nonsymmetric tensor variant (the reference keeps nonsymmetric A)
+    Ans = A + 0.3 * rng.standard_normal(A.shape)
+    Ans_pub = np.broadcast_to(np.moveaxis(Ans, (1, 2), (0, 1))[:, :, :, None], Apub.shape)
+    K2n = sk.asm(aniso, b2, A=np.ascontiguousarray(Ans_pub))
+    out["p2_aniso"]["Ans"] = Ans
+    out["p2_aniso"]["ns_data"] = np.asarray(K2n.data).copy()
+
+    # --- P2 Laplace with the default 11-point rule (negative weight) ---
+    b2d = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=1))
+    K2d = sk.asm(lap, b2d)
+    out["p2_laplace_default"] = dict(p=m2.p, t=m2.t, X=b2d.X, W=b2d.W, **csr_parts(K2d))
+
+    # --- Nedelec N1 Maxwell, relabelled 3^3 x 6 cube, 27-point Duffy rule ---
+    rng = np.random.default_rng(np.random.SeedSequence(3))
+    perm = rng.permutation(m0.p.shape[1])
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(len(perm))
+    p_r = m0.p[:, inv]
+    t_r = perm[m0.t]
+    mr = sk.MeshTet(p_r, t_r)
+    nb = sk.AffineTetN1Basis(mr)
+    mu = np.exp(rng.normal(0, 0.3, size=mr.nelements))
+    asmb = sk.TetN1Assembler(nb)
+    Kn = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=(1.0 / mu)[:, None])
+    topo = nb.dof_map.topology
+    out["n1_maxwell"] = dict(p=p_r, t=t_r, mu=mu, X=nb.X, W=nb.W, **csr_parts(Kn),
+                             edges=topo.edges, element_edges=topo.element_edges,
+                             signs=topo.element_edge_signs, detJ=nb.detJ)
+
+    # --- vector P1 elasticity terms: symmetric gradient + divergence + mass ---
+    mv = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3)
+    bv = sk.Basis(mv, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
+    nat = sk.NativeBilinearForm(bv)
+    lam_q = np.full(bv.dx.shape, 10.0)
+    mu_q = np.full(bv.dx.shape, 1.0)
+    Kv = nat.assemble(symmetric_gradient=2 * mu_q, divergence=lam_q, value=0.5 * mu_q)
+    out["vp1_elasticity"] = dict(p=mv.p, t=mv.t, X=X1, W=W1, **csr_parts(Kv))
+
+    # --- neo-Hookean residual + tangent (oracle pipeline pieces), vector P1 ---
+    rng = np.random.default_rng(np.random.SeedSequence(5))
+    u = np.zeros(bv.N)
+    xyz = bv.doflocs  # (3, N) repeated per component
+    for _ in range(8):
+        d = rng.standard_normal(3); d /= np.linalg.norm(d)
+        kv = rng.integers(-1, 2, size=3)
+        ph = rng.uniform(0, 2 * np.pi)
+        comp = np.arange(bv.N) % 3
+        u += 0.05 * d[comp] * np.sin(np.pi * (kv @ xyz) + ph)
+    dofs3 = bv.element_dofs.T.reshape(mv.nelements, 4, 3)
+    Gu = np.einsum("eac,eqaj->eqcj", u[dofs3], bv.tabulated_gradients)
+    F = np.eye(3) + Gu
+    FiT = np.swapaxes(np.linalg.inv(F), -1, -2)
+    lnJ = np.log(np.linalg.det(F))
+    mu_, la_ = 1.0, 10.0
+    P = mu_ * (F - FiT) + la_ * lnJ[..., None, None] * FiT
+    I3 = np.eye(3)
+    At = (mu_ * np.einsum("rc,ij->ricj", I3, I3)[None, None]
+          + (mu_ - la_ * lnJ)[..., None, None, None, None] * np.einsum("eqrj,eqci->eqricj", FiT, FiT)
+          + la_ * np.einsum("eqri,eqcj->eqricj", FiT, FiT))
+    res, _ = sk.NativeLinearForm(bv).assemble(gradient=np.ascontiguousarray(P))
+    cross = sk.NativeCrossBilinearForm(bv, bv)
+    Kt = cross.assemble_tensor("gradient", "gradient", np.ascontiguousarray(At))
+    out["nh_vp1"] = dict(p=mv.p, t=mv.t, X=X1, W=W1, u=u, residual=np.asarray(res).copy(),
+                         **csr_parts(Kt))
+
+    # --- linear form f.v on P2 with per-(E,Q) f ---
+    @sk.LinearForm
+    def load(v, w):
+        return dot(w.f, v)
+
+    fq = rng.standard_normal(b2.dx.shape)
+    rhs = sk.asm(load, b2, f=fq)
+    out["p2_load"] = dict(p=m2.p, t=m2.t, X=X4, W=W4, f=fq, rhs=np.asarray(rhs).copy())
+
+    os.makedirs(HERE, exist_ok=True)
+    for name, arrays in out.items():
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+        print(f"{name}: {os.path.getsize(path) / 1024:.1f} KiB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,143 @@
+"""Pin the CPU oracle against outputs of the reference itself (tests/golden).
+
+Index structures must match exactly; values are compared bit for bit where
+the oracle keeps the reference's summation order (serial paths), otherwise to
+1e-14 relative to the largest entry.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_golden
+
+X1 = np.array([[.25], [.25], [.25]])
+W1 = np.array([1 / 6])
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_mesh_generation_matches_reference():
+    g = load_golden("p1_laplace")
+    p, t = O.mesh_tet_tensor(*(np.linspace(0, 1, 5),) * 3)
+    assert np.array_equal(p, g["p"]) and np.array_equal(t, g["t"])
+
+
+def test_p2_mesh_first_seen_edges():
+    g = load_golden("p2_aniso")
+    p2, t2 = O.mesh_tet2_from_mesh(g["pj"], g["t0"])
+    assert np.array_equal(t2, g["t"])
+    assert np.array_equal(p2, g["p"])
+
+
+def test_p1_laplace_bit_exact():
+    g = load_golden("p1_laplace")
+    b = O.make_basis(g["p"], g["t"], False, quadrature=(X1, W1))
+    data, indptr, indices = O.bilinear_assemble(b, gradient=1.0)
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert np.array_equal(data, g["data"])
+    kd, _, _ = O.bilinear_assemble(b, gradient=g["kappa"][:, None])
+    assert np.array_equal(kd, g["kdata"])
+
+
+def test_p1_helmholtz_default_rule():
+    g = load_golden("p1_helmholtz")
+    b = O.make_basis(g["p"], g["t"], False)
+    assert np.array_equal(b.X, g["X"]) and np.array_equal(b.W, g["W"])
+    assert np.array_equal(b.dx, g["dx"]) and np.array_equal(b.grad, g["grads"])
+    data, indptr, indices = O.bilinear_assemble(b, value=g["s"], gradient=g["c"])
+    assert np.array_equal(indices, g["indices"])
+    assert rel(data, g["data"]) < 1e-14
+
+
+def test_p2_aniso_cross_tensor():
+    g = load_golden("p2_aniso")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    assert np.array_equal(b.dx, g["dx"]) and np.array_equal(b.grad, g["grads"])
+    assert np.array_equal(b.det, g["det"]) and np.array_equal(b.cond, g["cond"])
+    E, Q = b.dx.shape
+    T = O.anisotropic_tensor(np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q)), (E, Q))
+    data, indptr, indices = O.cross_gradient_tensor_assemble(b, T)
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert np.array_equal(data, g["data"])
+    Tn = O.anisotropic_tensor(np.broadcast_to(np.moveaxis(g["Ans"], (1, 2), (0, 1))[..., None], (3, 3, E, Q)), (E, Q))
+    dn, _, _ = O.cross_gradient_tensor_assemble(b, Tn)
+    assert np.array_equal(dn, g["ns_data"])
+
+
+def test_p2_threaded_colored_close():
+    g = load_golden("p2_aniso")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    E, Q = b.dx.shape
+    T = O.anisotropic_tensor(np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q)), (E, Q))
+    data, _, _ = O.cross_gradient_tensor_assemble(b, T, threads=4)
+    assert rel(data, g["data"]) < 1e-14
+
+
+def test_p2_laplace_default_keast():
+    g = load_golden("p2_laplace_default")
+    b = O.make_basis(g["p"], g["t"], True)
+    assert np.array_equal(b.X, g["X"]) and np.array_equal(b.W, g["W"])
+    data, indptr, indices = O.bilinear_assemble(b, gradient=1.0)
+    assert np.array_equal(indices, g["indices"])
+    assert np.array_equal(data, g["data"])
+
+
+def test_n1_maxwell():
+    g = load_golden("n1_maxwell")
+    nb = O.make_n1_basis(g["p"], g["t"])
+    assert np.array_equal(nb.edges, g["edges"])
+    assert np.array_equal(nb.element_dofs, g["element_edges"])
+    assert np.array_equal(nb.signs, g["signs"])
+    assert np.array_equal(nb.detJ, g["detJ"])
+    data, indptr, indices = O.n1_assemble_maxwell(nb, 1.0, (1.0 / g["mu"])[:, None])
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert rel(data, g["data"]) < 1e-14
+
+
+def test_vector_p1_elasticity_terms():
+    g = load_golden("vp1_elasticity")
+    b = O.make_basis(g["p"], g["t"], False, comp=3, quadrature=(X1, W1))
+    shp = b.dx.shape
+    data, indptr, indices = O.bilinear_assemble(
+        b, symmetric_gradient=np.full(shp, 2.0), divergence=np.full(shp, 10.0), value=np.full(shp, 0.5))
+    assert np.array_equal(indices, g["indices"])
+    assert np.array_equal(data, g["data"])
+
+
+def test_neo_hookean_pieces():
+    g = load_golden("nh_vp1")
+    b = O.make_basis(g["p"], g["t"], False, comp=3, quadrature=(X1, W1))
+    Gu = O.displacement_gradient(b, g["u"])
+    P = O.nh_first_piola(Gu, 1.0, 10.0)
+    r = O.linear_assemble(b, gradient=P)
+    assert rel(r, g["residual"]) < 1e-14
+    A = O.nh_tangent(Gu, 1.0, 10.0)
+    data, indptr, indices = O.cross_gradient_tensor_assemble(b, A)
+    assert np.array_equal(indices, g["indices"])
+    assert rel(data, g["data"]) < 1e-13
+
+
+def test_p2_load_vector():
+    g = load_golden("p2_load")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    r = O.linear_assemble(b, value=g["f"][..., None])
+    assert np.array_equal(r, g["rhs"])
+
+
+def test_repeated_corner_rejected():
+    t = np.array([[0], [1], [1], [2]])
+    with pytest.raises(ValueError, match="repeats a corner"):
+        O.edge_topology(t)
+
+
+def test_geometry_validation_messages():
+    p = np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 0.]])  # flat tet
+    t = np.array([[0], [1], [2], [3]])
+    with pytest.raises(O.GeometryError, match="cell=0, quadrature_point=0.*near_singular"):
+        O.make_basis(p, t, False)
+    # tiny but valid (scale-aware tolerance) is accepted
+    ps = np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 1.]]) * 1e-50
+    b = O.make_basis(ps, t, False)
+    assert b.det[0, 0] > 0
