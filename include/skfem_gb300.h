@@ -1,0 +1,239 @@
+/*
+ * skfem_gb300.h -- C ABI of the GB300 finite-element assembly backend.
+ *
+ * A drop-in for the native layer (`_skfn`, pybind11) that scikit-fem-native's
+ * Python wrappers call on the matrix-assembly path.  Every entry point below
+ * names the reference interface it replaces (paths relative to the reference
+ * project root).
+ *
+ * Conventions
+ *  - Plain C: pointers and sizes only.  `d_` arguments are device pointers
+ *    (CUDA global memory), `h_` arguments host pointers.
+ *  - Every call returns an int status (SKG_OK = 0); the message of the last
+ *    failure on the calling thread is available from skg_last_error().  No
+ *    C++ exception crosses this boundary.
+ *  - Work is enqueued on the caller's stream (`stream` is a cudaStream_t,
+ *    NULL = legacy default stream).  Calls documented as "synchronous" wait
+ *    for their own work before returning (setup paths that report data-
+ *    dependent errors).
+ *  - Outputs are caller-owned.  Handles (skg_pattern) own their device
+ *    memory until destroyed.
+ *  - Connectivity is int32 on the device; sizes are int64.
+ *  - Arrays use the reference's own layouts: mesh coordinates (3, npts),
+ *    mesh connectivity (nodes, elements) node-major like `mesh.t`, per-point
+ *    coefficients (elements, points) like `basis.dx`.
+ *  - Element-matrix sums into CSR slots are made in a fixed order (element
+ *    index ascending, then local index), so repeated calls give identical
+ *    bits.
+ */
+#ifndef SKFEM_GB300_H
+#define SKFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKG_OK 0
+#define SKG_EINVAL 1    /* invalid argument / shape (the reference raises ValueError) */
+#define SKG_ENOMEM 2    /* device allocation failed */
+#define SKG_ECUDA 3     /* CUDA runtime error */
+#define SKG_EGEOM 4     /* invalid element geometry (ValueError in the reference) */
+#define SKG_ERANGE 5    /* index out of range (ValueError in the reference) */
+#define SKG_EUNSUPPORTED 6
+
+/* Precision of the element contraction. */
+#define SKG_FP64 0          /* FP64 end to end */
+#define SKG_SPLIT_FP32 1    /* FP32 hi+lo split products, FP32 accumulation; FP64 geometry and slot sums */
+
+/* Library version (major*10000 + minor*100 + patch). */
+int skg_version(void);
+
+/* Message of the last failure on the calling thread ("" when none). */
+const char *skg_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Sparsity pattern.                                                    */
+/* Replaces the pattern build of BilinearFormAssembler                  */
+/* (cpp/src/assembly/bilinear_form_assembler.cpp:111-120),              */
+/* CrossBilinearAssembler (cpp/src/assembly/cross_bilinear_assembler.cpp */
+/* :311-320) and build_edge_csr_pattern                                 */
+/* (cpp/src/assembly/edge_topology.cpp:86-154): per-row sorted unique   */
+/* columns, identical indptr/indices.  The handle also keeps, per row,  */
+/* the (element, local row) incidences in ascending order, which fixes  */
+/* the summation order of every assembly on this pattern.               */
+
+typedef struct skg_pattern skg_pattern;
+
+/* d_row_dofs (n_elements, row_local), d_col_dofs (n_elements, col_local),
+ * element-major (the reference's `dofs (E, nodes, components)`).  n_rows /
+ * n_cols: matrix shape (rows must exceed every row dof).  With d_col_dofs
+ * NULL only the row incidence lists are built (nnz = 0): the handle then
+ * serves vector (linear-form) assembly.  Synchronous. */
+int skg_pattern_create(const int32_t *d_row_dofs, const int32_t *d_col_dofs,
+                       int64_t n_elements, int32_t row_local, int32_t col_local,
+                       int64_t n_rows, int64_t n_cols, void *stream,
+                       skg_pattern **out);
+int skg_pattern_destroy(skg_pattern *pattern);
+/* nnz and shape of the pattern. */
+int skg_pattern_info(const skg_pattern *pattern, int64_t *nnz, int64_t *n_rows,
+                     int64_t *n_cols);
+/* Copy the CSR structure out: d_indptr (n_rows+1) int64, d_indices (nnz) int32.
+ * Either may be NULL.  (BilinearFormAssembler.indptr / .indices views.) */
+int skg_pattern_export(const skg_pattern *pattern, int64_t *d_indptr,
+                       int32_t *d_indices, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Geometry tabulation.                                                 */
+/* Replaces tabulate_basis_geometry                                     */
+/* (cpp/src/assembly/basis_geometry.cpp:49-209): per (element, point)   */
+/* isoparametric Jacobian, scale-aware determinant tolerance, cofactor  */
+/* inverse, condition number, dx = |det| w, physical gradients and      */
+/* points, then the reference's validation (first failing element in    */
+/* element order; near-singular before orientation change).             */
+/* Tables (host, copied): shape (Q,nodes), refgrad (Q,nodes,3),         */
+/* gshape (Q,gnodes), grefgrad (Q,gnodes,3), W (Q).  Output arrays      */
+/* (device, any may be NULL): shape (E,Q,nodes), grad (E,Q,nodes,3),    */
+/* dx (E,Q), x (E,Q,3), det, tol, cond (E,Q).  Synchronous; on a        */
+/* validation failure returns SKG_EGEOM with h_bad = {cell, point,      */
+/* reason (1 near_singular_or_non_finite, 2 orientation_change)} and    */
+/* the message formatted as the reference's.                            */
+int skg_tabulate_geometry(const double *d_p, int64_t npts, const int32_t *d_t,
+                          int32_t gnodes, int64_t n_elements, int32_t nq,
+                          int32_t nodes, const double *h_shape,
+                          const double *h_refgrad, const double *h_gshape,
+                          const double *h_grefgrad, const double *h_w,
+                          double *d_shape, double *d_grad, double *d_dx,
+                          double *d_x, double *d_det, double *d_tol,
+                          double *d_cond, int64_t *h_bad, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Nodal H1 bilinear assembly from tabulated geometry.                  */
+/* Replaces BilinearFormAssembler.assemble                              */
+/* (cpp/src/assembly/bilinear_form_assembler.cpp:39-105):               */
+/*   K[a c, b d] += w (v N_a N_b + g grad N_a . grad N_b) delta_cd      */
+/*                  + 1/2 s (...) + div (...)                            */
+/* d_dofs (E, nodes*comp); shape (E,Q,nodes), grad (E,Q,nodes,3),       */
+/* w (E,Q); coefficients (E,Q) or NULL (at least one required).         */
+/* d_values (nnz) is overwritten.  d_scratch: NULL, or E*L*L doubles    */
+/* (L = nodes*comp) for the element matrices.                            */
+int skg_h1_assemble_tabulated(const skg_pattern *pattern, const int32_t *d_dofs,
+                              int64_t n_elements, int32_t nodes, int32_t comp,
+                              int32_t nq, const double *d_shape,
+                              const double *d_grad, const double *d_w,
+                              const double *d_value, const double *d_gradient,
+                              const double *d_symgrad, const double *d_div,
+                              double *d_values, double *d_scratch, void *stream);
+
+/* Test x trial assembly with a full tensor coefficient on gradients.
+ * Replaces CrossBilinearAssembler.assemble(coefficient, "gradient",
+ * "gradient") (cpp/src/assembly/cross_bilinear_assembler.cpp:55-107,
+ * 207-247; cpp/include/native_fem/cross_contraction.hpp:67-84) for one shared
+ * basis: K[a r, b c] += w sum_ij gradN_a[i] C[e,q,r,i,c,j] gradN_b[j].
+ * d_coef (E,Q,comp,3,comp,3). */
+int skg_h1_assemble_tensor_tabulated(const skg_pattern *pattern,
+                                     const int32_t *d_dofs, int64_t n_elements,
+                                     int32_t nodes, int32_t comp, int32_t nq,
+                                     const double *d_grad, const double *d_w,
+                                     const double *d_coef, double *d_values,
+                                     double *d_scratch, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Fused scalar P1/P2 assembly straight from mesh coordinates.          */
+/* Replaces the whole `asm(BilinearForm, Basis)` chain for             */
+/*   w.kappa * ddot(grad u, grad v)      (coef_kind 0: scalar)           */
+/*   dot(mul(w.A, grad u), grad v)       (coef_kind 1: 3x3 tensor)       */
+/* on affine tetrahedra (python/skfemntv/forms.py:276-374 ->            */
+/* bilinear_form.py:13-99 / 102-367 -> the two native assemblers):      */
+/* geometry, element contraction and the fixed-order CSR sum in one     */
+/* pass, without tabulated per-point arrays.                            */
+/*  d_p (3, npts); d_t (nodes, E) with nodes 4 (P1) or 10 (P2, the      */
+/*  mesh must be affine: edge nodes at midpoints); d_dofs (E, nodes)    */
+/*  scalar DOFs.  h_X (3,Q), h_W (Q): the quadrature rule.              */
+/*  coef_kind 0: d_coef per element (E) or NULL for 1.                   */
+/*  coef_kind 1: d_coef per element (E,3,3), row-major A[i][j].          */
+/*  coef_kind 2: d_coef per element, component-first (3,3,E) (the        */
+/*  reference's public (3,3,E,Q) layout with the point axis dropped).     */
+/*  precision: SKG_FP64 or SKG_SPLIT_FP32.                               */
+/*  d_values (nnz) is overwritten.                                       */
+int skg_h1_assemble_affine(const skg_pattern *pattern, const double *d_p,
+                           int64_t npts, const int32_t *d_t, int32_t nodes,
+                           int64_t n_elements, const int32_t *d_dofs,
+                           int32_t nq, const double *h_X, const double *h_W,
+                           int32_t coef_kind, const double *d_coef,
+                           int32_t precision, double *d_values, void *stream);
+
+/* Same as skg_h1_assemble_affine, and writes the duration of its two
+ * kernels (element pass, row pass) in milliseconds to h_kernel_ms[0..1],
+ * measured with CUDA events on `stream`.  Synchronous. */
+int skg_h1_assemble_affine_profiled(const skg_pattern *pattern, const double *d_p,
+                                    int64_t npts, const int32_t *d_t, int32_t nodes,
+                                    int64_t n_elements, const int32_t *d_dofs,
+                                    int32_t nq, const double *h_X, const double *h_W,
+                                    int32_t coef_kind, const double *d_coef,
+                                    int32_t precision, double *d_values,
+                                    float *h_kernel_ms, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Nedelec N1 (lowest-order H(curl)) on affine tets.                    */
+
+/* First-seen oriented edge numbering.  Replaces build_oriented_edge_topology
+ * (cpp/src/assembly/edge_topology.cpp:30-84) and MeshTet2.from_mesh's edge
+ * numbering (python/skfemntv/basis.py:644-658): global edge ids in cell-
+ * major, local-edge-major first-seen order, key = ascending vertex pair,
+ * sign +1 when the local edge runs from the smaller vertex.
+ * d_t (4, E); outputs d_edges (2, 6E capacity, packed row stride 6E),
+ * d_elem_edges (6, E), d_signs (6, E) int8.  *h_n_edges receives the edge
+ * count.  A cell that repeats a corner vertex gives SKG_EINVAL with
+ * h_bad_cell set.  Synchronous. */
+int skg_edge_topology(const int32_t *d_t, int64_t n_elements, int32_t *d_edges,
+                      int32_t *d_elem_edges, int8_t *d_signs, int64_t *h_n_edges,
+                      int64_t *h_bad_cell, void *stream);
+
+/* TetN1 Maxwell assembly K = sum_q dx (mass v_a.v_b + curl c_a.c_b).
+ * Replaces TetN1Assembler.assemble_maxwell / assemble_mass /
+ * assemble_curl_curl (python/skfemntv/hcurl_assembler.py:160-215 with
+ * integrate_tet_n1, cpp/src/assembly/edge_topology.cpp:156-233, and the
+ * np.add.at scatter, hcurl_assembler.py:94-97), straight from coordinates:
+ * affine Jacobian, covariant Piola values J^-T phi, curls J c / det J,
+ * orientation signs.  d_mass / d_curl: per element (E) or NULL for 1;
+ * include flags select the terms.  h_X (3,Q), h_W (Q).  pattern built on
+ * d_elem_edges^T.  d_values (nnz) overwritten. */
+int skg_n1_assemble(const skg_pattern *pattern, const double *d_p, int64_t npts,
+                    const int32_t *d_t, const int32_t *d_elem_edges,
+                    const int8_t *d_signs, int64_t n_elements, int32_t nq,
+                    const double *h_X, const double *h_W, const double *d_mass,
+                    const double *d_curl, int32_t include_mass,
+                    int32_t include_curl, int32_t precision, double *d_values,
+                    void *stream);
+
+/* Per-point coefficients: d_mass / d_curl (E, Q) (not NULL); the explicit
+ * quadrature loop of integrate_tet_n1 (edge_topology.cpp:156-233) on the
+ * mapped basis computed in the kernel. */
+int skg_n1_assemble_pointwise(const skg_pattern *pattern, const double *d_p,
+                              int64_t npts, const int32_t *d_t, const int8_t *d_signs,
+                              int64_t n_elements, int32_t nq, const double *h_X,
+                              const double *h_W, const double *d_mass,
+                              const double *d_curl, int32_t include_mass,
+                              int32_t include_curl, double *d_values, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Linear forms.  Replaces LinearFormAssembler.assemble                 */
+/* (cpp/src/assembly/linear_form_assembler.cpp:41-154):                 */
+/*   r[dof(a,c)] += sum_q w (f_c N_a + G_cj dN_a/dx_j)                  */
+/* value (E,Q,comp) or NULL, gradient (E,Q,comp,3) or NULL.  The sum    */
+/* per DOF is made in element order (deterministic).  d_out (n_dofs).   */
+int skg_linear_assemble_tabulated(const skg_pattern *pattern,
+                                  const int32_t *d_dofs, int64_t n_elements,
+                                  int32_t nodes, int32_t comp, int32_t nq,
+                                  const double *d_shape, const double *d_grad,
+                                  const double *d_w, const double *d_value,
+                                  const double *d_gradient, double *d_out,
+                                  void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKFEM_GB300_H */

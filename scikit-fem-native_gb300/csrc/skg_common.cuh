@@ -1,0 +1,148 @@
+// Shared host/device infrastructure of the GB300 assembly backend:
+// status handling (no exception crosses the C ABI), stream-ordered device
+// buffers, launch helpers and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "skfem_gb300.h"
+
+namespace skg {
+
+// ---------------------------------------------------------------- errors
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+[[noreturn]] inline void fail(int code, const std::string &msg) { throw Error(code, msg); }
+
+inline void check_cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            fail(SKG_ENOMEM, std::string(what) + ": out of device memory");
+        }
+        fail(SKG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+#define SKG_CUDA(call) ::skg::check_cuda((call), #call)
+#define SKG_LAUNCH_CHECK(name) ::skg::check_cuda(cudaGetLastError(), name)
+
+inline void require(bool ok, const std::string &msg, int code = SKG_EINVAL) {
+    if (!ok) fail(code, msg);
+}
+
+// Runs `body` and converts any failure into a status code + message.
+template <class F>
+int guarded(F &&body) {
+    try {
+        body();
+        set_last_error("");
+        return SKG_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return SKG_ENOMEM;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return SKG_ECUDA;
+    } catch (...) {
+        set_last_error("unknown failure");
+        return SKG_ECUDA;
+    }
+}
+
+// ---------------------------------------------------------------- buffers
+
+// Device buffer.  Temporaries are stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the call's stream); buffers owned by handles, which may
+// outlive the stream that created them, use plain cudaMalloc / cudaFree.
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t n = 0;
+    cudaStream_t stream = nullptr;
+    bool async = false;
+    DevBuf() = default;
+    DevBuf(size_t count, cudaStream_t s) : n(count), stream(s), async(true) {
+        if (count) SKG_CUDA(cudaMallocAsync((void **)&ptr, count * sizeof(T), s));
+    }
+    static DevBuf owned(size_t count) {
+        DevBuf b;
+        b.n = count;
+        if (count) SKG_CUDA(cudaMalloc((void **)&b.ptr, count * sizeof(T)));
+        return b;
+    }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), n(o.n), stream(o.stream), async(o.async) {
+        o.ptr = nullptr; o.n = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        release();
+        ptr = o.ptr; n = o.n; stream = o.stream; async = o.async;
+        o.ptr = nullptr; o.n = 0;
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) {
+            if (async) cudaFreeAsync(ptr, stream);
+            else cudaFree(ptr);
+        }
+        ptr = nullptr;
+        n = 0;
+    }
+    T *get() const { return ptr; }
+};
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffffLL) g = 0x7fffffffLL;
+    return (unsigned)g;
+}
+
+// Exclusive scan of n int32 counts into out[0..n] (out[n] = total) on the
+// stream; returns nothing (total read by the caller if needed).  Counts and
+// totals must stay below 2^31.
+void exclusive_scan_i32(const int32_t *d_in, int32_t *d_out, int64_t n, cudaStream_t s);
+
+// ---------------------------------------------------------------- device
+
+__device__ __forceinline__ int lower_bound_i32(const int32_t *b, int n, int32_t key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (b[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+}  // namespace skg
+
+// Pattern handle (defined here so every translation unit sees the layout).
+struct skg_pattern {
+    int64_t n_elements = 0, n_rows = 0, n_cols = 0, nnz = 0;
+    int32_t row_local = 0, col_local = 0;
+    skg::DevBuf<int32_t> row_dofs;  // (E, row_local) copy
+    skg::DevBuf<int32_t> col_dofs;  // (E, col_local) copy
+    skg::DevBuf<int32_t> indptr;    // (n_rows+1)
+    skg::DevBuf<int32_t> indices;   // (nnz)
+    skg::DevBuf<int32_t> inc_ptr;   // (n_rows+1) incidences per row
+    skg::DevBuf<int32_t> inc;       // (E*row_local) e*row_local + i, ascending per row
+};

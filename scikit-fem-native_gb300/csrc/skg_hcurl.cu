@@ -1,0 +1,339 @@
+// Lowest-order Nedelec (N1, Whitney edge) elements on affine tetrahedra.
+//
+// Edge topology: the reference numbers global edges in first-seen order
+// while walking cells and their local edges (0,1),(1,2),(2,0),(0,3),(1,3),
+// (2,3) (cpp/src/assembly/edge_topology.cpp:30-84).  That sequential rule is
+// reproduced exactly in parallel: every (cell, local edge) item is inserted
+// into a device hash table keyed by its ascending vertex pair, keeping the
+// smallest item index (its first occurrence); items that are their key's
+// first occurrence are flagged, an exclusive scan of the flags in item order
+// gives each first occurrence its edge id, and every item takes the id of
+// its key's first occurrence.
+//
+// Assembly (TetN1Assembler.assemble_maxwell, python/skfemntv/
+// hcurl_assembler.py:160-215): with barycentric gradients g_k = b_k / det J
+// (b_k rows of adj J, b_0 = -(b_1+b_2+b_3)), the mapped basis of directed
+// edge a = (i, j) is J^-T phi_a = lambda_i g_j - lambda_j g_i and its curl
+// J c_a / det J (c_a = 2 ghat_i x ghat_j), each times the orientation sign
+// (python/skfemntv/hcurl_basis.py:353-364, _hcurl_mapping.py:46-97).  For
+// coefficients constant per element the quadrature sum collapses to
+//   M_ab = mass * s_a s_b sum_{k,l} (b_k.b_l / |det|) Tm^{kl}_ab,
+//   Tm^{kl}_ab = sum_q w_q d^k_a(xi_q) d^l_b(xi_q)   (host table, per rule)
+//   C_ab = curl * s_a s_b (sum_q w_q) (J c_a).(J c_b) / |det|.
+// Per-point coefficients use the explicit quadrature loop.  The 6x6 element
+// matrices then go through the same fixed-order row-owner gather as H1.
+#include <climits>
+#include <vector>
+
+#include "skg_common.cuh"
+
+namespace skg {
+
+void gather_element_matrices(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s);
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+    return x;
+}
+
+__constant__ int kEdge[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+
+constexpr unsigned long long kEmpty = ~0ull;
+
+__global__ void k_edge_insert(const int32_t *__restrict__ t, int64_t ne, unsigned long long *keys,
+                              int32_t *first, uint64_t mask, int32_t *bad_cell, int32_t *overflow) {
+    const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= ne * 6) return;
+    const int64_t cell = item / 6;
+    const int l = (int)(item % 6);
+    if (l == 0) {
+        int32_t v[4];
+        for (int k = 0; k < 4; ++k) v[k] = t[k * ne + cell];
+        for (int f = 0; f < 4; ++f)
+            for (int g = f + 1; g < 4; ++g)
+                if (v[f] == v[g]) atomicMin(bad_cell, (int32_t)cell);
+    }
+    const int32_t a = t[kEdge[l][0] * ne + cell], b = t[kEdge[l][1] * ne + cell];
+    const uint32_t lo = (uint32_t)min(a, b), hi = (uint32_t)max(a, b);
+    const unsigned long long key = ((unsigned long long)lo << 32) | hi;
+    uint64_t h = mix64(key) & mask;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long prev = atomicCAS(&keys[h], kEmpty, key);
+        if (prev == kEmpty || prev == key) {
+            atomicMin(&first[h], (int32_t)item);
+            return;
+        }
+        h = (h + 1) & mask;
+    }
+    *overflow = 1;
+}
+
+__global__ void k_edge_flag(const int32_t *__restrict__ t, int64_t ne, const unsigned long long *keys,
+                            const int32_t *first, uint64_t mask, int32_t *flag, int32_t *slot_of) {
+    const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= ne * 6) return;
+    const int64_t cell = item / 6;
+    const int l = (int)(item % 6);
+    const int32_t a = t[kEdge[l][0] * ne + cell], b = t[kEdge[l][1] * ne + cell];
+    const uint32_t lo = (uint32_t)min(a, b), hi = (uint32_t)max(a, b);
+    const unsigned long long key = ((unsigned long long)lo << 32) | hi;
+    uint64_t h = mix64(key) & mask;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+        if (keys[h] == key) break;
+        h = (h + 1) & mask;
+    }
+    slot_of[item] = (int32_t)h;
+    flag[item] = first[h] == (int32_t)item ? 1 : 0;
+}
+
+__global__ void k_edge_emit(const int32_t *__restrict__ t, int64_t ne, const int32_t *first,
+                            const int32_t *slot_of, const int32_t *flag, const int32_t *scan, int32_t *edges,
+                            int32_t *elem_edges, int8_t *signs) {
+    const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= ne * 6) return;
+    const int64_t cell = item / 6;
+    const int l = (int)(item % 6);
+    const int32_t a = t[kEdge[l][0] * ne + cell], b = t[kEdge[l][1] * ne + cell];
+    const int32_t id = scan[first[slot_of[item]]];
+    elem_edges[l * ne + cell] = id;
+    signs[l * ne + cell] = (int8_t)(a < b ? 1 : -1);
+    if (flag[item]) {
+        edges[id] = min(a, b);
+        edges[ne * 6 + id] = max(a, b);
+    }
+}
+
+// ---------------------------------------------------------------- assembly
+
+struct N1Table {
+    double Tm[6][6][4];  // [a][b][s*2+t], s/t index the support (i, j) of a / b
+    double wsum;
+};
+
+__device__ __forceinline__ void n1_geometry(const double *__restrict__ p, int64_t npts,
+                                            const int32_t *__restrict__ t, int64_t ne, int64_t e, double J[9],
+                                            double b[4][3], double &det) {
+    int32_t v0 = t[e], v1 = t[ne + e], v2 = t[2 * ne + e], v3 = t[3 * ne + e];
+    // out-of-range vertex ids never reach memory: the element becomes NaN
+    const bool ok = v0 >= 0 && v0 < npts && v1 >= 0 && v1 < npts && v2 >= 0 && v2 < npts && v3 >= 0 && v3 < npts;
+    if (!ok) v0 = v1 = v2 = v3 = 0;
+    const int32_t v[3] = {v1, v2, v3};
+    for (int i = 0; i < 3; ++i) {
+        const double x0 = p[i * npts + v0];
+        for (int r = 0; r < 3; ++r) J[i * 3 + r] = ok ? p[i * npts + v[r]] - x0 : __longlong_as_double(0x7ff8000000000000LL);
+    }
+    b[1][0] = J[4] * J[8] - J[5] * J[7];
+    b[1][1] = J[2] * J[7] - J[1] * J[8];
+    b[1][2] = J[1] * J[5] - J[2] * J[4];
+    b[2][0] = J[5] * J[6] - J[3] * J[8];
+    b[2][1] = J[0] * J[8] - J[2] * J[6];
+    b[2][2] = J[2] * J[3] - J[0] * J[5];
+    b[3][0] = J[3] * J[7] - J[4] * J[6];
+    b[3][1] = J[1] * J[6] - J[0] * J[7];
+    b[3][2] = J[0] * J[4] - J[1] * J[3];
+    det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
+    for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
+}
+
+// Reference curls c_a = 2 ghat_i x ghat_j for the directed local edges.
+__constant__ double kRefCurl[6][3] = {{0, -2, 2}, {0, 0, 2}, {-2, 0, 2}, {-2, 2, 0}, {0, -2, 0}, {2, 0, 0}};
+
+// Thread per element: Ke (E, 6, 6).  mass/curl: per element (qstride 0) or
+// per point (qstride 1, explicit quadrature loop); NULL = 1.
+template <bool SPLIT>
+__global__ void k_n1_element(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+                             const int8_t *__restrict__ signs, int nq, const double *__restrict__ Xq,
+                             const double *__restrict__ Wq, N1Table tab, const double *__restrict__ mass,
+                             const double *__restrict__ curl, int qstride, int inc_mass, int inc_curl,
+                             double *__restrict__ Ke) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    double J[9], b[4][3], det;
+    n1_geometry(p, npts, t, ne, e, J, b, det);
+    const double adet = fabs(det), inv = 1.0 / adet;
+    double s[6];
+    for (int a = 0; a < 6; ++a) s[a] = (double)signs[a * ne + e];
+    double Jc[6][3];
+    for (int a = 0; a < 6; ++a)
+        for (int i = 0; i < 3; ++i)
+            Jc[a][i] = J[i * 3 + 0] * kRefCurl[a][0] + J[i * 3 + 1] * kRefCurl[a][1] + J[i * 3 + 2] * kRefCurl[a][2];
+    double K[6][6];
+    if (qstride == 0) {
+        const double mu = inc_mass ? (mass ? mass[e] : 1.0) : 0.0;
+        const double nu = inc_curl ? (curl ? curl[e] : 1.0) : 0.0;
+        double Gm[4][4];
+        for (int k = 0; k < 4; ++k)
+            for (int l = 0; l < 4; ++l) Gm[k][l] = (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]) * inv;
+        for (int a = 0; a < 6; ++a)
+            for (int c = a; c < 6; ++c) {
+                const int ai = kEdge[a][0], aj = kEdge[a][1], ci = kEdge[c][0], cj = kEdge[c][1];
+                const int ka[2] = {ai, aj}, kc[2] = {ci, cj};
+                double m = 0.;
+                for (int u = 0; u < 2; ++u)
+                    for (int v = 0; v < 2; ++v) m += Gm[ka[u]][kc[v]] * tab.Tm[a][c][u * 2 + v];
+                const double cc = (Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2]) * inv * tab.wsum;
+                const double val = s[a] * s[c] * (mu * m + nu * cc);
+                K[a][c] = val;
+                K[c][a] = val;
+            }
+    } else {
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 6; ++c) K[a][c] = 0.;
+        for (int q = 0; q < nq; ++q) {
+            const double x = Xq[q], y = Xq[nq + q], z = Xq[2 * nq + q];
+            const double lam[4] = {1.0 - x - y - z, x, y, z};
+            const double dx = adet * Wq[q];
+            const double mu = inc_mass ? (mass ? mass[e * nq + q] : 1.0) : 0.0;
+            const double nu = inc_curl ? (curl ? curl[e * nq + q] : 1.0) : 0.0;
+            double phi[6][3];
+            for (int a = 0; a < 6; ++a) {
+                const int i = kEdge[a][0], j = kEdge[a][1];
+                for (int d = 0; d < 3; ++d) phi[a][d] = (lam[i] * b[j][d] - lam[j] * b[i][d]) / det;
+            }
+            for (int a = 0; a < 6; ++a)
+                for (int c = 0; c < 6; ++c) {
+                    const double vv = phi[a][0] * phi[c][0] + phi[a][1] * phi[c][1] + phi[a][2] * phi[c][2];
+                    const double ccv = (Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2]) / (det * det);
+                    K[a][c] += dx * (mu * vv + nu * ccv) * s[a] * s[c];
+                }
+        }
+    }
+    double *out = Ke + e * 36;
+    for (int a = 0; a < 6; ++a)
+        for (int c = 0; c < 6; ++c) {
+            out[a * 6 + c] = K[a][c];
+        }
+}
+
+}  // namespace
+}  // namespace skg
+
+using namespace skg;
+
+extern "C" int skg_edge_topology(const int32_t *d_t, int64_t ne, int32_t *d_edges, int32_t *d_elem_edges,
+                                 int8_t *d_signs, int64_t *h_n_edges, int64_t *h_bad_cell, void *stream) {
+    return guarded([&] {
+        require(ne >= 0 && (ne == 0 || (d_t && d_edges && d_elem_edges && d_signs)), "invalid edge topology arguments");
+        require(ne * 6 < INT_MAX, "mesh too large for 32-bit edge items");
+        if (h_bad_cell) *h_bad_cell = -1;
+        if (h_n_edges) *h_n_edges = 0;
+        if (ne == 0) return;
+        cudaStream_t s = as_stream(stream);
+        const int64_t items = ne * 6;
+        uint64_t cap = 64;
+        while (cap < (uint64_t)(2 * items)) cap <<= 1;
+        DevBuf<unsigned long long> keys(cap, s);
+        DevBuf<int32_t> first(cap, s), flag(items + 1, s), slot_of(items, s), scan(items + 1, s), misc(2, s);
+        SKG_CUDA(cudaMemsetAsync(keys.get(), 0xff, cap * 8, s));
+        SKG_CUDA(cudaMemsetAsync(first.get(), 0x7f, cap * 4, s));
+        const int32_t init[2] = {INT_MAX, 0};
+        SKG_CUDA(cudaMemcpyAsync(misc.get(), init, 8, cudaMemcpyHostToDevice, s));
+        k_edge_insert<<<grid_for(items, 256), 256, 0, s>>>(d_t, ne, keys.get(), first.get(), cap - 1, misc.get(),
+                                                          misc.get() + 1);
+        SKG_LAUNCH_CHECK("edge_insert");
+        int32_t h_misc[2];
+        SKG_CUDA(cudaMemcpyAsync(h_misc, misc.get(), 8, cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        if (h_misc[0] != INT_MAX) {
+            if (h_bad_cell) *h_bad_cell = h_misc[0];
+            fail(SKG_EINVAL, "cell " + std::to_string(h_misc[0]) + " repeats a corner vertex");
+        }
+        require(h_misc[1] == 0, "edge hash table overflow", SKG_ECUDA);
+        k_edge_flag<<<grid_for(items, 256), 256, 0, s>>>(d_t, ne, keys.get(), first.get(), cap - 1, flag.get(),
+                                                        slot_of.get());
+        SKG_LAUNCH_CHECK("edge_flag");
+        exclusive_scan_i32(flag.get(), scan.get(), items, s);
+        k_edge_emit<<<grid_for(items, 256), 256, 0, s>>>(d_t, ne, first.get(), slot_of.get(), flag.get(), scan.get(),
+                                                        d_edges, d_elem_edges, d_signs);
+        SKG_LAUNCH_CHECK("edge_emit");
+        int32_t n_edges = 0;
+        SKG_CUDA(cudaMemcpyAsync(&n_edges, scan.get() + items, 4, cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        if (h_n_edges) *h_n_edges = n_edges;
+    });
+}
+
+static void n1_table(int nq, const double *X, const double *W, N1Table &tab) {
+    static const int edges[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+    // d^{k}_a: for directed edge (i, j), phi = lambda_i g_j - lambda_j g_i,
+    // so the coefficient of g_i is -lambda_j (support slot 0) and of g_j is
+    // lambda_i (support slot 1).
+    auto d = [&](int a, int slot, int q) {
+        const double x = X[q], y = X[nq + q], z = X[2 * nq + q];
+        const double lam[4] = {1.0 - x - y - z, x, y, z};
+        const int i = edges[a][0], j = edges[a][1];
+        return slot == 0 ? -lam[j] : lam[i];
+    };
+    tab.wsum = 0.;
+    for (int q = 0; q < nq; ++q) tab.wsum += W[q];
+    for (int a = 0; a < 6; ++a)
+        for (int c = 0; c < 6; ++c)
+            for (int u = 0; u < 2; ++u)
+                for (int v = 0; v < 2; ++v) {
+                    double acc = 0.;
+                    for (int q = 0; q < nq; ++q) acc += W[q] * d(a, u, q) * d(c, v, q);
+                    tab.Tm[a][c][u * 2 + v] = acc;
+                }
+}
+
+extern "C" int skg_n1_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
+                               const int32_t *d_elem_edges, const int8_t *d_signs, int64_t ne, int32_t nq,
+                               const double *h_X, const double *h_W, const double *d_mass, const double *d_curl,
+                               int32_t include_mass, int32_t include_curl, int32_t precision, double *d_values,
+                               void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(ne == pat->n_elements && pat->row_local == 6 && pat->col_local == 6, "mesh does not match the pattern");
+        require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+        require(d_p && d_t && d_signs, "mesh arrays are NULL");
+        (void)d_elem_edges;
+        cudaStream_t s = as_stream(stream);
+        N1Table tab;
+        n1_table(nq, h_X, h_W, tab);
+        DevBuf<double> Ke((size_t)ne * 36, s);
+        if (ne) {
+            if (precision == SKG_SPLIT_FP32)
+                k_n1_element<true><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, nullptr, nullptr,
+                                                                    tab, d_mass, d_curl, 0, include_mass, include_curl,
+                                                                    Ke.get());
+            else
+                k_n1_element<false><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, nullptr,
+                                                                     nullptr, tab, d_mass, d_curl, 0, include_mass,
+                                                                     include_curl, Ke.get());
+            SKG_LAUNCH_CHECK("n1_element");
+        }
+        gather_element_matrices(pat, Ke.get(), d_values, s);
+    });
+}
+
+// Per-point coefficients (mass/curl (E, Q)): explicit quadrature loop.
+extern "C" int skg_n1_assemble_pointwise(const skg_pattern *pat, const double *d_p, int64_t npts,
+                                         const int32_t *d_t, const int8_t *d_signs, int64_t ne, int32_t nq,
+                                         const double *h_X, const double *h_W, const double *d_mass,
+                                         const double *d_curl, int32_t include_mass, int32_t include_curl,
+                                         double *d_values, void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(ne == pat->n_elements && pat->row_local == 6 && pat->col_local == 6, "mesh does not match the pattern");
+        require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+        cudaStream_t s = as_stream(stream);
+        N1Table tab;
+        n1_table(nq, h_X, h_W, tab);
+        std::vector<double> xw(4 * (size_t)nq);
+        for (int i = 0; i < 3 * nq; ++i) xw[i] = h_X[i];
+        for (int q = 0; q < nq; ++q) xw[3 * nq + q] = h_W[q];
+        DevBuf<double> dxw(xw.size(), s);
+        SKG_CUDA(cudaMemcpyAsync(dxw.get(), xw.data(), xw.size() * 8, cudaMemcpyHostToDevice, s));
+        DevBuf<double> Ke((size_t)ne * 36, s);
+        if (ne) {
+            k_n1_element<false><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, dxw.get(),
+                                                                 dxw.get() + 3 * nq, tab, d_mass, d_curl, 1,
+                                                                 include_mass, include_curl, Ke.get());
+            SKG_LAUNCH_CHECK("n1_element_pointwise");
+        }
+        gather_element_matrices(pat, Ke.get(), d_values, s);
+    });
+}

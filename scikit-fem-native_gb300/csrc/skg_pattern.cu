@@ -1,0 +1,312 @@
+// CSR sparsity pattern on the device.
+//
+// Same result as the reference's per-row "collect, sort, unique" pattern
+// (cpp/src/assembly/bilinear_form_assembler.cpp:111-116 and the identical
+// rule in cross_bilinear_assembler.cpp and edge_topology.cpp:86-154), built
+// GPU-first:
+//   1. row incidence lists: for every row r the (element, local row) pairs
+//      whose row dof is r, as e*row_local+i, sorted ascending.  These lists
+//      are kept: every assembly on the pattern sums a slot's contributions
+//      in this order, which makes the result run-to-run deterministic;
+//   2. per row, one warp gathers the candidate columns of its incidences into
+//      shared memory, sorts them with a bitonic network and counts / writes
+//      the unique ones (rows with more candidates than fit in shared memory
+//      use a slower repeated-minimum extraction over global memory).
+#include <climits>
+
+#include "skg_common.cuh"
+
+namespace skg {
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_block(const int32_t *in, int32_t *out, int32_t *block_sums, int64_t n) {
+    __shared__ int32_t s[kScanBlock];
+    const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    const int32_t v = i < n ? in[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        int32_t t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = s[threadIdx.x] - v;  // exclusive
+    if (threadIdx.x == kScanBlock - 1 && block_sums) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void k_scan_add(int32_t *out, const int32_t *offsets, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += offsets[blockIdx.x];
+}
+
+__global__ void k_set_total(const int32_t *in, int32_t *out, int64_t n) {
+    // out[n] = out[n-1] + in[n-1]
+    if (threadIdx.x == 0 && blockIdx.x == 0) out[n] = n ? out[n - 1] + in[n - 1] : 0;
+}
+
+void scan_rec(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s) {
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb <= 1) {
+        k_scan_block<<<1, kScanBlock, 0, s>>>(in, out, nullptr, n);
+        SKG_LAUNCH_CHECK("scan");
+        return;
+    }
+    DevBuf<int32_t> sums(nb, s), offs(nb, s);
+    k_scan_block<<<(unsigned)nb, kScanBlock, 0, s>>>(in, out, sums.get(), n);
+    SKG_LAUNCH_CHECK("scan");
+    scan_rec(sums.get(), offs.get(), nb, s);
+    k_scan_add<<<(unsigned)nb, kScanBlock, 0, s>>>(out, offs.get(), n);
+    SKG_LAUNCH_CHECK("scan_add");
+}
+
+}  // namespace
+
+void exclusive_scan_i32(const int32_t *d_in, int32_t *d_out, int64_t n, cudaStream_t s) {
+    if (n > 0) scan_rec(d_in, d_out, n, s);
+    k_set_total<<<1, 32, 0, s>>>(d_in, d_out, n);
+    SKG_LAUNCH_CHECK("scan_total");
+}
+
+namespace {
+
+__global__ void k_check_range(const int32_t *v, int64_t n, int64_t hi, int32_t *err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t x = v[i];
+        if (x < 0 || x >= hi) atomicMin(err, (int32_t)(i < (int64_t)INT_MAX - 1 ? i : (int64_t)INT_MAX - 1));
+    }
+}
+
+__global__ void k_count_rows(const int32_t *row_dofs, int64_t total, int32_t *cnt) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[row_dofs[i]], 1);
+}
+
+__global__ void k_fill_incidence(const int32_t *row_dofs, int64_t total, const int32_t *inc_ptr,
+                                 int32_t *cursor, int32_t *inc) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = row_dofs[i];
+        const int32_t pos = inc_ptr[r] + atomicAdd(&cursor[r], 1);
+        inc[pos] = (int32_t)i;
+    }
+}
+
+// Thread per row: insertion sort of the (short) incidence list.
+__global__ void k_sort_incidence(const int32_t *inc_ptr, int32_t *inc, int64_t n_rows) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    const int32_t b = inc_ptr[r], e = inc_ptr[r + 1];
+    for (int32_t k = b + 1; k < e; ++k) {
+        const int32_t x = inc[k];
+        int32_t j = k - 1;
+        while (j >= b && inc[j] > x) {
+            inc[j + 1] = inc[j];
+            --j;
+        }
+        inc[j + 1] = x;
+    }
+}
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kCap = 1024;  // candidates per warp held in shared memory
+
+// Warp per row.  mode 0: write the unique-column count to counts[r];
+// mode 1: write the unique columns to indices[indptr[r]...].
+__global__ void k_row_columns(const int32_t *inc_ptr, const int32_t *inc, const int32_t *col_dofs,
+                              int32_t row_local, int32_t col_local, int64_t n_rows, int mode,
+                              int32_t *counts, const int32_t *indptr, int32_t *indices) {
+    __shared__ int32_t smem[kWarpsPerBlock * kCap];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
+    if (r >= n_rows) return;
+    const int32_t ib = inc_ptr[r];
+    const int32_t ninc = inc_ptr[r + 1] - ib;
+    const int64_t n = (int64_t)ninc * col_local;
+    int32_t *buf = smem + warp * kCap;
+    if (n <= kCap) {
+        int P = 1;
+        while (P < n) P <<= 1;
+        for (int k = lane; k < P; k += 32) {
+            int32_t v = INT_MAX;
+            if (k < n) {
+                const int32_t item = inc[ib + k / col_local];
+                const int32_t e = item / row_local;
+                v = col_dofs[(int64_t)e * col_local + k % col_local];
+            }
+            buf[k] = v;
+        }
+        __syncwarp();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int t = lane; t < P / 2; t += 32) {
+                    const int lo = 2 * t - (t & (stride - 1));
+                    const int hi = lo + stride;
+                    const bool up = (lo & size) == 0;
+                    const int32_t a = buf[lo], c = buf[hi];
+                    if ((a > c) == up) { buf[lo] = c; buf[hi] = a; }
+                }
+                __syncwarp();
+            }
+        }
+        int32_t written = 0;
+        const int32_t base = mode == 1 ? indptr[r] : 0;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            const int k = k0 + lane;
+            const bool first = k < n && (k == 0 || buf[k] != buf[k - 1]);
+            const unsigned m = __ballot_sync(0xffffffffu, first);
+            if (mode == 1 && first) indices[base + written + __popc(m & ((1u << lane) - 1u))] = buf[k];
+            written += __popc(m);
+        }
+        if (mode == 0 && lane == 0) counts[r] = written;
+        return;
+    }
+    // Large row: extract the distinct columns in increasing order.
+    int32_t last = INT_MIN, written = 0;
+    const int32_t base = mode == 1 ? indptr[r] : 0;
+    for (;;) {
+        int32_t best = INT_MAX;
+        for (int64_t k = lane; k < n; k += 32) {
+            const int32_t item = inc[ib + k / col_local];
+            const int32_t e = item / row_local;
+            const int32_t v = col_dofs[(int64_t)e * col_local + k % col_local];
+            if (v > last && v < best) best = v;
+        }
+        for (int off = 16; off > 0; off >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, off));
+        if (best == INT_MAX) break;
+        if (mode == 1 && lane == 0) indices[base + written] = best;
+        ++written;
+        last = best;
+    }
+    if (mode == 0 && lane == 0) counts[r] = written;
+}
+
+}  // namespace
+
+}  // namespace skg
+
+using namespace skg;
+
+extern "C" int skg_pattern_create(const int32_t *d_row_dofs, const int32_t *d_col_dofs,
+                                  int64_t n_elements, int32_t row_local, int32_t col_local,
+                                  int64_t n_rows, int64_t n_cols, void *stream, skg_pattern **out) {
+    return guarded([&] {
+        require(out != nullptr, "output handle pointer is NULL");
+        *out = nullptr;
+        const bool with_csr = d_col_dofs != nullptr;
+        if (!with_csr) col_local = 0;
+        require(n_elements >= 0 && row_local > 0 && (col_local > 0 || !with_csr), "invalid pattern sizes");
+        require(n_rows >= 0 && n_cols >= 0, "invalid matrix shape");
+        require(n_elements == 0 || d_row_dofs, "dof arrays are NULL");
+        const int64_t tr = n_elements * row_local, tc = n_elements * col_local;
+        require(tr < INT_MAX && tc < INT_MAX && n_rows < INT_MAX && n_cols < INT_MAX,
+                "pattern too large for 32-bit element indexing");
+        require(n_elements * row_local * (int64_t)col_local < (int64_t)INT_MAX * 8,
+                "pattern too large");
+        cudaStream_t s = as_stream(stream);
+        auto *p = new skg_pattern();
+        try {
+            p->n_elements = n_elements; p->row_local = row_local; p->col_local = col_local;
+            p->n_rows = n_rows; p->n_cols = n_cols;
+            p->row_dofs = DevBuf<int32_t>::owned(tr);
+            p->col_dofs = DevBuf<int32_t>::owned(tc);
+            if (tr) SKG_CUDA(cudaMemcpyAsync(p->row_dofs.get(), d_row_dofs, tr * 4, cudaMemcpyDeviceToDevice, s));
+            if (tc) SKG_CUDA(cudaMemcpyAsync(p->col_dofs.get(), d_col_dofs, tc * 4, cudaMemcpyDeviceToDevice, s));
+            // range checks (the reference raises "element DOF index is out of bounds")
+            DevBuf<int32_t> err(2, s);
+            const int32_t init[2] = {INT_MAX, INT_MAX};
+            SKG_CUDA(cudaMemcpyAsync(err.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+            if (tr) k_check_range<<<grid_for(tr, 256), 256, 0, s>>>(p->row_dofs.get(), tr, n_rows, err.get());
+            if (tc) k_check_range<<<grid_for(tc, 256), 256, 0, s>>>(p->col_dofs.get(), tc, n_cols, err.get() + 1);
+            SKG_LAUNCH_CHECK("check_range");
+            int32_t herr[2];
+            SKG_CUDA(cudaMemcpyAsync(herr, err.get(), sizeof(herr), cudaMemcpyDeviceToHost, s));
+            SKG_CUDA(cudaStreamSynchronize(s));
+            require(herr[0] == INT_MAX && herr[1] == INT_MAX, "element DOF index is out of bounds", SKG_ERANGE);
+
+            DevBuf<int32_t> cnt(n_rows + 1, s), cursor(n_rows + 1, s);
+            SKG_CUDA(cudaMemsetAsync(cnt.get(), 0, (n_rows + 1) * 4, s));
+            SKG_CUDA(cudaMemsetAsync(cursor.get(), 0, (n_rows + 1) * 4, s));
+            if (tr) k_count_rows<<<grid_for(tr, 256), 256, 0, s>>>(p->row_dofs.get(), tr, cnt.get());
+            SKG_LAUNCH_CHECK("count_rows");
+            p->inc_ptr = DevBuf<int32_t>::owned(n_rows + 1);
+            exclusive_scan_i32(cnt.get(), p->inc_ptr.get(), n_rows, s);
+            p->inc = DevBuf<int32_t>::owned(tr);
+            if (tr) k_fill_incidence<<<grid_for(tr, 256), 256, 0, s>>>(p->row_dofs.get(), tr, p->inc_ptr.get(), cursor.get(), p->inc.get());
+            SKG_LAUNCH_CHECK("fill_incidence");
+            if (n_rows) k_sort_incidence<<<grid_for(n_rows, 128), 128, 0, s>>>(p->inc_ptr.get(), p->inc.get(), n_rows);
+            SKG_LAUNCH_CHECK("sort_incidence");
+            if (!with_csr) {
+                p->indptr = DevBuf<int32_t>::owned(n_rows + 1);
+                SKG_CUDA(cudaMemsetAsync(p->indptr.get(), 0, (n_rows + 1) * 4, s));
+                SKG_CUDA(cudaStreamSynchronize(s));
+                *out = p;
+                return;
+            }
+            const unsigned gw = grid_for(n_rows, kWarpsPerBlock);
+            if (n_rows)
+                k_row_columns<<<gw, 32 * kWarpsPerBlock, 0, s>>>(p->inc_ptr.get(), p->inc.get(), p->col_dofs.get(),
+                                                                 row_local, col_local, n_rows, 0, cnt.get(), nullptr, nullptr);
+            SKG_LAUNCH_CHECK("row_columns_count");
+            p->indptr = DevBuf<int32_t>::owned(n_rows + 1);
+            exclusive_scan_i32(cnt.get(), p->indptr.get(), n_rows, s);
+            int32_t nnz = 0;
+            SKG_CUDA(cudaMemcpyAsync(&nnz, p->indptr.get() + n_rows, 4, cudaMemcpyDeviceToHost, s));
+            SKG_CUDA(cudaStreamSynchronize(s));
+            require(nnz >= 0, "pattern too large for 32-bit CSR offsets");
+            p->nnz = nnz;
+            p->indices = DevBuf<int32_t>::owned(nnz);
+            if (n_rows)
+                k_row_columns<<<gw, 32 * kWarpsPerBlock, 0, s>>>(p->inc_ptr.get(), p->inc.get(), p->col_dofs.get(),
+                                                                 row_local, col_local, n_rows, 1, nullptr, p->indptr.get(),
+                                                                 p->indices.get());
+            SKG_LAUNCH_CHECK("row_columns_write");
+            SKG_CUDA(cudaStreamSynchronize(s));
+        } catch (...) {
+            delete p;
+            throw;
+        }
+        *out = p;
+    });
+}
+
+extern "C" int skg_pattern_destroy(skg_pattern *pattern) {
+    return guarded([&] { delete pattern; });
+}
+
+extern "C" int skg_pattern_info(const skg_pattern *p, int64_t *nnz, int64_t *n_rows, int64_t *n_cols) {
+    return guarded([&] {
+        require(p != nullptr, "pattern is NULL");
+        if (nnz) *nnz = p->nnz;
+        if (n_rows) *n_rows = p->n_rows;
+        if (n_cols) *n_cols = p->n_cols;
+    });
+}
+
+namespace skg {
+namespace {
+__global__ void k_widen(const int32_t *in, int64_t *out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+}  // namespace
+}  // namespace skg
+
+extern "C" int skg_pattern_export(const skg_pattern *p, int64_t *d_indptr, int32_t *d_indices, void *stream) {
+    return guarded([&] {
+        require(p != nullptr, "pattern is NULL");
+        cudaStream_t s = as_stream(stream);
+        if (d_indptr) {
+            k_widen<<<grid_for(p->n_rows + 1, 256), 256, 0, s>>>(p->indptr.get(), d_indptr, p->n_rows + 1);
+            SKG_LAUNCH_CHECK("export_indptr");
+        }
+        if (d_indices && p->nnz)
+            SKG_CUDA(cudaMemcpyAsync(d_indices, p->indices.get(), p->nnz * 4, cudaMemcpyDeviceToDevice, s));
+    });
+}

@@ -1,0 +1,368 @@
+"""GPU assemblers behind ``asm`` (python/skfemntv/bilinear_form.py:13-367,
+linear_form.py:17-107, forms.py:276-404).
+
+Ownership follows the reference: the plain bilinear path returns one reused
+``csr_matrix`` whose values are overwritten by the next call on the same
+(form, basis); the tensor (anisotropic) path returns a fresh copy.  The CSR
+pattern is built once per (form, basis) on the device.
+
+Path selection for scalar P1/P2 on affine meshes with coefficients that are
+constant over each element's quadrature points: the fused affine kernel
+(geometry + contraction + fixed-order CSR sum from coordinates).  Anything
+else (vector fields, symmetric-gradient / divergence / mass terms, per-point
+coefficients, curved P2 geometry) goes through the tabulated path (device
+geometry tabulation, element matrices, the same fixed-order gather).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+from scipy.sparse import csr_matrix
+
+from . import _device as dev
+from ._native import SKG_FP64, SKG_SPLIT_FP32, call
+from .errors import UnsupportedNativeForm
+from .preflight import enforce_memory_budget, estimate_bilinear_memory
+
+PRECISIONS = {"fp64": SKG_FP64, "split_fp32": SKG_SPLIT_FP32}
+
+
+def _precision(name):
+    try:
+        return PRECISIONS[name]
+    except KeyError:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}") from None
+
+
+class Pattern:
+    """Device CSR pattern + row incidence lists (skg_pattern handle)."""
+
+    def __init__(self, row_dofs_dev, col_dofs_dev, n_elements, row_local, col_local, n_rows, n_cols):
+        h = ctypes.c_void_p()
+        call("skg_pattern_create", dev.ptr(row_dofs_dev), dev.ptr(col_dofs_dev), n_elements, row_local,
+             col_local, n_rows, n_cols, dev.stream_ptr(), ctypes.byref(h))
+        self.h = h
+        nnz = ctypes.c_int64()
+        call("skg_pattern_info", h, ctypes.byref(nnz), None, None)
+        self.nnz = nnz.value
+        self.n_rows, self.n_cols = n_rows, n_cols
+
+    def host_csr(self):
+        indptr = dev.empty(self.n_rows + 1, np.int64)
+        indices = dev.empty(max(1, self.nnz), np.int32)
+        call("skg_pattern_export", self.h, dev.ptr(indptr), dev.ptr(indices), dev.stream_ptr())
+        return indptr.cpu().numpy(), indices[: self.nnz].cpu().numpy()
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            try:
+                from ._native import load
+
+                load().skg_pattern_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def per_element(c, E, Q, name):
+    """(E,) values when ``c`` (broadcastable to (E, Q)) is constant over the
+    points of every element, else None."""
+    c = np.asarray(c, dtype=np.float64)
+    if c.ndim == 0:
+        return np.full(E, float(c))
+    try:
+        b = np.broadcast_to(c, (E, Q))
+    except ValueError as error:
+        raise ValueError(f"{name} coefficient must broadcast to {(E, Q)}") from error
+    if Q == 1 or b.strides[1] == 0 or np.array_equal(b, b[:, :1] * np.ones((1, Q))):
+        return np.ascontiguousarray(b[:, 0])
+    return None
+
+
+def per_point(c, E, Q, name):
+    c = np.asarray(c, dtype=np.float64)
+    try:
+        return np.ascontiguousarray(np.broadcast_to(c, (E, Q)))
+    except ValueError as error:
+        raise ValueError(f"{name} coefficient must broadcast to {(E, Q)}") from error
+
+
+def anisotropic_tensor(raw, E, Q, dim=3):
+    """(3,3) | (3,3,E,Q) public | (E,Q,3,3) native -> (E,Q,3,3) view
+    (forms.py:377-404)."""
+    tensor = np.asarray(raw, dtype=np.float64)
+    shape = (E, Q)
+    if tensor.shape == (dim, dim):
+        return np.broadcast_to(tensor, shape + (dim, dim))
+    if tensor.shape == (dim, dim) + shape:
+        return np.moveaxis(tensor, (0, 1), (-2, -1))
+    if tensor.shape == shape + (dim, dim):
+        return tensor
+    raise ValueError(
+        "anisotropic tensor must use the recommended scikit-fem shape "
+        f"{(dim, dim) + shape}, constant shape ({dim}, {dim}), or the low-level native "
+        f"compatibility shape {shape + (dim, dim)}; got {tensor.shape}")
+
+
+def tensor_per_element(raw, E, Q, dim=3):
+    """Per-element view of a tensor coefficient constant over the points of
+    each element, as (array, coef_kind): coef_kind 2 for the public
+    component-first layout (3, 3, E), 1 for (E, 3, 3).  None when the tensor
+    varies over points."""
+    A = np.asarray(raw, dtype=np.float64)
+    if A.shape == (dim, dim):
+        return np.broadcast_to(A, (E, dim, dim)), 1
+    if A.shape == (dim, dim, E, Q):
+        if Q == 1 or A.strides[3] == 0 or np.array_equal(A, np.broadcast_to(A[..., :1], A.shape)):
+            return A[..., 0], 2
+        return None
+    if A.shape == (E, Q, dim, dim):
+        if Q == 1 or A.strides[1] == 0 or np.array_equal(A, np.broadcast_to(A[:, :1], A.shape)):
+            return A[:, 0], 1
+        return None
+    anisotropic_tensor(A, E, Q, dim)  # raises the shape error
+    return None
+
+
+class _Staging:
+    """Pinned host buffer + device buffer for per-call coefficient uploads
+    (host copy into page-locked memory, then one asynchronous H2D copy)."""
+
+    def __init__(self):
+        self.n = 0
+        self.h = self.hv = self.d = None
+        self.done = None  # event recorded after the last H2D copy
+
+    def upload(self, a):
+        import torch
+
+        a = np.asarray(a, dtype=np.float64)
+        n = a.size
+        if self.done is not None:
+            self.done.synchronize()  # the previous copy has left the pinned buffer
+        if n > self.n:
+            self.h, self.hv = dev.pinned_empty(n)
+            self.d = dev.empty(n, np.float64)
+            self.n = n
+        np.copyto(self.hv[:n].reshape(a.shape), a)
+        self.d[:n].copy_(self.h[:n], non_blocking=True)
+        self.done = torch.cuda.Event()
+        self.done.record()
+        return self.d
+
+
+class _MatrixTarget:
+    """Device values + reused host CSR matrix sharing one pinned buffer."""
+
+    def __init__(self, pattern, shape):
+        self.pattern = pattern
+        indptr, indices = pattern.host_csr()
+        self.d_values = dev.empty(max(1, pattern.nnz), np.float64)
+        self._pinned, host = dev.pinned_empty(max(1, pattern.nnz))
+        self.matrix = csr_matrix((host[: pattern.nnz], indices, indptr), shape=shape, copy=False)
+
+    def download(self):
+        import torch
+
+        self._pinned[: self.pattern.nnz].copy_(self.d_values[: self.pattern.nnz], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return self.matrix
+
+
+class NativeBilinearForm:
+    """value / gradient / symmetric-gradient / divergence assembly on one basis."""
+
+    def __init__(self, basis, *, memory_limit_bytes=None, memory_safety_factor=1.25):
+        self.memory_estimate = estimate_bilinear_memory(basis)
+        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
+        self.basis = basis
+        E, L = basis.mesh.nelements, basis._nodes * basis._comp
+        dofs = basis._dev_dofs()
+        self.pattern = Pattern(dofs, dofs, E, L, L, basis.N, basis.N)
+        self.target = _MatrixTarget(self.pattern, (basis.N, basis.N))
+
+    @property
+    def matrix(self):
+        return self.target.matrix
+
+    def assemble_device(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
+                        precision="fp64"):
+        """Assemble into the device values (no host copy); returns the device tensor."""
+        b = self.basis
+        E, Q = b._coefficient_shape
+        prec = _precision(precision)
+        if value is None and gradient is None and symmetric_gradient is None and divergence is None:
+            raise ValueError("at least one coefficient is required")
+        fast = None
+        if (b._comp == 1 and value is None and symmetric_gradient is None and divergence is None
+                and b.is_affine):
+            fast = per_element(gradient, E, Q, "gradient")
+        if fast is not None:
+            coef = None if np.all(fast == 1.0) else dev.to_device(fast, np.float64)
+            call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.hptr(b.W), 0, dev.ptr(coef), prec, dev.ptr(self.target.d_values), dev.stream_ptr())
+            return self.target.d_values
+        if prec != SKG_FP64:
+            raise UnsupportedNativeForm("split precision is available on the affine scalar gradient path")
+        tab = b._device_tabulation()
+        coefs = [None if c is None else dev.to_device(per_point(c, E, Q, n), np.float64)
+                 for c, n in ((value, "value"), (gradient, "gradient"),
+                              (symmetric_gradient, "symmetric_gradient"), (divergence, "divergence"))]
+        call("skg_h1_assemble_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, b._comp, Q,
+             dev.ptr(tab["shape"]), dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), *(dev.ptr(c) for c in coefs),
+             dev.ptr(self.target.d_values), None, dev.stream_ptr())
+        return self.target.d_values
+
+    def assemble(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
+                 num_threads=0, precision="fp64"):
+        self.assemble_device(value=value, gradient=gradient, symmetric_gradient=symmetric_gradient,
+                             divergence=divergence, precision=precision)
+        return self.target.download()
+
+
+class NativeTensorForm:
+    """dot(mul(A, grad u), grad v) on one scalar basis (NativeCrossBilinearForm
+    .assemble_tensor("gradient", "gradient", ...), bilinear_form.py:336-367)."""
+
+    def __init__(self, basis, *, memory_limit_bytes=None, memory_safety_factor=1.25):
+        if basis._comp != 1:
+            raise UnsupportedNativeForm("anisotropic gradient tensor currently requires a scalar field")
+        self.memory_estimate = estimate_bilinear_memory(basis)
+        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
+        self.basis = basis
+        E, L = basis.mesh.nelements, basis._nodes
+        dofs = basis._dev_dofs()
+        self.pattern = Pattern(dofs, dofs, E, L, L, basis.N, basis.N)
+        self.target = _MatrixTarget(self.pattern, (basis.N, basis.N))
+        self._staging = _Staging()
+
+    def assemble_device(self, raw, precision="fp64", tensor_device=None, tensor_kind=2):
+        """Assemble into the device values.  ``tensor_device``: a per-element
+        float64 device tensor already resident, (3,3,E) for tensor_kind 2 or
+        (E,3,3) for tensor_kind 1 (skips the host upload)."""
+        b = self.basis
+        E, Q = b._coefficient_shape
+        prec = _precision(precision)
+        kind = tensor_kind
+        d_coef = tensor_device
+        if d_coef is None and b.is_affine:
+            pe = tensor_per_element(raw, E, Q)
+            if pe is not None:
+                arr, kind = pe
+                d_coef = self._staging.upload(arr)
+        if d_coef is not None:
+            call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.hptr(b.W), kind, dev.ptr(d_coef), prec, dev.ptr(self.target.d_values),
+                 dev.stream_ptr())
+            return self.target.d_values
+        if prec != SKG_FP64:
+            raise UnsupportedNativeForm("split precision is available on the affine tensor path")
+        T = anisotropic_tensor(raw, E, Q)
+        tab = b._device_tabulation()
+        coef = self._staging.upload(T)
+        call("skg_h1_assemble_tensor_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, 1, Q,
+             dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(coef), dev.ptr(self.target.d_values), None,
+             dev.stream_ptr())
+        return self.target.d_values
+
+    def assemble(self, raw, precision="fp64"):
+        self.assemble_device(raw, precision)
+        return self.target.download().copy()
+
+
+class NativeLinearForm:
+    """f.v + G:grad v on one basis (linear_form.py:17-107)."""
+
+    def __init__(self, basis):
+        self.basis = basis
+        E, L = basis.mesh.nelements, basis._nodes * basis._comp
+        self.pattern = Pattern(basis._dev_dofs(), None, E, L, 0, basis.N, 0)
+        self.d_out = dev.empty(max(1, basis.N), np.float64)
+
+    def assemble(self, *, value=None, gradient=None):
+        b = self.basis
+        E, Q = b._coefficient_shape
+        C = b._comp
+        if value is None and gradient is None:
+            raise ValueError("at least one coefficient is required")
+        dv = dg = None
+        if value is not None:
+            v = np.asarray(value, dtype=np.float64)
+            v = np.broadcast_to(v, (E, Q, C)) if v.shape != (C,) else np.broadcast_to(v, (E, Q, C))
+            dv = dev.to_device(np.ascontiguousarray(v), np.float64)
+        if gradient is not None:
+            g = np.asarray(gradient, dtype=np.float64)
+            try:
+                g = np.broadcast_to(g, (E, Q, C, 3))
+            except ValueError as error:
+                raise ValueError(f"gradient coefficient must broadcast to {(E, Q, C, 3)}") from error
+            dg = dev.to_device(np.ascontiguousarray(g), np.float64)
+        tab = b._device_tabulation()
+        call("skg_linear_assemble_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, C, Q,
+             dev.ptr(tab["shape"]), dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(dv), dev.ptr(dg),
+             dev.ptr(self.d_out), dev.stream_ptr())
+        return self.d_out[: b.N].cpu().numpy()
+
+
+def assemble_bilinear(form, basis, terms, *, precision="fp64", memory_limit_bytes=None,
+                      memory_safety_factor=1.25):
+    plain = {"value": None, "gradient": None, "symmetric_gradient": None, "divergence": None}
+    tensors = []
+    for kind, coef in terms:
+        if kind in plain:
+            plain[kind] = coef if plain[kind] is None else plain[kind] + coef
+        elif kind == "gradient_tensor":
+            tensors.append(coef)
+        else:
+            raise UnsupportedNativeForm(f"unsupported bilinear term kind {kind!r}")
+    result = None
+    if any(v is not None for v in plain.values()):
+        native = form._native_cache.get(basis)
+        if native is None:
+            native = NativeBilinearForm(basis, memory_limit_bytes=memory_limit_bytes,
+                                        memory_safety_factor=memory_safety_factor)
+            form._native_cache[basis] = native
+        elif memory_limit_bytes is not None:
+            enforce_memory_budget(native.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
+        result = native.assemble(precision=precision, **plain)
+    if tensors:
+        tnative = form._tensor_cache.get(basis)
+        if tnative is None:
+            tnative = NativeTensorForm(basis, memory_limit_bytes=memory_limit_bytes,
+                                       memory_safety_factor=memory_safety_factor)
+            form._tensor_cache[basis] = tnative
+        for raw in tensors:
+            m = tnative.assemble(raw, precision)
+            result = m if result is None else result + m
+    if result is None:
+        raise UnsupportedNativeForm("bilinear form contains no assembled terms")
+    return result
+
+
+def assemble_linear(form, basis, terms):
+    native = form._native_cache.get(basis)
+    if native is None:
+        native = NativeLinearForm(basis)
+        form._native_cache[basis] = native
+    E, Q = basis._coefficient_shape
+    C = basis._comp
+    value = gradient = None
+    for kind, c in terms:
+        c = np.asarray(c, dtype=np.float64)
+        if kind == "value":
+            if C == 1 and c.shape == (E, Q):
+                c = c[..., None]
+            elif c.ndim and c.shape[0] == C and c.shape != (C,):
+                c = np.moveaxis(c, 0, -1)
+            value = c if value is None else value + c
+        elif kind == "gradient":
+            if c.ndim >= 2 and c.shape[:2] == (C, 3):
+                c = np.moveaxis(c, (0, 1), (-2, -1))
+            gradient = c if gradient is None else gradient + c
+        else:
+            raise UnsupportedNativeForm
+    return native.assemble(value=value, gradient=gradient)

@@ -1,0 +1,209 @@
+"""Lowest-order Nedelec H(curl) on affine tetrahedra
+(python/skfemntv/hcurl_basis.py:292-445, hcurl_assembler.py:52-215,
+edge_topology.py, edge_dof_map.py).
+
+Edge numbering, orientation signs and the Maxwell assembly run on the GPU.
+The mapped per-point basis arrays the reference keeps, ``(E, 6, 3, Q)`` for
+values and curls, are not stored; they are produced on demand by the
+``values`` / ``curls`` properties for callers that read them.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _device as dev
+from . import quadrature as quad
+from ._native import SKG_FP64, call
+from .assembly import Pattern, _MatrixTarget, _precision, per_element, per_point
+from .mesh import oriented_edges
+from .preflight import AssemblyMemoryEstimate, enforce_memory_budget
+
+
+@dataclass(frozen=True)
+class OrientedEdgeTopology:
+    edges: np.ndarray
+    element_edges: np.ndarray
+    element_edge_signs: np.ndarray
+    local_edges: tuple
+
+
+@dataclass(frozen=True)
+class OrientedEdgeDofMap:
+    topology: OrientedEdgeTopology
+
+    @property
+    def ndofs(self):
+        return int(self.topology.edges.shape[1])
+
+    @property
+    def element_dofs(self):
+        return self.topology.element_edges
+
+    @property
+    def basis_signs(self):
+        return self.topology.element_edge_signs
+
+
+@dataclass(frozen=True)
+class HcurlTetGeometryDiagnostics:
+    minimum_signed_determinant: float
+    minimum_absolute_determinant: float
+    minimum_volume: float
+    maximum_aspect_ratio: float
+    inverted_cell_count: int
+
+
+def _ref_basis(X):
+    lam = np.concatenate(((1.0 - X.sum(axis=0))[None], X), axis=0)
+    g = quad._DL
+    vals = np.empty((6, 3) + X.shape[1:])
+    for k, (a, b) in enumerate(quad.TET_EDGES):
+        vals[k] = lam[a][None] * g[b][:, None] - lam[b][None] * g[a][:, None]
+    curls = np.array([2.0 * np.cross(g[a], g[b]) for a, b in quad.TET_EDGES])
+    return vals, curls
+
+
+class AffineTetN1Basis:
+    """Lowest-order H(curl) basis on affine tetrahedral meshes."""
+
+    def __init__(self, mesh, *, intorder=2, max_aspect_ratio=None):
+        if mesh.dim() != 3 or mesh.t.shape[0] not in (4, 10):
+            raise TypeError("AffineTetN1Basis requires a tetrahedral mesh")
+        self.mesh = mesh
+        E = mesh.nelements
+        t4 = mesh._dev("t")[:4].contiguous()
+        edges, ee, sg = oriented_edges(t4, E)
+        self._t4 = t4
+        self._ee_dev, self._signs_dev = ee, sg
+        topo = OrientedEdgeTopology(edges, ee.cpu().numpy().astype(np.int64), sg.cpu().numpy(),
+                                    quad.TET_EDGES)
+        self.dof_map = OrientedEdgeDofMap(topo)
+        self.N = self.dof_map.ndofs
+        self.element_dofs = self.dof_map.element_dofs
+        self.basis_signs = self.dof_map.basis_signs
+        self.X, self.W = quad.duffy_rule(intorder)
+        v = mesh.p[:, mesh.t[:4]]
+        self.jacobians = np.stack(tuple(v[:, k] - v[:, 0] for k in (1, 2, 3)), axis=1)
+        J = self.jacobians
+        self.detJ = (J[0, 0] * (J[1, 1] * J[2, 2] - J[1, 2] * J[2, 1])
+                     - J[0, 1] * (J[1, 0] * J[2, 2] - J[1, 2] * J[2, 0])
+                     + J[0, 2] * (J[1, 0] * J[2, 1] - J[1, 1] * J[2, 0]))
+        if np.any(np.isclose(self.detJ, 0.0)):
+            raise ValueError("H(curl) basis requires nonsingular tetrahedra")
+        lengths = [np.linalg.norm(v[:, b] - v[:, a], axis=0) for a, b in quad.TET_EDGES]
+        aspect = np.max(lengths, axis=0) ** 3 / np.abs(self.detJ)
+        self.geometry_diagnostics = HcurlTetGeometryDiagnostics(
+            minimum_signed_determinant=float(np.min(self.detJ)),
+            minimum_absolute_determinant=float(np.min(np.abs(self.detJ))),
+            minimum_volume=float(np.min(np.abs(self.detJ)) / 6.0),
+            maximum_aspect_ratio=float(np.max(aspect)),
+            inverted_cell_count=int(np.count_nonzero(self.detJ < 0.0)))
+        if max_aspect_ratio is not None:
+            if (isinstance(max_aspect_ratio, bool) or not np.isscalar(max_aspect_ratio)
+                    or not np.isfinite(max_aspect_ratio) or max_aspect_ratio <= 0.0):
+                raise ValueError("max_aspect_ratio must be a positive finite scalar")
+            if self.geometry_diagnostics.maximum_aspect_ratio > max_aspect_ratio:
+                raise ValueError(
+                    f"H(curl) tetrahedron aspect ratio exceeds max_aspect_ratio={max_aspect_ratio}")
+        self.dx = np.abs(self.detJ)[:, None] * self.W[None, :]
+
+    def _mapped(self):
+        ref_v, ref_c = _ref_basis(self.X)
+        J = np.moveaxis(self.jacobians, (0, 1), (-2, -1))  # (E,3,3)
+        inv = np.linalg.inv(J)
+        vals = np.einsum("erp,brq->ebpq", inv, ref_v)
+        curls = np.einsum("epr,br->ebp", J, ref_c)[..., None] / self.detJ[:, None, None, None]
+        curls = np.broadcast_to(curls, vals.shape)
+        s = self.basis_signs.T[:, :, None, None]
+        return vals * s, curls * s
+
+    @property
+    def values(self):
+        """Mapped values as (basis, component, cell, quadrature)."""
+        return self._mapped()[0].transpose(1, 2, 0, 3)
+
+    @property
+    def curls(self):
+        return self._mapped()[1].transpose(1, 2, 0, 3)
+
+
+def estimate_tet_n1_assembly_memory(basis):
+    if not isinstance(basis, AffineTetN1Basis):
+        raise TypeError("basis must be AffineTetN1Basis")
+    E, N = basis.mesh.nelements, basis.N
+    nnz = min(N * N, E * 36)
+    return AssemblyMemoryEstimate(
+        kind="hcurl_tet_n1", rows=N, columns=N, entity_count=E, quadrature_points_per_entity=len(basis.W),
+        row_local_dofs=6, column_local_dofs=6, nnz_upper_bound=nnz,
+        device_pattern_bytes=4 * (12 * E + 2 * (N + 1) + 6 * E + nnz), device_values_bytes=8 * nnz,
+        device_scratch_bytes=8 * 36 * E, host_csr_bytes=12 * nnz + 8 * (N + 1),
+        pattern_temporary_bytes_upper_bound=8 * (N + 1) + 16 * E * 6)
+
+
+class TetN1Assembler:
+    """Reusable mass / curl-curl assembler; assembly methods overwrite and
+    return one CSR matrix (call ``.copy()`` to keep a result)."""
+
+    def __init__(self, basis, *, memory_limit_bytes=None, memory_safety_factor=1.25):
+        if not isinstance(basis, AffineTetN1Basis):
+            raise TypeError("basis must be AffineTetN1Basis")
+        self.basis = basis
+        self.memory_estimate = estimate_tet_n1_assembly_memory(basis)
+        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
+        E = basis.mesh.nelements
+        self._dofs = basis._ee_dev.t().contiguous()  # (E, 6)
+        self.pattern = Pattern(self._dofs, self._dofs, E, 6, 6, basis.N, basis.N)
+        self.target = _MatrixTarget(self.pattern, (basis.N, basis.N))
+
+    def _coef(self, name, value):
+        E, Q = self.basis.dx.shape
+        if value is None:
+            return None, None
+        pe = per_element(value, E, Q, name)
+        if pe is not None:
+            return (None if np.all(pe == 1.0) else dev.to_device(pe, np.float64)), None
+        return None, dev.to_device(per_point(value, E, Q, name), np.float64)
+
+    def assemble_device(self, *, mass_coefficient=None, curl_coefficient=None, include_mass=True,
+                        include_curl=True, precision="fp64"):
+        b = self.basis
+        E = b.mesh.nelements
+        Q = len(b.W)
+        prec = _precision(precision)
+        m_el, m_pt = self._coef("mass", mass_coefficient)
+        c_el, c_pt = self._coef("curl", curl_coefficient)
+        if m_pt is None and c_pt is None:
+            call("skg_n1_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b._t4), dev.ptr(b._ee_dev), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W),
+                 dev.ptr(m_el), dev.ptr(c_el), int(include_mass), int(include_curl), prec,
+                 dev.ptr(self.target.d_values), dev.stream_ptr())
+        else:
+            if prec != SKG_FP64:
+                from .errors import UnsupportedNativeForm
+
+                raise UnsupportedNativeForm("split precision needs per-element coefficients")
+            ones = dev.to_device(np.ones((E, Q)), np.float64)
+            mp = m_pt if m_pt is not None else (
+                ones if m_el is None else dev.to_device(np.repeat(m_el.cpu().numpy()[:, None], Q, 1), np.float64))
+            cp = c_pt if c_pt is not None else (
+                ones if c_el is None else dev.to_device(np.repeat(c_el.cpu().numpy()[:, None], Q, 1), np.float64))
+            call("skg_n1_assemble_pointwise", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b._t4), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W), dev.ptr(mp),
+                 dev.ptr(cp), int(include_mass), int(include_curl), dev.ptr(self.target.d_values),
+                 dev.stream_ptr())
+        return self.target.d_values
+
+    def assemble_maxwell(self, *, mass_coefficient=None, curl_coefficient=None, precision="fp64"):
+        self.assemble_device(mass_coefficient=mass_coefficient, curl_coefficient=curl_coefficient,
+                             precision=precision)
+        return self.target.download()
+
+    def assemble_mass(self, coefficient=None, precision="fp64"):
+        self.assemble_device(mass_coefficient=coefficient, include_curl=False, precision=precision)
+        return self.target.download()
+
+    def assemble_curl_curl(self, coefficient=None, precision="fp64"):
+        self.assemble_device(curl_coefficient=coefficient, include_mass=False, precision=precision)
+        return self.target.download()

@@ -1,0 +1,265 @@
+"""GPU parity: the CUDA path through the public API / C ABI against the
+reference's own outputs (tests/golden) and the CPU oracle.
+
+Index structures (indptr, indices, edge ids, signs) must match exactly; FP64
+values within 1e-12 relative to the largest entry (the tolerance the
+reference's own FP64 contract states); geometry tabulation bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+sk = pytest.importorskip("skfemntv_gb300")
+from skfemntv_gb300.forms import ddot, dot, grad, mul, sym_grad, div  # noqa: E402
+
+RTOL = 1e-12
+X1 = np.array([[.25], [.25], [.25]])
+W1 = np.array([1 / 6])
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def same_pattern(K, g):
+    assert np.array_equal(K.indptr, g["indptr"])
+    assert np.array_equal(K.indices, g["indices"])
+
+
+@sk.BilinearForm
+def lap(u, v, w):
+    return ddot(grad(u), grad(v))
+
+
+@sk.BilinearForm
+def lap_dot(u, v, w):
+    return dot(grad(u), grad(v))
+
+
+@sk.BilinearForm
+def klap(u, v, w):
+    return w.kappa * ddot(grad(u), grad(v))
+
+
+@sk.BilinearForm
+def aniso(u, v, w):
+    return dot(mul(w.A, grad(u)), grad(v))
+
+
+def test_p1_laplace_one_point():
+    g = load_golden("p1_laplace")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X1, W1))
+    K = sk.asm(lap, b)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+    K2 = sk.asm(lap_dot, b)
+    assert relerr(K2.data, g["data"]) < RTOL
+    Kk = sk.asm(klap, b, kappa=g["kappa"][:, None])
+    assert relerr(Kk.data, g["kdata"]) < RTOL
+
+
+def test_p1_reused_matrix_semantics():
+    g = load_golden("p1_laplace")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X1, W1))
+    K1 = sk.asm(klap, b, kappa=np.ones((b.mesh.nelements, 1)))
+    d1 = K1.data.copy()
+    K2 = sk.asm(klap, b, kappa=2 * np.ones((b.mesh.nelements, 1)))
+    assert K1 is K2  # same object, values overwritten (bilinear_form.py:50-59)
+    assert np.allclose(K2.data, 2 * d1, rtol=1e-15, atol=0)
+
+
+def test_p1_mass_stiffness_tabulated_path():
+    g = load_golden("p1_helmholtz")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1))
+
+    @sk.BilinearForm
+    def helm(u, v, w):
+        return w.c * ddot(grad(u), grad(v)) + w.s * dot(u, v)
+
+    K = sk.asm(helm, b, c=g["c"], s=g["s"])
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+    # the device geometry tabulation reproduces the reference bit for bit
+    assert np.array_equal(b.dx, g["dx"])
+    assert np.array_equal(b.tabulated_gradients, g["grads"])
+
+
+def p2_basis(g, quadrature=None):
+    m = sk.MeshTet2(g["p"], g["t"])
+    return sk.Basis(m, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=quadrature)
+
+
+def test_p2_mesh_from_mesh_first_seen():
+    g = load_golden("p2_aniso")
+    m2 = sk.MeshTet2.from_mesh(sk.MeshTet(g["pj"], g["t0"]))
+    assert np.array_equal(m2.t, g["t"]) and np.array_equal(m2.p, g["p"])
+
+
+def test_p2_anisotropic_fused():
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    assert b.is_affine
+    E, Q = b._coefficient_shape
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    K = sk.asm(aniso, b, A=Apub)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+    Ans = np.broadcast_to(np.moveaxis(g["Ans"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    Kn = sk.asm(aniso, b, A=Ans)
+    assert relerr(Kn.data, g["ns_data"]) < RTOL
+    # native (E,Q,3,3) layout and materialised per-point copies give the same
+    Knat = sk.asm(aniso, b, A=np.ascontiguousarray(np.broadcast_to(g["A"][:, None], (E, Q, 3, 3))))
+    assert relerr(Knat.data, g["data"]) < RTOL
+    # geometry tabulated on the device matches the reference bit for bit
+    assert np.array_equal(b.dx, g["dx"]) and np.array_equal(b.tabulated_gradients, g["grads"])
+    assert np.array_equal(b._geometry_determinants, g["det"])
+
+
+def test_p2_anisotropic_per_point_tabulated_path():
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    rng = np.random.default_rng(11)
+    Aq = np.broadcast_to(g["A"][:, None], (E, Q, 3, 3)) * (1 + 0.1 * rng.random((E, Q, 1, 1)))
+    K = sk.asm(aniso, b, A=Aq)
+    ob = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    data, indptr, indices = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(Aq, (E, Q)))
+    assert np.array_equal(K.indices, indices)
+    assert relerr(K.data, data) < RTOL
+
+
+def test_p2_split_precision_error_bound():
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    K = sk.asm(aniso, b, A=Apub, precision="split_fp32")
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < 1e-7
+
+
+def test_p2_laplace_default_keast_rule():
+    g = load_golden("p2_laplace_default")
+    b = p2_basis(g)
+    K = sk.asm(lap, b)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+
+
+def test_n1_maxwell():
+    g = load_golden("n1_maxwell")
+    nb = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]))
+    assert np.array_equal(nb.dof_map.topology.edges, g["edges"])
+    assert np.array_equal(nb.element_dofs, g["element_edges"])
+    assert np.array_equal(nb.basis_signs, g["signs"])
+    asmb = sk.TetN1Assembler(nb)
+    K = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=(1.0 / g["mu"])[:, None])
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+    # per-point coefficients through the explicit quadrature loop
+    Q = len(nb.W)
+    Kp = asmb.assemble_maxwell(mass_coefficient=np.ones((nb.mesh.nelements, Q)),
+                               curl_coefficient=np.repeat((1.0 / g["mu"])[:, None], Q, 1)
+                               * (1 + 0 * np.arange(Q))[None])
+    assert relerr(Kp.data, g["data"]) < RTOL
+
+
+def test_n1_mass_and_curl_separately():
+    g = load_golden("n1_maxwell")
+    nb = O.make_n1_basis(g["p"], g["t"])
+    gb = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]))
+    a = sk.TetN1Assembler(gb)
+    E, Q = nb.dx.shape
+    Km = a.assemble_mass(2.0).copy()
+    Kc = a.assemble_curl_curl().copy()
+    dm, _, _ = O.n1_assemble_maxwell(nb, 2.0, 0.0)
+    dc, _, _ = O.n1_assemble_maxwell(nb, 0.0, 1.0)
+    assert relerr(Km.data, dm) < RTOL and relerr(Kc.data, dc) < RTOL
+
+
+def test_vector_p1_elasticity_terms():
+    g = load_golden("vp1_elasticity")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
+
+    @sk.BilinearForm
+    def elast(u, v, w):
+        return 2.0 * ddot(sym_grad(u), sym_grad(v)) + 10.0 * div(u) * div(v) + 0.5 * dot(u, v)
+
+    K = sk.asm(elast, b)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+
+
+def test_vector_tensor_tabulated_abi():
+    """Full (E,Q,3,3,3,3) tensor through the C ABI (the neo-Hookean tangent layout)."""
+    import torch
+
+    from skfemntv_gb300 import _device as dev
+    from skfemntv_gb300._native import call
+    from skfemntv_gb300.assembly import Pattern
+
+    g = load_golden("nh_vp1")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
+    ob = O.make_basis(g["p"], g["t"], False, comp=3, quadrature=(X1, W1))
+    A = O.nh_tangent(O.displacement_gradient(ob, g["u"]), 1.0, 10.0)
+    E, Q = b._coefficient_shape
+    pat = Pattern(b._dev_dofs(), b._dev_dofs(), E, 12, 12, b.N, b.N)
+    vals = dev.empty(pat.nnz, np.float64)
+    tab = b._device_tabulation()
+    call("skg_h1_assemble_tensor_tabulated", pat.h, dev.ptr(b._dev_dofs()), E, 4, 3, Q, dev.ptr(tab["grad"]),
+         dev.ptr(tab["dx"]), dev.ptr(dev.to_device(A, np.float64)), dev.ptr(vals), None, dev.stream_ptr())
+    torch.cuda.synchronize()
+    indptr, indices = pat.host_csr()
+    assert np.array_equal(indices, g["indices"])
+    assert relerr(vals.cpu().numpy(), g["data"]) < RTOL
+
+
+def test_p2_load_vector():
+    g = load_golden("p2_load")
+    b = p2_basis(g, (g["X"], g["W"]))
+
+    @sk.LinearForm
+    def load(v, w):
+        return dot(w.f, v)
+
+    r = sk.asm(load, b, f=g["f"])
+    assert relerr(r, g["rhs"]) < RTOL
+
+
+def test_repeatable_bits():
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    d1 = sk.asm(aniso, b, A=Apub).data.copy()
+    d2 = sk.asm(aniso, b, A=Apub).data.copy()
+    assert np.array_equal(d1.view(np.int64), d2.view(np.int64))
+
+
+def test_geometry_errors_match_reference():
+    flat = sk.MeshTet(np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 0.]]), np.array([[0], [1], [2], [3]]))
+    with pytest.raises(ValueError, match="cell=0, quadrature_point=0.*near_singular_or_non_finite"):
+        sk.Basis(flat, sk.ElementVector(sk.ElementTetP1(), dim=1))
+    tiny = sk.MeshTet(np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 1.]]) * 1e-50,
+                      np.array([[0], [1], [2], [3]]))
+    b = sk.Basis(tiny, sk.ElementVector(sk.ElementTetP1(), dim=1))
+    assert b.geometry_diagnostics.minimum_determinant > 0
+    bad = sk.MeshTet(np.eye(3, 4), np.array([[0], [1], [1], [2]]))
+    with pytest.raises(ValueError, match="repeats a corner"):
+        sk.AffineTetN1Basis(bad)
+
+
+def test_full_size_p1_laplace_vs_oracle():
+    """The 32^3 x 6 Laplace configuration, compared entry by entry."""
+    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 33),) * 3)
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X1, W1))
+    K = sk.asm(lap, b)
+    assert K.nnz == 513313
+    ob = O.make_basis(m.p, m.t, False, quadrature=(X1, W1))
+    data, indptr, indices = O.bilinear_assemble(ob, gradient=1.0)
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, data) < RTOL

@@ -1,0 +1,177 @@
+"""Host-side tests that need no GPU: the C ABI library loads and exports every
+symbol declared in include/skfem_gb300.h, and the host logic of the drop-in
+(form tracing, quadrature tables, mesh generation, DOF numbering, runtime
+controls, memory preflight) matches the reference's behaviour."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import ROOT, load_golden
+
+import skfemntv_gb300 as sk
+from skfemntv_gb300 import _native, quadrature
+from skfemntv_gb300.basis import number_dofs
+from skfemntv_gb300.forms import (Parameters, QuadratureValue, _Field, _LinearSum, _LinearTerm, _Sum, _Term,
+                                  ddot, div, dot, grad, mul, sym_grad)
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "skfem_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(skg_\w+)\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.load()
+    syms = header_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+        assert s in _native.SIGNATURES, f"{s} missing from the ctypes binding"
+    assert lib.skg_version() >= 100
+
+
+def test_nvcc_targets_sm103a_only():
+    import build_native
+
+    assert build_native.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+# ---------------------------------------------------------------- forms
+
+def _trial():
+    return _Field("trial", "value")
+
+
+def _test():
+    return _Field("test", "value")
+
+
+def test_form_terms():
+    u, v = _trial(), _test()
+    assert ddot(grad(u), grad(v)) == _Term("gradient", None, 1.0)
+    assert dot(grad(u), grad(v)) == _Term("gradient", None, 1.0)  # accepted (reference raises)
+    assert dot(u, v) == _Term("value", None, 1.0)
+    assert ddot(sym_grad(u), sym_grad(v)) == _Term("symmetric_gradient", None, 1.0)
+    assert div(u) * div(v) == _Term("divergence", None, 1.0)
+    A = np.eye(3)
+    t = dot(mul(A, grad(u)), grad(v))
+    assert t.kind == "gradient_tensor" and np.array_equal(t.coefficient, A)
+    s = 2.0 * ddot(grad(u), grad(v)) + dot(u, v) - dot(u, v)
+    assert isinstance(s, _Sum) and [x.factor for x in s.terms] == [2.0, 1.0, -1.0]
+
+
+def test_coefficients_and_parameters():
+    w = Parameters({"kappa": QuadratureValue(np.ones((5, 1)), "kappa")})
+    u, v = _trial(), _test()
+    t = w.kappa * ddot(grad(u), grad(v))
+    assert t.kind == "gradient" and t.coefficient.shape == (5, 1)
+    sym = w.missing * dot(u, v)
+    assert sym.coefficient.name == "missing"
+    f = dot(w.kappa, v)
+    assert isinstance(f, _LinearTerm) and f.kind == "value"
+    g = ddot(np.zeros((3, 3, 5, 1)), grad(v)) + dot(w.kappa, v)
+    assert isinstance(g, _LinearSum)
+
+
+def test_unsupported_forms_raise():
+    u, v = _trial(), _test()
+    with pytest.raises(sk.UnsupportedNativeForm):
+        dot(grad(u), v)
+    with pytest.raises(sk.UnsupportedNativeForm):
+        mul(np.eye(3), u)
+    with pytest.raises(sk.UnsupportedNativeForm):
+        dot(mul(np.eye(3), grad(u)), grad(u))
+
+
+def test_asm_rejects_foreign_forms():
+    with pytest.raises(TypeError):
+        sk.asm(object(), None)
+    with pytest.raises(ValueError):
+        sk.asm(sk.BilinearForm(lambda u, v, w: dot(u, v)), None, num_threads=0)
+
+
+# ---------------------------------------------------------------- setup
+
+def test_quadrature_tables_match_reference_rules():
+    g1 = load_golden("p1_helmholtz")
+    X, W = quadrature.tet_rule_p1()
+    assert np.array_equal(X, g1["X"]) and np.array_equal(W, g1["W"])
+    g2 = load_golden("p2_laplace_default")
+    X, W = quadrature.tet_rule_p2()
+    assert np.array_equal(X, g2["X"]) and np.array_equal(W, g2["W"])
+    gn = load_golden("n1_maxwell")
+    X, W = quadrature.duffy_rule(2)
+    assert np.array_equal(X, gn["X"]) and np.array_equal(W, gn["W"])
+    for quadratic in (False, True):
+        s1, g1_ = quadrature.tabulate(X, quadratic)
+        s2, g2_ = O.tabulate_reference(X, quadratic)
+        assert np.array_equal(s1, s2) and np.array_equal(g1_, g2_)
+
+
+def test_quadrature_validation():
+    with pytest.raises(ValueError, match="shape"):
+        quadrature.validate((np.zeros((2, 3)), np.zeros(3)))
+    with pytest.raises(ValueError, match="finite"):
+        quadrature.validate((np.full((3, 1), np.nan), np.ones(1)))
+
+
+def test_mesh_init_tensor_matches_reference():
+    g = load_golden("p1_laplace")
+    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3)
+    assert np.array_equal(m.p, g["p"]) and np.array_equal(m.t, g["t"])
+    x = np.array([0.0, 0.3, 1.0])
+    y = np.array([0.0, 0.5, 0.7, 1.0])
+    z = np.array([0.0, 1.0])
+    m2 = sk.MeshTet.init_tensor(x, y, z)
+    p, t = O.mesh_tet_tensor(x, y, z)
+    assert np.array_equal(m2.p, p) and np.array_equal(m2.t, t)
+
+
+def test_dof_numbering_matches_oracle():
+    g = load_golden("p2_aniso")
+    for nodes, comp in ((10, 1), (4, 3), (4, 1)):
+        conn = g["t"][:nodes]
+        N, _, ed, _ = number_dofs(g["p"].shape[1], conn, comp)
+        # oracle numbering (restated from basis.py:1749-1777)
+        used = np.zeros(g["p"].shape[1], bool)
+        used[conn] = True
+        act = np.flatnonzero(used)
+        assert N == len(act) * comp
+        pos = np.full(g["p"].shape[1], -1)
+        pos[act] = np.arange(len(act))
+        nd = np.arange(N).reshape(-1, comp).T
+        ref = nd[:, pos[conn]].transpose(2, 1, 0).reshape(conn.shape[1], nodes * comp).T
+        assert np.array_equal(ed, ref)
+
+
+def test_runtime_controls():
+    assert sk.get_num_threads() >= 1
+    with pytest.raises(ValueError):
+        sk.set_num_threads(0)
+    with pytest.raises(ValueError):
+        sk.set_num_threads(True)
+    before = sk.get_num_threads()
+    with sk.thread_limit(1) as eff:
+        assert eff == 1 and sk.get_num_threads() == 1
+    assert sk.get_num_threads() == before
+
+
+def test_memory_budget_error():
+    est = sk.AssemblyMemoryEstimate("bilinear", 10, 10, 4, 1, 4, 4, 64, 1000, 512, 0, 768, 100)
+    with pytest.raises(sk.AssemblyMemoryBudgetError, match="budget exceeded"):
+        sk.enforce_memory_budget(est, 100)
+    sk.enforce_memory_budget(est, 10 ** 9)
+    with pytest.raises(ValueError):
+        sk.enforce_memory_budget(est, -1)
+    assert issubclass(sk.AssemblyMemoryBudgetError, MemoryError)
+
+
+def test_no_product_module_imports_oracle():
+    pkg = os.path.join(ROOT, "scikit-fem-native_gb300", "skfemntv_gb300")
+    for f in os.listdir(pkg):
+        if f.endswith(".py"):
+            src = open(os.path.join(pkg, f)).read()
+            assert "oracle" not in src.replace("oracle-free", ""), f
