@@ -230,48 +230,65 @@ def run_gpu(args, rank, world):
     form = NativeTensorForm(basis)
     nnz = form.pattern.nnz
     dA = dev.to_device(A_cf, np.float64)
+    prec = {"fp64": 0, "split_fp32": 1, "fp64_emulated": 2}
+    stream = torch.cuda.current_stream()
 
-    def step_device():
-        form.assemble_device(None, tensor_device=dA, tensor_kind=2)
+    def step_device(mode):
+        form.assemble_device(None, precision=mode, tensor_device=dA, tensor_kind=2)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(max(3, args.warmup)):
-        step_device()
-    barrier()
+    def max_over_ranks(x):
+        if world > 1:
+            tt = torch.tensor([x], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            return float(tt.item())
+        return x
 
-    # ---- value: device-resident inputs, CUDA events on the launching stream
-    stream = torch.cuda.current_stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(torch.cuda.current_device()) as clocks:
+    def time_mode(mode):
+        for _ in range(max(3, args.warmup)):
+            step_device(mode)
         barrier()
-        ev0.record(stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(torch.cuda.current_device()) as clocks:
+            barrier()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                step_device(mode)
+            ev1.record(stream)
+            barrier()
+        ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)
+        kms = (ctypes.c_float * 2)()
+        k_el, k_rows = [], []
         for _ in range(args.steps):
-            step_device()
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * nnz / (ms * 1e-3)
+            call("skg_h1_assemble_affine_profiled", form.pattern.h, dev.ptr(m2._dev("p")), m2.p.shape[1],
+                 dev.ptr(m2._dev("t")), 10, E, dev.ptr(basis._dev_dofs()), Q, dev.hptr(basis.X), dev.hptr(basis.W),
+                 2, dev.ptr(dA), prec[mode], dev.ptr(form.target.d_values), kms, dev.stream_ptr())
+            k_el.append(kms[0])
+            k_rows.append(kms[1])
+        return ms, statistics.mean(k_el), statistics.mean(k_rows), clocks.summary()
 
-    # ---- per-kernel durations (profiled entry point: events around each kernel)
-    kms = (ctypes.c_float * 2)()
-    k_el, k_rows = [], []
-    for _ in range(args.steps):
-        call("skg_h1_assemble_affine_profiled", form.pattern.h, dev.ptr(m2._dev("p")), m2.p.shape[1],
-             dev.ptr(m2._dev("t")), 10, E, dev.ptr(basis._dev_dofs()), Q, dev.hptr(basis.X), dev.hptr(basis.W), 2,
-             dev.ptr(dA), 0, dev.ptr(form.target.d_values), kms, dev.stream_ptr())
-        k_el.append(kms[0])
-        k_rows.append(kms[1])
-    t_el, t_rows = statistics.mean(k_el), statistics.mean(k_rows)
+    results = {}
+    reference_values = None
+    for mode in ("fp64", "fp64_emulated", "split_fp32"):
+        ms, t_el, t_rows, clk = time_mode(mode)
+        vals = form.target.d_values[:nnz].clone()
+        if reference_values is None:
+            reference_values = vals
+            err = 0.0
+        else:
+            err = float((vals - reference_values).abs().max() / reference_values.abs().max())
+        results[mode] = {"value": world * nnz / (ms * 1e-3), "ms_per_step": ms,
+                         "kernel_ms": {"element_pass": t_el, "row_pass": t_rows},
+                         "max_rel_err_vs_fp64": err, "clocks": clk}
+    head = results["fp64"]
+    ms, t_el, t_rows = head["ms_per_step"], head["kernel_ms"]["element_pass"], head["kernel_ms"]["row_pass"]
+    value = head["value"]
 
-    # ---- e2e: host (page-locked) A in, host CSR values out, through the assembler API
+    # ---- e2e (native FP64): host (page-locked) A in, host CSR values out, through the assembler API
     for _ in range(2):
         form.assemble_device(A_pub)
         form.target.download()
@@ -281,21 +298,17 @@ def run_gpu(args, rank, world):
         form.assemble_device(A_pub)
         form.target.download()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     e2e_value = world * nnz / e2e_s
 
-    # ---- roofline of the dominant kernel (the row pass)
+    # ---- roofline of the dominant kernel (headline mode)
     peak, peak_kind = measured_peak()
     npts_vertex = (N_CELLS + 1) ** 3
     bytes_elem = 24 * npts_vertex + 16 * E + 72 * E     # vertex coords + 4 vertex ids + A
     bytes_rows = 40 * E + 8 * nnz                       # 10 dof ids per element + CSR values
-    dominant = ("k_affine_rows", bytes_rows, t_rows) if t_rows >= t_el else ("k_affine_element_G", bytes_elem, t_el)
+    dominant = ("k_rows_block", bytes_rows, t_rows) if t_rows >= t_el else ("k_elem_fp64", bytes_elem, t_el)
     achieved = dominant[1] / (dominant[2] * 1e-3) / 1e9
-    traffic = profiled_traffic() if dominant[0] == "k_affine_rows" else None
+    traffic = profiled_traffic() if dominant[0] == "k_rows_block" else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -307,10 +320,10 @@ def run_gpu(args, rank, world):
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes_per_launch": dominant[1],
-                     "kernel_ms": {"k_affine_element_G": t_el, "k_affine_rows": t_rows},
                      "whole_assembly_hbm_frac": (bytes_elem + bytes_rows) / ((t_el + t_rows) * 1e-3) / 1e9 / peak},
+        "precision_variants": results,
         "gpu_launches": 2 * args.steps,
-        "clocks": clocks.summary(),
+        "clocks": head["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
         sample = OracleSample(REFERENCE_SAMPLE_CELLS, host_threads())

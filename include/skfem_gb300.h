@@ -45,7 +45,8 @@ extern "C" {
 
 /* Precision of the element contraction. */
 #define SKG_FP64 0          /* FP64 end to end */
-#define SKG_SPLIT_FP32 1    /* FP32 hi+lo split products, FP32 accumulation; FP64 geometry and slot sums */
+#define SKG_SPLIT_FP32 1    /* FP32 hi+lo split products, FP32 accumulation; FP64-class geometry and slot sums */
+#define SKG_FP64_EMULATED 2 /* FP64-accurate: double-float (FP32 pair) arithmetic throughout, exact FP64 output */
 
 /* Library version (major*10000 + minor*100 + patch). */
 int skg_version(void);
@@ -155,7 +156,9 @@ int skg_h1_assemble_tensor_tabulated(const skg_pattern *pattern,
 /*  coef_kind 1: d_coef per element (E,3,3), row-major A[i][j].          */
 /*  coef_kind 2: d_coef per element, component-first (3,3,E) (the        */
 /*  reference's public (3,3,E,Q) layout with the point axis dropped).     */
-/*  precision: SKG_FP64 or SKG_SPLIT_FP32.                               */
+/*  precision: SKG_FP64, SKG_FP64_EMULATED or SKG_SPLIT_FP32 (the last   */
+/*  two fall back to SKG_FP64 when the mesh or coefficient leaves FP32    */
+/*  range after a power-of-two rescaling).                                */
 /*  d_values (nnz) is overwritten.                                       */
 int skg_h1_assemble_affine(const skg_pattern *pattern, const double *d_p,
                            int64_t npts, const int32_t *d_t, int32_t nodes,

@@ -145,4 +145,17 @@ struct skg_pattern {
     skg::DevBuf<int32_t> indices;   // (nnz)
     skg::DevBuf<int32_t> inc_ptr;   // (n_rows+1) incidences per row
     skg::DevBuf<int32_t> inc;       // (E*row_local) e*row_local + i, ascending per row
+    // Row blocks for shared-memory accumulation: block b owns rows
+    // [blk_row0[b], blk_row0[b+1]); its slots fit kBlockSlots, its rows kBlockRows.
+    int32_t n_blocks = 0;
+    skg::DevBuf<int32_t> blk_row0;
+    // Incidence records (col_local <= 12 and every row shorter than 256):
+    // one int4 per incidence in `inc` order, x = e*row_local + i and the
+    // bytes of y, z, w = column offset within the row of each local column.
+    skg::DevBuf<int4> rec;
 };
+
+namespace skg {
+constexpr int kBlockRows = 256;
+constexpr int kBlockSlots = 8192;
+}  // namespace skg

@@ -13,6 +13,7 @@
 //      the unique ones (rows with more candidates than fit in shared memory
 //      use a slower repeated-minimum extraction over global memory).
 #include <climits>
+#include <vector>
 
 #include "skg_common.cuh"
 
@@ -186,7 +187,61 @@ __global__ void k_row_columns(const int32_t *inc_ptr, const int32_t *inc, const 
     if (mode == 0 && lane == 0) counts[r] = written;
 }
 
+// Thread per row: column offsets of every incidence's local columns.
+__global__ void k_records(int64_t n_rows, const int32_t *__restrict__ indptr, const int32_t *__restrict__ indices,
+                          const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
+                          const int32_t *__restrict__ col_dofs, int32_t row_local, int32_t col_local,
+                          int4 *__restrict__ rec) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    const int32_t rb = indptr[r], rn = indptr[r + 1] - rb;
+    const int32_t *cols = indices + rb;
+    for (int32_t it = inc_ptr[r]; it < inc_ptr[r + 1]; ++it) {
+        const int32_t item = inc[it];
+        const int64_t e = item / row_local;
+        unsigned w[3] = {0u, 0u, 0u};
+        for (int k = 0; k < col_local; ++k) {
+            const int pos = lower_bound_i32(cols, rn, col_dofs[e * col_local + k]);
+            w[k >> 2] |= (unsigned)(pos & 0xff) << (8 * (k & 3));
+        }
+        rec[it] = make_int4(item, (int)w[0], (int)w[1], (int)w[2]);
+    }
+}
+
 }  // namespace
+
+// Greedy partition of rows into blocks (<= kBlockRows rows, <= kBlockSlots
+// slots) and the incidence records; skipped when the pattern is unsuitable
+// (wide elements or rows of 256+ columns), in which case assemblies use the
+// per-row global-memory gather.
+void build_row_blocks(skg_pattern *p, cudaStream_t s) {
+    if (p->col_local > 12 || p->n_rows == 0) return;
+    std::vector<int32_t> ip(p->n_rows + 1);
+    SKG_CUDA(cudaMemcpyAsync(ip.data(), p->indptr.get(), ip.size() * 4, cudaMemcpyDeviceToHost, s));
+    SKG_CUDA(cudaStreamSynchronize(s));
+    std::vector<int32_t> blocks{0};
+    int64_t r = 0;
+    while (r < p->n_rows) {
+        const int64_t r0 = r;
+        if (ip[r + 1] - ip[r] > 255) return;
+        while (r < p->n_rows && r - r0 < kBlockRows && ip[r + 1] - ip[r0] <= kBlockSlots) {
+            if (ip[r + 1] - ip[r] > 255) return;
+            ++r;
+        }
+        if (r == r0) return;
+        blocks.push_back((int32_t)r);
+    }
+    p->n_blocks = (int32_t)blocks.size() - 1;
+    p->blk_row0 = DevBuf<int32_t>::owned(blocks.size());
+    SKG_CUDA(cudaMemcpyAsync(p->blk_row0.get(), blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice, s));
+    const int64_t n_inc = p->n_elements * p->row_local;
+    p->rec = DevBuf<int4>::owned(n_inc);
+    k_records<<<grid_for(p->n_rows, 128), 128, 0, s>>>(p->n_rows, p->indptr.get(), p->indices.get(),
+                                                       p->inc_ptr.get(), p->inc.get(), p->col_dofs.get(),
+                                                       p->row_local, p->col_local, p->rec.get());
+    SKG_LAUNCH_CHECK("records");
+    SKG_CUDA(cudaStreamSynchronize(s));
+}
 
 }  // namespace skg
 
@@ -267,6 +322,7 @@ extern "C" int skg_pattern_create(const int32_t *d_row_dofs, const int32_t *d_co
                                                                  p->indices.get());
             SKG_LAUNCH_CHECK("row_columns_write");
             SKG_CUDA(cudaStreamSynchronize(s));
+            build_row_blocks(p, s);
         } catch (...) {
             delete p;
             throw;

@@ -21,6 +21,7 @@ SKG_EUNSUPPORTED = 6
 
 SKG_FP64 = 0
 SKG_SPLIT_FP32 = 1
+SKG_FP64_EMULATED = 2
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64

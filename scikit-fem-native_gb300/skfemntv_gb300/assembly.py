@@ -21,11 +21,11 @@ import numpy as np
 from scipy.sparse import csr_matrix
 
 from . import _device as dev
-from ._native import SKG_FP64, SKG_SPLIT_FP32, call
+from ._native import SKG_FP64, SKG_FP64_EMULATED, SKG_SPLIT_FP32, call
 from .errors import UnsupportedNativeForm
 from .preflight import enforce_memory_budget, estimate_bilinear_memory
 
-PRECISIONS = {"fp64": SKG_FP64, "split_fp32": SKG_SPLIT_FP32}
+PRECISIONS = {"fp64": SKG_FP64, "fp64_emulated": SKG_FP64_EMULATED, "split_fp32": SKG_SPLIT_FP32}
 
 
 def _precision(name):

@@ -132,6 +132,39 @@ def test_p2_anisotropic_per_point_tabulated_path():
     assert relerr(K.data, data) < RTOL
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp64_emulated"])
+def test_p2_fp64_class_paths(precision):
+    """Native FP64 and the double-float (FP32-pair) path both meet the FP64 bar."""
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    K = sk.asm(aniso, b, A=Apub, precision=precision)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+    Ans = np.broadcast_to(np.moveaxis(g["Ans"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    assert relerr(sk.asm(aniso, b, A=Ans, precision=precision).data, g["ns_data"]) < RTOL
+
+
+@pytest.mark.parametrize("precision", ["fp64_emulated", "split_fp32"])
+def test_p1_reduced_paths(precision):
+    g = load_golden("p1_laplace")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X1, W1))
+    Kk = sk.asm(klap, b, kappa=g["kappa"][:, None], precision=precision)
+    assert relerr(Kk.data, g["kdata"]) < (RTOL if precision == "fp64_emulated" else 1e-7)
+
+
+def test_emulated_path_handles_extreme_scales():
+    """A mesh scaled by 1e-50 leaves FP32 range: the emulated path must still
+    return FP64-accurate values (it falls back to FP64)."""
+    g = load_golden("p1_laplace")
+    for scale in (1e-50, 1e40):
+        b = sk.Basis(sk.MeshTet(g["p"] * scale, g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1),
+                     quadrature=(X1, W1))
+        K = sk.asm(lap, b, precision="fp64_emulated")
+        assert relerr(K.data / scale, g["data"]) < RTOL
+
+
 def test_p2_split_precision_error_bound():
     g = load_golden("p2_aniso")
     b = p2_basis(g, (g["X"], g["W"]))
