@@ -306,9 +306,9 @@ def run_gpu(args, rank, world):
     npts_vertex = (N_CELLS + 1) ** 3
     bytes_elem = 24 * npts_vertex + 16 * E + 72 * E     # vertex coords + 4 vertex ids + A
     bytes_rows = 40 * E + 8 * nnz                       # 10 dof ids per element + CSR values
-    dominant = ("k_rows_block", bytes_rows, t_rows) if t_rows >= t_el else ("k_elem_fp64", bytes_elem, t_el)
+    dominant = ("k_rows_group", bytes_rows, t_rows) if t_rows >= t_el else ("k_elem_fp64", bytes_elem, t_el)
     achieved = dominant[1] / (dominant[2] * 1e-3) / 1e9
-    traffic = profiled_traffic() if dominant[0] == "k_rows_block" else None
+    traffic = profiled_traffic() if dominant[0] == "k_rows_group" else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -18,12 +18,12 @@
 // Passes.
 //  1. element pass (thread per element): G (4x4) from coordinates and the
 //     coefficient, written to a scratch array.
-//  2. row pass (CTA per row block): the block's CSR slots live in shared
-//     memory; one thread per row walks the row's incidence records
-//     (element, local row, column offsets) in ascending element order,
-//     evaluates row a of K_e on the fly and adds it into the row's slots;
-//     the block then writes its slot range out once, coalesced.  Every slot
-//     is summed by one thread in a fixed order: results are bitwise
+//  2. row pass (thread per CSR row, warp per group of up to 32 rows): the
+//     thread walks its row's incidence records (element, local row, column
+//     offsets) in ascending element order, evaluates row a of K_e on the fly
+//     and adds it into shared-memory accumulators of the row's slots; the
+//     warp then writes the group's slot range with coalesced stores.  Every
+//     slot is summed by one thread in a fixed order: results are bitwise
 //     reproducible, with no atomics.
 //
 // Precision modes.
@@ -38,7 +38,9 @@
 // The FP32-pair modes work in units scaled by 2^-s (s from the largest
 // vertex coordinate) so FP32 range holds; a mesh or coefficient outside that
 // range is detected in the element pass and re-run in FP64.
+#include <algorithm>
 #include <climits>
+#include <type_traits>
 #include <cmath>
 #include <vector>
 
@@ -84,59 +86,78 @@ __device__ __forceinline__ double load_coef(const double *__restrict__ coef, int
     return coef_kind == 1 ? coef[e * 9 + k] : coef[(int64_t)k * ne + e];
 }
 
-__global__ void k_elem_fp64(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
-                            int coef_kind, const double *__restrict__ coef, double *__restrict__ G) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    int32_t v[4];
-    const bool ok = load_vertices(t, ne, e, npts, v);
-    double J[9];
+constexpr int kElemBlock = 128;
+constexpr int kStagePad = 9;  // 8 x 16-byte chunks per element + 1 pad (bank-conflict-free staging)
+
+// Writes the block's staged G rows (8 x 16 bytes per element) to global
+// memory with coalesced 16-byte stores.
+__device__ __forceinline__ void flush_stage(const float4 *stage, float4 *Gout, int64_t e0, int64_t ne) {
+    __syncthreads();
+    const int64_t rest = ne - e0;
+    const int64_t nvalid = rest < kElemBlock ? rest : (int64_t)kElemBlock;
+    float4 *dst = Gout + e0 * 8;
+    for (int i = threadIdx.x; i < nvalid * 8; i += kElemBlock) dst[i] = stage[(i >> 3) * kStagePad + (i & 7)];
+}
+
+__global__ void __launch_bounds__(kElemBlock) k_elem_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                          const int32_t *__restrict__ t, int coef_kind,
+                                                          const double *__restrict__ coef, float4 *__restrict__ G) {
+    __shared__ float4 stage[kElemBlock * kStagePad];
+    const int64_t e0 = (int64_t)blockIdx.x * kElemBlock;
+    const int64_t e = e0 + threadIdx.x;
+    if (e < ne) {
+        int32_t v[4];
+        const bool ok = load_vertices(t, ne, e, npts, v);
+        double J[9];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const double x0 = p[i * npts + v[0]];
+        for (int i = 0; i < 3; ++i) {
+            const double x0 = p[i * npts + v[0]];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
-    }
-    double b[4][3];
-    b[1][0] = J[4] * J[8] - J[5] * J[7];
-    b[1][1] = J[2] * J[7] - J[1] * J[8];
-    b[1][2] = J[1] * J[5] - J[2] * J[4];
-    b[2][0] = J[5] * J[6] - J[3] * J[8];
-    b[2][1] = J[0] * J[8] - J[2] * J[6];
-    b[2][2] = J[2] * J[3] - J[0] * J[5];
-    b[3][0] = J[3] * J[7] - J[4] * J[6];
-    b[3][1] = J[1] * J[6] - J[0] * J[7];
-    b[3][2] = J[0] * J[4] - J[1] * J[3];
-    const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
+            for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
+        }
+        double b[4][3];
+        b[1][0] = J[4] * J[8] - J[5] * J[7];
+        b[1][1] = J[2] * J[7] - J[1] * J[8];
+        b[1][2] = J[1] * J[5] - J[2] * J[4];
+        b[2][0] = J[5] * J[6] - J[3] * J[8];
+        b[2][1] = J[0] * J[8] - J[2] * J[6];
+        b[2][2] = J[2] * J[3] - J[0] * J[5];
+        b[3][0] = J[3] * J[7] - J[4] * J[6];
+        b[3][1] = J[1] * J[6] - J[0] * J[7];
+        b[3][2] = J[0] * J[4] - J[1] * J[3];
+        const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
-    const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
-    double *g = G + e * 16;
-    if (coef_kind == 0) {
-        const double sc = (coef ? coef[e] : 1.0) * inv;
+        for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
+        const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
+        double g[16];
+        if (coef_kind == 0) {
+            const double sc = (coef ? coef[e] : 1.0) * inv;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+            for (int k = 0; k < 4; ++k)
 #pragma unroll
-            for (int l = k; l < 4; ++l) {
-                const double val = sc * (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]);
-                g[k * 4 + l] = val;
-                g[l * 4 + k] = val;
+                for (int l = k; l < 4; ++l) {
+                    const double val = sc * (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]);
+                    g[k * 4 + l] = val;
+                    g[l * 4 + k] = val;
+                }
+        } else {
+            double A[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                double Ab[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) Ab[i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) g[k * 4 + l] = inv * (b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2]);
             }
-    } else {
-        double A[9];
+        }
+        double2 *st = reinterpret_cast<double2 *>(stage + threadIdx.x * kStagePad);
 #pragma unroll
-        for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
-        double Ab[4][3];
-#pragma unroll
-        for (int l = 0; l < 4; ++l)
-#pragma unroll
-            for (int i = 0; i < 3; ++i) Ab[l][i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-#pragma unroll
-            for (int l = 0; l < 4; ++l)
-                g[k * 4 + l] = inv * (b[k][0] * Ab[l][0] + b[k][1] * Ab[l][1] + b[k][2] * Ab[l][2]);
+        for (int m = 0; m < 8; ++m) st[m] = make_double2(g[2 * m], g[2 * m + 1]);
     }
+    flush_stage(stage, G, e0, ne);
 }
 
 __device__ __forceinline__ bool df_in_range(df64 x) {
@@ -160,196 +181,403 @@ __global__ void k_scale(const double *__restrict__ p, int64_t n, int *__restrict
 }
 
 // Element pass in double-float.  G (scaled by 2^-s) as 16 df64.
-__global__ void k_elem_df64(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
-                            int coef_kind, const double *__restrict__ coef, const int *__restrict__ s_ptr,
-                            df64 *__restrict__ G, int *__restrict__ range_flag) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    const int s = *s_ptr;
-    int32_t v[4];
-    bool ok = load_vertices(t, ne, e, npts, v);
-    df64 J[9];
+__global__ void __launch_bounds__(kElemBlock, 6) k_elem_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                             const int32_t *__restrict__ t, int coef_kind,
+                                                             const double *__restrict__ coef,
+                                                             const int *__restrict__ s_ptr, float4 *__restrict__ G,
+                                                             int *__restrict__ range_flag, bool div30) {
+    __shared__ float4 stage[kElemBlock * kStagePad];
+    const int64_t e0 = (int64_t)blockIdx.x * kElemBlock;
+    const int64_t e = e0 + threadIdx.x;
+    if (e < ne) {
+        const int s = *s_ptr;
+        int32_t v[4];
+        bool ok = load_vertices(t, ne, e, npts, v);
+        df64 J[9];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const double x0 = p[i * npts + v[0]];
+        for (int i = 0; i < 3; ++i) {
+            const double x0 = p[i * npts + v[0]];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) J[i * 3 + r] = df_from_double(p[i * npts + v[r + 1]] - x0, -s, ok);
-    }
-    df64 b[4][3];
-#define SKG_CROSS(a, bb, c, d) df_sub(df_mul(J[a], J[bb]), df_mul(J[c], J[d]))
-    b[1][0] = SKG_CROSS(4, 8, 5, 7);
-    b[1][1] = SKG_CROSS(2, 7, 1, 8);
-    b[1][2] = SKG_CROSS(1, 5, 2, 4);
-    b[2][0] = SKG_CROSS(5, 6, 3, 8);
-    b[2][1] = SKG_CROSS(0, 8, 2, 6);
-    b[2][2] = SKG_CROSS(2, 3, 0, 5);
-    b[3][0] = SKG_CROSS(3, 7, 4, 6);
-    b[3][1] = SKG_CROSS(1, 6, 0, 7);
-    b[3][2] = SKG_CROSS(0, 4, 1, 3);
+            for (int r = 0; r < 3; ++r) J[i * 3 + r] = df_from_double(p[i * npts + v[r + 1]] - x0, -s, ok);
+        }
+        df64 b[4][3];
+#define SKG_CROSS(a, bb, c, d) df_add_fast(df_mul(J[a], J[bb]), df_neg(df_mul(J[c], J[d])))
+        b[1][0] = SKG_CROSS(4, 8, 5, 7);
+        b[1][1] = SKG_CROSS(2, 7, 1, 8);
+        b[1][2] = SKG_CROSS(1, 5, 2, 4);
+        b[2][0] = SKG_CROSS(5, 6, 3, 8);
+        b[2][1] = SKG_CROSS(0, 8, 2, 6);
+        b[2][2] = SKG_CROSS(2, 3, 0, 5);
+        b[3][0] = SKG_CROSS(3, 7, 4, 6);
+        b[3][1] = SKG_CROSS(1, 6, 0, 7);
+        b[3][2] = SKG_CROSS(0, 4, 1, 3);
 #undef SKG_CROSS
-    df64 det = df_add(df_add(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
+        df64 det = df_add_fast(df_add_fast(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
 #pragma unroll
-    for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add(df_add(b[1][i], b[2][i]), b[3][i]));
-    if (det.hi < 0.f) det = df_neg(det);
-    ok = ok && det.hi > 1e-30f;
-    const df64 inv = df_recip(det);
-    df64 *g = G + e * 16;
-    if (coef_kind == 0) {
-        df64 sc = inv;
-        if (coef) sc = df_mul(sc, df_from_double(coef[e], 0, ok));
+        for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add_fast(df_add_fast(b[1][i], b[2][i]), b[3][i]));
+        if (det.hi < 0.f) det = df_neg(det);
+        ok = ok && det.hi > 1e-30f;
+        df64 inv = df_recip(det);
+        // exact-rule P2 path: store G / 30 (the row pass multiplies by 30 T)
+        if (div30) inv = df_mul(inv, df64{0x1.111112p-5f, -0x1.dddddep-30f});
+        float2 *st = reinterpret_cast<float2 *>(stage + threadIdx.x * kStagePad);
+        if (coef_kind == 0) {
+            df64 sc = inv;
+            if (coef) sc = df_mul(sc, df_from_double(coef[e], 0, ok));
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+            for (int k = 0; k < 4; ++k)
 #pragma unroll
-            for (int l = k; l < 4; ++l) {
-                df64 d = df_add(df_add(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])), df_mul(b[k][2], b[l][2]));
-                d = df_mul(sc, d);
-                ok = ok && df_in_range(d);
-                g[k * 4 + l] = d;
-                g[l * 4 + k] = d;
-            }
-    } else {
-        df64 A[9];
+                for (int l = k; l < 4; ++l) {
+                    df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])),
+                                         df_mul(b[k][2], b[l][2]));
+                    d = df_mul(sc, d);
+                    ok = ok && df_in_range(d);
+                    st[k * 4 + l] = make_float2(d.hi, d.lo);
+                    st[l * 4 + k] = make_float2(d.hi, d.lo);
+                }
+        } else {
+            df64 A[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) A[k] = df_from_double(load_coef(coef, coef_kind, ne, e, k), 0, ok);
-        df64 Ab[4][3];
-#pragma unroll
-        for (int l = 0; l < 4; ++l)
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-                Ab[l][i] = df_add(df_add(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
-                                  df_mul(A[i * 3 + 2], b[l][2]));
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
+            for (int k = 0; k < 9; ++k) A[k] = df_from_double(load_coef(coef, coef_kind, ne, e, k), 0, ok);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
-                df64 d = df_add(df_add(df_mul(b[k][0], Ab[l][0]), df_mul(b[k][1], Ab[l][1])), df_mul(b[k][2], Ab[l][2]));
-                d = df_mul(inv, d);
-                ok = ok && df_in_range(d);
-                g[k * 4 + l] = d;
+                df64 Ab[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    Ab[i] = df_add_fast(df_add_fast(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
+                                        df_mul(A[i * 3 + 2], b[l][2]));
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], Ab[0]), df_mul(b[k][1], Ab[1])),
+                                         df_mul(b[k][2], Ab[2]));
+                    d = df_mul(inv, d);
+                    ok = ok && df_in_range(d);
+                    st[k * 4 + l] = make_float2(d.hi, d.lo);
+                }
             }
+        }
+        if (!ok) atomicExch(range_flag, 1);
     }
-    if (!ok) atomicExch(range_flag, 1);
+    flush_stage(stage, G, e0, ne);
 }
 
 // ------------------------------------------------------------ row pass
 
 enum { MODE_FP64 = 0, MODE_SPLIT = 1, MODE_DF64 = 2 };
 
-// Row pass over one row block.  Templated on the element size N (4 or 10)
-// and the precision mode.  Shared memory: kBlockSlots accumulators (8 bytes
-// each: double, or a df64 pair) + the T table + the support table.
-template <int N, int MODE>
-__global__ void __launch_bounds__(kBlockRows) k_rows_block(
-    const int32_t *__restrict__ blk_row0, const int32_t *__restrict__ indptr, const int32_t *__restrict__ inc_ptr,
-    const int4 *__restrict__ rec, const void *__restrict__ Gv, const double *__restrict__ Tg, Support sp,
-    const int *__restrict__ s_ptr, double *__restrict__ values) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    double *acc_d = reinterpret_cast<double *>(smem);
-    df64 *acc_f = reinterpret_cast<df64 *>(smem);
-    double *Td = reinterpret_cast<double *>(smem + kBlockSlots * 8);
-    df64 *Tf = reinterpret_cast<df64 *>(smem + kBlockSlots * 8 + N * N * 4 * 8);
-    int *sup = reinterpret_cast<int *>(smem + kBlockSlots * 8 + N * N * 4 * 16);
+// (hi, lo) += v without renormalising (renormalised once at write-out)
+__device__ __forceinline__ void df_acc(df64 &a, df64 v) {
+    const df64 sm = two_sum(a.hi, v.hi);
+    a.hi = sm.hi;
+    a.lo += sm.lo + v.lo;
+}
 
-    const int32_t r0 = blk_row0[blockIdx.x], r1 = blk_row0[blockIdx.x + 1];
-    const int32_t s0 = indptr[r0], s1 = indptr[r1];
-    const int nslots = s1 - s0;
-    for (int i = threadIdx.x; i < N * N * 4; i += blockDim.x) {
-        const double tv = Tg[i];
-        Td[i] = tv;
-        const float h = (float)tv;
-        Tf[i] = df64{h, (float)(tv - (double)h)};
-    }
-    if (threadIdx.x < N) {
-        sup[2 * threadIdx.x] = sp.sup[threadIdx.x][0];
-        sup[2 * threadIdx.x + 1] = sp.sup[threadIdx.x][1];
-    }
-    for (int i = threadIdx.x; i < nslots; i += blockDim.x) {
-        if (MODE == MODE_FP64) acc_d[i] = 0.0;
-        else acc_f[i] = df64{0.f, 0.f};
-    }
-    __syncthreads();
+constexpr int kRowWarps = 4;  // warps per CTA in the row pass
 
-    const int32_t r = r0 + (int32_t)threadIdx.x;
-    if (r < r1) {
-        const int base = indptr[r] - s0;
-        const int32_t it1 = inc_ptr[r + 1];
-        for (int32_t it = inc_ptr[r]; it < it1; ++it) {
-            const int4 rc = rec[it];
-            const int32_t item = rc.x;
-            const int32_t e = item / N;
-            const int a = item - e * N;
-            const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
-            const int ka0 = a < 4 ? a : sup[2 * a], ka1 = a < 4 ? a : sup[2 * a + 1];
-            const bool edge_a = ka1 != ka0;
-            if (MODE == MODE_FP64) {
-                const double *g = reinterpret_cast<const double *>(Gv) + (int64_t)e * 16;
-                double g0[4], g1[4];
+// Barycentric-support rows of G needed by local row a: g0 = G[ka0][:],
+// g1 = G[ka1][:] (zero for a single-vertex support).
+template <typename GT>
+struct GRows {
+    GT g0[4], g1[4];
+};
+
+// 16-byte vector loads of one G row (4 entries).
+__device__ __forceinline__ void load_g4(const double *__restrict__ G, double out[4]) {
+    const double2 x = __ldg(reinterpret_cast<const double2 *>(G));
+    const double2 y = __ldg(reinterpret_cast<const double2 *>(G) + 1);
+    out[0] = x.x; out[1] = x.y; out[2] = y.x; out[3] = y.y;
+}
+__device__ __forceinline__ void load_g4(const df64 *__restrict__ G, df64 out[4]) {
+    const float4 x = __ldg(reinterpret_cast<const float4 *>(G));
+    const float4 y = __ldg(reinterpret_cast<const float4 *>(G) + 1);
+    out[0] = df64{x.x, x.y}; out[1] = df64{x.z, x.w}; out[2] = df64{y.x, y.y}; out[3] = df64{y.z, y.w};
+}
+
+template <int N, typename GT>
+__device__ __forceinline__ void load_grows(const GT *__restrict__ Gbase, int4 rc, GRows<GT> &gr) {
+    const int32_t e = rc.x / N;
+    const int a = rc.x - e * N;
+    const int ka0 = sup_lo(a), ka1 = sup_hi(a);
+    const GT *G = Gbase + (int64_t)e * 16;
+    load_g4(G + ka0 * 4, gr.g0);
+    if (ka1 != ka0) {
+        load_g4(G + ka1 * 4, gr.g1);
+    } else {
 #pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    g0[l] = g[ka0 * 4 + l];
-                    g1[l] = edge_a ? g[ka1 * 4 + l] : 0.0;
-                }
+        for (int l = 0; l < 4; ++l) gr.g1[l] = GT{};
+    }
+}
+
+// Adds row a of K_e (incidence record rc, G rows gr) into the accumulators.
+// The N entries are computed first, then the N accumulators (distinct slots:
+// an element's columns are distinct) are loaded together, updated and stored,
+// so the shared-memory round trips overlap instead of forming a chain.
+template <int N, int MODE, typename GT>
+__device__ __forceinline__ void add_row(int4 rc, const GRows<GT> &gr, const double *__restrict__ Td,
+                                        const df64 *__restrict__ Tf, double *accd, df64 *accf, int base) {
+    const int32_t e = rc.x / N;
+    const int a = rc.x - e * N;
+    const bool edge_a = sup_hi(a) != sup_lo(a);
+    const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+    int off[N];
 #pragma unroll
-                for (int bb = 0; bb < N; ++bb) {
-                    const int kb0 = sup_lo(bb), kb1 = sup_hi(bb);
-                    const double *T = Td + (a * N + bb) * 4;
-                    double val = g0[kb0] * T[0];
-                    if (kb1 != kb0) val += g0[kb1] * T[1];
-                    if (edge_a) {
-                        val += g1[kb0] * T[2];
-                        if (kb1 != kb0) val += g1[kb1] * T[3];
-                    }
-                    const int off = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                    acc_d[off] += val;
-                }
-            } else {
-                const df64 *g = reinterpret_cast<const df64 *>(Gv) + (int64_t)e * 16;
-                df64 g0[4], g1[4];
+    for (int bb = 0; bb < N; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+    if constexpr (MODE == MODE_FP64) {
+        double val[N];
 #pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    g0[l] = g[ka0 * 4 + l];
-                    g1[l] = edge_a ? g[ka1 * 4 + l] : df64{0.f, 0.f};
-                }
+        for (int bb = 0; bb < N; ++bb) {
+            const int kb0 = sup_lo(bb), kb1 = sup_hi(bb);
+            const bool edge_b = kb1 != kb0;
+            const double *T = Td + (a * N + bb) * 4;
+            double v = gr.g0[kb0] * T[0];
+            if (edge_b) v += gr.g0[kb1] * T[1];
+            if (edge_a) {
+                v += gr.g1[kb0] * T[2];
+                if (edge_b) v += gr.g1[kb1] * T[3];
+            }
+            val[bb] = v;
+        }
+        double acc[N];
 #pragma unroll
-                for (int bb = 0; bb < N; ++bb) {
-                    const int kb0 = sup_lo(bb), kb1 = sup_hi(bb);
-                    const df64 *T = Tf + (a * N + bb) * 4;
-                    const bool edge_b = kb1 != kb0;
-                    df64 val;
-                    if (MODE == MODE_DF64) {
-                        val = df_mul(g0[kb0], T[0]);
-                        if (edge_b) val = df_add(val, df_mul(g0[kb1], T[1]));
-                        if (edge_a) {
-                            val = df_add(val, df_mul(g1[kb0], T[2]));
-                            if (edge_b) val = df_add(val, df_mul(g1[kb1], T[3]));
-                        }
-                    } else {
-                        // split products hi*hi (exact via FMA) + hi*lo + lo*hi, FP32 accumulation
-                        float hsum = 0.f, corr = 0.f;
-                        const df64 xs[4] = {g0[kb0], g0[kb1], g1[kb0], g1[kb1]};
-                        const bool use[4] = {true, edge_b, edge_a, edge_a && edge_b};
+        for (int bb = 0; bb < N; ++bb) acc[bb] = accd[off[bb]];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            if (!use[q]) continue;
-                            const df64 x = xs[q], y = T[q];
-                            const float ph = x.hi * y.hi;
-                            corr += fmaf(x.hi, y.hi, -ph) + fmaf(x.hi, y.lo, x.lo * y.hi);
-                            hsum += ph;
-                        }
-                        val = fast_two_sum(hsum, corr);
-                    }
-                    const int off = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                    acc_f[off] = df_add(acc_f[off], val);
+        for (int bb = 0; bb < N; ++bb) accd[off[bb]] = acc[bb] + val[bb];
+    } else {
+        df64 val[N];
+#pragma unroll
+        for (int bb = 0; bb < N; ++bb) {
+            const int kb0 = sup_lo(bb), kb1 = sup_hi(bb);
+            const bool edge_b = kb1 != kb0;
+            const df64 *T = Tf + (a * N + bb) * 4;
+            const df64 xs[4] = {gr.g0[kb0], gr.g0[kb1], gr.g1[kb0], gr.g1[kb1]};
+            float S = 0.f, L = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if ((q & 1) && !edge_b) continue;
+                if (q >= 2 && !edge_a) continue;
+                const df64 x = xs[q], y = T[q];
+                const float ph = x.hi * y.hi;
+                float err = fmaf(x.hi, y.hi, -ph);
+                err = fmaf(x.hi, y.lo, err);
+                err = fmaf(x.lo, y.hi, err);
+                if constexpr (MODE == MODE_DF64) {
+                    const df64 ts = two_sum(S, ph);
+                    S = ts.hi;
+                    L += ts.lo + err;
+                } else {
+                    S += ph;  // FP32 accumulation of the split products
+                    L += err;
                 }
             }
+            val[bb] = df64{S, L};
+        }
+        df64 acc[N];
+#pragma unroll
+        for (int bb = 0; bb < N; ++bb) acc[bb] = accf[off[bb]];
+#pragma unroll
+        for (int bb = 0; bb < N; ++bb) {
+            df_acc(acc[bb], val[bb]);
+            accf[off[bb]] = acc[bb];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- exact rule
+// For a quadrature rule that integrates quadratics exactly, 30 T^{kl}_ab of
+// P2 is an integer in {-1, 3, 4, 8}: with the reference tetrahedron integrals
+// int l_x l_y = (1 + d_xy) / 120, int l_x = 1/24, int 1 = 1/6, the supports
+// and coefficients above give
+//   vertex-vertex   (4 l_a - 1)(4 l_b - 1):  4 (1 + d_ab) - 5
+//   vertex-edge     (4 l_a - 1) 4 l_y:       4 (1 + d_ay) - 5
+//   edge-edge       4 l_x 4 l_y:             4 (1 + d_xy)
+// where x / y is the barycentric factor multiplying the support vertex.
+// The host checks the caller's rule against this table; the element pass
+// then stores G / 30 and the row pass multiplies by these compile-time
+// integers (exact double-float scalings).
+__host__ __device__ constexpr int factor_of(int a, int slot) {
+    // barycentric index whose (4 lambda) multiplies support slot `slot` of
+    // edge function a (slot 0 -> 4 lambda_j on vertex i, slot 1 -> 4 lambda_i on j)
+    return slot == 0 ? sup_hi(a) : sup_lo(a);
+}
+__host__ __device__ constexpr int t30(int a, int b, int sa, int sb) {
+    const bool ea = a >= 4, eb = b >= 4;
+    if (!ea && !eb) return 4 * (1 + (a == b)) - 5;
+    if (!ea && eb) return 4 * (1 + (a == factor_of(b, sb))) - 5;
+    if (ea && !eb) return 4 * (1 + (b == factor_of(a, sa))) - 5;
+    return 4 * (1 + (factor_of(a, sa) == factor_of(b, sb)));
+}
+
+// t * x for a small integer t, as an unnormalised double-float.
+template <int TV>
+__device__ __forceinline__ df64 df_mul_int(df64 x) {
+    if constexpr (TV == 1) return x;
+    else if constexpr (TV == -1) return df64{-x.hi, -x.lo};
+    else if constexpr (TV == 4 || TV == 8 || TV == -4 || TV == -8) return df64{x.hi * (float)TV, x.lo * (float)TV};
+    else {
+        const float ph = x.hi * (float)TV;
+        const float err = fmaf(x.hi, (float)TV, -ph);
+        return df64{ph, fmaf(x.lo, (float)TV, err)};
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ void sum_term(float &S, float &L, df64 t) {
+    if constexpr (MODE == MODE_DF64) {
+        const df64 ts = two_sum(S, t.hi);
+        S = ts.hi;
+        L += ts.lo + t.lo;
+    } else {
+        S += t.hi;
+        L += t.lo;
+    }
+}
+
+template <int A, int MODE>
+__device__ __forceinline__ void add_row_exact(const GRows<df64> &gr, df64 *accf, const int off[10]) {
+    constexpr int ka0 = sup_lo(A), ka1 = sup_hi(A);
+    constexpr bool edge_a = ka1 != ka0;
+    df64 val[10];
+#pragma unroll
+    for (int bb = 0; bb < 10; ++bb) {
+        const int kb0 = sup_lo(bb), kb1 = sup_hi(bb);
+        const bool edge_b = kb1 != kb0;
+        float S = 0.f, L = 0.f;
+        // slot pairs (sa, sb); the integer factors fold to immediates
+        switch (bb) {
+#define SKG_T(BB)                                                                                   \
+    case BB: {                                                                                      \
+        constexpr int kb0c = sup_lo(BB), kb1c = sup_hi(BB);                                         \
+        sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 0, 0)>(gr.g0[kb0c]));                            \
+        if constexpr (kb1c != kb0c) sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 0, 1)>(gr.g0[kb1c])); \
+        if constexpr (edge_a) {                                                                     \
+            sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 1, 0)>(gr.g1[kb0c]));                        \
+            if constexpr (kb1c != kb0c) sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 1, 1)>(gr.g1[kb1c])); \
+        }                                                                                           \
+    } break;
+            SKG_T(0) SKG_T(1) SKG_T(2) SKG_T(3) SKG_T(4) SKG_T(5) SKG_T(6) SKG_T(7) SKG_T(8) SKG_T(9)
+#undef SKG_T
+        }
+        (void)kb0; (void)kb1; (void)edge_b;
+        val[bb] = df64{S, L};
+    }
+    df64 acc[10];
+#pragma unroll
+    for (int bb = 0; bb < 10; ++bb) acc[bb] = accf[off[bb]];
+#pragma unroll
+    for (int bb = 0; bb < 10; ++bb) {
+        df_acc(acc[bb], val[bb]);
+        accf[off[bb]] = acc[bb];
+    }
+}
+
+// P2 rows with the exact-rule table: dispatch on the local row index so all
+// T factors are compile-time constants.
+template <int MODE>
+__device__ __forceinline__ void add_row_p2_exact(int4 rc, const GRows<df64> &gr, df64 *accf, int base) {
+    const int32_t e = rc.x / 10;
+    const int a = rc.x - e * 10;
+    const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+    int off[10];
+#pragma unroll
+    for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+    switch (a) {
+        case 0: add_row_exact<0, MODE>(gr, accf, off); break;
+        case 1: add_row_exact<1, MODE>(gr, accf, off); break;
+        case 2: add_row_exact<2, MODE>(gr, accf, off); break;
+        case 3: add_row_exact<3, MODE>(gr, accf, off); break;
+        case 4: add_row_exact<4, MODE>(gr, accf, off); break;
+        case 5: add_row_exact<5, MODE>(gr, accf, off); break;
+        case 6: add_row_exact<6, MODE>(gr, accf, off); break;
+        case 7: add_row_exact<7, MODE>(gr, accf, off); break;
+        case 8: add_row_exact<8, MODE>(gr, accf, off); break;
+        default: add_row_exact<9, MODE>(gr, accf, off); break;
+    }
+}
+
+// Row pass, P threads per CSR row (P = 1 for short rows, 2 for long rows).
+// Each warp owns one row group (<= 32 / P consecutive rows whose slots, times
+// P accumulator copies, fit SLOTS in shared memory).  Thread part p of row r
+// walks the row's incidence records p, p + P, p + 2P, ... (ascending element
+// order), evaluates row a of K_e on the fly and adds it into accumulator copy
+// p; the next record and its G rows are loaded one step ahead.  The warp
+// then sums the copies in copy order and writes the group's contiguous slot
+// range with coalesced stores.  Each (copy, slot) is updated by one thread in
+// a fixed order: bitwise reproducible, no atomics, no block-wide barrier
+// after the table load.
+template <int N, int MODE, int SLOTS, int P, bool EXACT>
+__global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
+    int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
+    const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec, const void *__restrict__ Gv,
+    const double *__restrict__ Tg, const int *__restrict__ s_ptr, double *__restrict__ values) {
+    using GT = typename std::conditional<MODE == MODE_FP64, double, df64>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *Td = reinterpret_cast<double *>(smem);
+    df64 *Tf = reinterpret_cast<df64 *>(smem);
+    unsigned char *warp_area = smem + N * N * 4 * 8;
+    for (int i = threadIdx.x; i < N * N * 4; i += blockDim.x) {
+        const double tv = Tg[i];
+        if constexpr (MODE == MODE_FP64) {
+            Td[i] = tv;
+        } else {
+            const float h = (float)tv;
+            Tf[i] = df64{h, (float)(tv - (double)h)};
         }
     }
     __syncthreads();
-    if (MODE == MODE_FP64) {
-        for (int i = threadIdx.x; i < nslots; i += blockDim.x) values[s0 + i] = acc_d[i];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kRowWarps + warp;
+    if (gi >= n_groups) return;
+    double *accd = reinterpret_cast<double *>(warp_area + (size_t)warp * SLOTS * 8);
+    df64 *accf = reinterpret_cast<df64 *>(accd);
+    const int2 grp = groups[gi];
+    const int32_t s0 = indptr[grp.x];
+    const int nslots = indptr[grp.y] - s0;
+    for (int j = lane; j < P * nslots; j += 32) {
+        if constexpr (MODE == MODE_FP64) accd[j] = 0.0;
+        else accf[j] = df64{0.f, 0.f};
+    }
+    __syncwarp();
+    const int ridx = lane / P, part = lane - (lane / P) * P;
+    const int32_t r = grp.x + ridx;
+    if (ridx < 32 / P && r < grp.y) {
+        const int base = indptr[r] - s0 + part * nslots;
+        const int32_t it1 = inc_ptr[r + 1];
+        int32_t it = inc_ptr[r] + part;
+        const GT *Gb = reinterpret_cast<const GT *>(Gv);
+        if (it < it1) {
+            int4 rc = rec[it];
+            GRows<GT> cur;
+            load_grows<N>(Gb, rc, cur);
+            int4 rcn = it + P < it1 ? rec[it + P] : make_int4(0, 0, 0, 0);
+            for (; it < it1; it += P) {
+                const bool has_next = it + P < it1;
+                GRows<GT> nxt;
+                if (has_next) load_grows<N>(Gb, rcn, nxt);
+                const int4 rcnn = it + 2 * P < it1 ? rec[it + 2 * P] : make_int4(0, 0, 0, 0);
+                if constexpr (EXACT && N == 10 && MODE != MODE_FP64) add_row_p2_exact<MODE>(rc, cur, accf, base);
+                else add_row<N, MODE>(rc, cur, Td, Tf, accd, accf, base);
+                rc = rcn;
+                rcn = rcnn;
+                if (has_next) cur = nxt;
+            }
+        }
+    }
+    __syncwarp();
+    if constexpr (MODE == MODE_FP64) {
+        for (int j = lane; j < nslots; j += 32) {
+            double v = accd[j];
+#pragma unroll
+            for (int c = 1; c < P; ++c) v += accd[c * nslots + j];
+            values[s0 + j] = v;
+        }
     } else {
-        const int s = *s_ptr;
-        for (int i = threadIdx.x; i < nslots; i += blockDim.x) values[s0 + i] = df_to_double(acc_f[i], s);
+        const int sc = *s_ptr;
+        for (int j = lane; j < nslots; j += 32) {
+            df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
+#pragma unroll
+            for (int c = 1; c < P; ++c) v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
+            values[s0 + j] = df_to_double(v, sc);
+        }
     }
 }
 
@@ -416,19 +644,41 @@ void affine_table(int nodes, int nq, const double *X, const double *W, std::vect
                 }
 }
 
-template <int N, int MODE>
-void launch_rows_block(const skg_pattern *pat, const void *G, const double *Tg, const Support &sp, const int *s_ptr,
-                       double *values, cudaStream_t s) {
-    const size_t smem = (size_t)kBlockSlots * 8 + (size_t)N * N * 4 * 16 + 2 * N * sizeof(int);
-    static bool configured = false;  // per instantiation; attribute set once per process
-    if (!configured) {
-        SKG_CUDA(cudaFuncSetAttribute(k_rows_block<N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
-    k_rows_block<N, MODE><<<pat->n_blocks, kBlockRows, smem, s>>>(pat->blk_row0.get(), pat->indptr.get(),
-                                                                  pat->inc_ptr.get(), pat->rec.get(), G, Tg, sp, s_ptr,
-                                                                  values);
-    SKG_LAUNCH_CHECK("rows_block");
+template <int N, int MODE, int SLOTS, int P, bool EXACT>
+void launch_group_class(int n_groups, const int2 *groups, const skg_pattern *pat, const void *G, const double *Tg,
+                        const int *s_ptr, double *values, cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)N * N * 4 * 8 + (size_t)kRowWarps * SLOTS * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_rows_group<N, MODE, SLOTS, P, EXACT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
+    k_rows_group<N, MODE, SLOTS, P, EXACT><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
+                                                                      pat->inc_ptr.get(), pat->rec.get(), G, Tg, s_ptr,
+                                                                      values);
+    SKG_LAUNCH_CHECK("rows_group");
+}
+
+template <int N, int MODE, bool EXACT = false>
+void launch_rows_groups(const skg_pattern *pat, const void *G, const double *Tg, const int *s_ptr, double *values,
+                        cudaStream_t s) {
+    launch_group_class<N, MODE, kGroupSlotsSmall, 1, EXACT>(pat->n_groups_small, pat->groups_small.get(), pat, G, Tg,
+                                                            s_ptr, values, s);
+    launch_group_class<N, MODE, kGroupSlotsLarge, 2, EXACT>(pat->n_groups_large, pat->groups_large.get(), pat, G, Tg,
+                                                            s_ptr, values, s);
+}
+
+// True when the caller's rule reproduces the exact P2 table (30 T integer).
+bool p2_rule_is_exact(const std::vector<double> &T) {
+    for (int a = 0; a < 10; ++a)
+        for (int b = 0; b < 10; ++b)
+            for (int sa = 0; sa < 2; ++sa)
+                for (int sb = 0; sb < 2; ++sb) {
+                    const bool used = (sa == 0 || sup_hi(a) != sup_lo(a)) && (sb == 0 || sup_hi(b) != sup_lo(b));
+                    const double want = used ? t30(a, b, sa, sb) / 30.0 : 0.0;
+                    if (std::fabs(T[(a * 10 + b) * 4 + sa * 2 + sb] - want) > 1e-13) return false;
+                }
+    return true;
 }
 
 }  // namespace
@@ -452,7 +702,8 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     DevBuf<double> Tg(T.size(), s);
     SKG_CUDA(cudaMemcpyAsync(Tg.get(), T.data(), T.size() * 8, cudaMemcpyHostToDevice, s));
     DevBuf<double> G((size_t)ne * 16, s);  // 16 doubles or 16 df64 pairs per element
-    const bool blocked = pat->n_blocks > 0;
+    const bool blocked = pat->max_row_len > 0;
+    const bool exact = nodes == 10 && blocked && precision != SKG_FP64 && p2_rule_is_exact(T);
     int mode = precision == SKG_FP64 ? MODE_FP64 : precision == SKG_SPLIT_FP32 ? MODE_SPLIT : MODE_DF64;
     if (!blocked) mode = MODE_FP64;
     DevBuf<int> misc(2, s);  // [0] scale exponent, [1] range flag
@@ -463,8 +714,9 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_LAUNCH_CHECK("scale");
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
         if (ne) {
-            k_elem_df64<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef, misc.get(),
-                                                         reinterpret_cast<df64 *>(G.get()), misc.get() + 1);
+            k_elem_df64<<<grid_for(ne, kElemBlock), kElemBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
+                                                                       misc.get(), reinterpret_cast<float4 *>(G.get()),
+                                                                       misc.get() + 1, exact);
             SKG_LAUNCH_CHECK("elem_df64");
         }
         int h_misc[2];
@@ -475,7 +727,8 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     if (mode == MODE_FP64) {
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
         if (ne) {
-            k_elem_fp64<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef, G.get());
+            k_elem_fp64<<<grid_for(ne, kElemBlock), kElemBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
+                                                                       reinterpret_cast<float4 *>(G.get()));
             SKG_LAUNCH_CHECK("elem_fp64");
         }
     }
@@ -493,15 +746,20 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_LAUNCH_CHECK("rows_global");
     } else {
         const int *sp_ptr = misc.get();
-#define SKG_ROWS(NN, MM) launch_rows_block<NN, MM>(pat, G.get(), Tg.get(), sp, sp_ptr, d_values, s)
+#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s)
         if (nodes == 4) {
             if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
             else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
             else SKG_ROWS(4, MODE_DF64);
         } else {
             if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
-            else if (mode == MODE_SPLIT) SKG_ROWS(10, MODE_SPLIT);
-            else SKG_ROWS(10, MODE_DF64);
+            else if (mode == MODE_SPLIT) {
+                if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s);
+                else SKG_ROWS(10, MODE_SPLIT);
+            } else {
+                if (exact) launch_rows_groups<10, MODE_DF64, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s);
+                else SKG_ROWS(10, MODE_DF64);
+            }
         }
 #undef SKG_ROWS
     }

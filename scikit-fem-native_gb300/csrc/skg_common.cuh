@@ -135,6 +135,11 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *b, int n, int32_t 
 
 }  // namespace skg
 
+namespace skg {
+constexpr int kGroupSlotsSmall = 768;
+constexpr int kGroupSlotsLarge = 2048;
+}  // namespace skg
+
 // Pattern handle (defined here so every translation unit sees the layout).
 struct skg_pattern {
     int64_t n_elements = 0, n_rows = 0, n_cols = 0, nnz = 0;
@@ -145,17 +150,18 @@ struct skg_pattern {
     skg::DevBuf<int32_t> indices;   // (nnz)
     skg::DevBuf<int32_t> inc_ptr;   // (n_rows+1) incidences per row
     skg::DevBuf<int32_t> inc;       // (E*row_local) e*row_local + i, ascending per row
-    // Row blocks for shared-memory accumulation: block b owns rows
-    // [blk_row0[b], blk_row0[b+1]); its slots fit kBlockSlots, its rows kBlockRows.
-    int32_t n_blocks = 0;
-    skg::DevBuf<int32_t> blk_row0;
+    // Longest row (columns); 0 when no incidence records were built.
+    int32_t max_row_len = 0;
+    // Row groups for the thread-per-row kernels: up to 32 consecutive rows
+    // whose slots fit a warp's shared-memory budget, split into a class of
+    // short groups (<= kGroupSlotsSmall slots) and long groups.  Each entry is
+    // (first row, end row).
+    int32_t n_groups_small = 0, n_groups_large = 0;
+    skg::DevBuf<int2> groups_small, groups_large;
     // Incidence records (col_local <= 12 and every row shorter than 256):
     // one int4 per incidence in `inc` order, x = e*row_local + i and the
     // bytes of y, z, w = column offset within the row of each local column.
     skg::DevBuf<int4> rec;
 };
 
-namespace skg {
-constexpr int kBlockRows = 256;
-constexpr int kBlockSlots = 8192;
-}  // namespace skg
+

@@ -56,6 +56,15 @@ __device__ __forceinline__ df64 df_add(df64 x, df64 y) {
     return fast_two_sum(s.hi, s.lo);
 }
 
+// Dekker's add: one TwoSum on the high parts, low parts added plainly.  Its
+// error is bounded relative to the operands (as for an FP64 addition), which
+// is all a geometric contraction needs; 11 instructions instead of 20.
+__device__ __forceinline__ df64 df_add_fast(df64 x, df64 y) {
+    df64 s = two_sum(x.hi, y.hi);
+    s.lo += x.lo + y.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+
 __device__ __forceinline__ df64 df_neg(df64 x) { return {-x.hi, -x.lo}; }
 
 __device__ __forceinline__ df64 df_sub(df64 x, df64 y) { return df_add(x, df_neg(y)); }

@@ -13,6 +13,7 @@
 //      the unique ones (rows with more candidates than fit in shared memory
 //      use a slower repeated-minimum extraction over global memory).
 #include <climits>
+#include <algorithm>
 #include <vector>
 
 #include "skg_common.cuh"
@@ -210,37 +211,91 @@ __global__ void k_records(int64_t n_rows, const int32_t *__restrict__ indptr, co
 
 }  // namespace
 
-// Greedy partition of rows into blocks (<= kBlockRows rows, <= kBlockSlots
-// slots) and the incidence records; skipped when the pattern is unsuitable
-// (wide elements or rows of 256+ columns), in which case assemblies use the
-// per-row global-memory gather.
-void build_row_blocks(skg_pattern *p, cudaStream_t s) {
+// First element referenced by each row (rows without incidences: INT_MAX).
+__global__ void k_first_element(int64_t n_rows, const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
+                                int32_t row_local, int32_t *__restrict__ first) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    first[r] = inc_ptr[r] < inc_ptr[r + 1] ? inc[inc_ptr[r]] / row_local : INT_MAX;
+}
+
+// Incidence records for the warp-per-row assembly kernels; skipped when the
+// pattern is unsuitable (elements wider than 12 columns or rows of 256+
+// columns), in which case assemblies use the per-row global-memory gather.
+void build_records(skg_pattern *p, cudaStream_t s) {
     if (p->col_local > 12 || p->n_rows == 0) return;
     std::vector<int32_t> ip(p->n_rows + 1);
     SKG_CUDA(cudaMemcpyAsync(ip.data(), p->indptr.get(), ip.size() * 4, cudaMemcpyDeviceToHost, s));
     SKG_CUDA(cudaStreamSynchronize(s));
-    std::vector<int32_t> blocks{0};
-    int64_t r = 0;
-    while (r < p->n_rows) {
-        const int64_t r0 = r;
-        if (ip[r + 1] - ip[r] > 255) return;
-        while (r < p->n_rows && r - r0 < kBlockRows && ip[r + 1] - ip[r0] <= kBlockSlots) {
-            if (ip[r + 1] - ip[r] > 255) return;
-            ++r;
-        }
-        if (r == r0) return;
-        blocks.push_back((int32_t)r);
-    }
-    p->n_blocks = (int32_t)blocks.size() - 1;
-    p->blk_row0 = DevBuf<int32_t>::owned(blocks.size());
-    SKG_CUDA(cudaMemcpyAsync(p->blk_row0.get(), blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice, s));
+    int32_t longest = 0;
+    for (int64_t r = 0; r < p->n_rows; ++r) longest = std::max(longest, ip[r + 1] - ip[r]);
+    if (longest > 255) return;
     const int64_t n_inc = p->n_elements * p->row_local;
     p->rec = DevBuf<int4>::owned(n_inc);
     k_records<<<grid_for(p->n_rows, 128), 128, 0, s>>>(p->n_rows, p->indptr.get(), p->indices.get(),
                                                        p->inc_ptr.get(), p->inc.get(), p->col_dofs.get(),
                                                        p->row_local, p->col_local, p->rec.get());
     SKG_LAUNCH_CHECK("records");
+    // Row groups.  A group first takes up to 32 consecutive rows within
+    // kGroupSlotsSmall slots (one thread per row); when fewer than 24 rows
+    // fit (long rows), it is re-formed as up to 16 rows within
+    // kGroupSlotsLarge / 2 slots, served by two threads per row with one
+    // accumulator copy each.
+    std::vector<int2> small, large;
+    int64_t r = 0;
+    while (r < p->n_rows) {
+        const int64_t r0 = r;
+        int64_t r1 = r0;
+        while (r1 < p->n_rows && r1 - r0 < 32 && ip[r1 + 1] - ip[r0] <= kGroupSlotsSmall) ++r1;
+        if (r1 - r0 >= 24 || r1 == p->n_rows) {
+            if (r1 == r0) r1 = r0 + 1;
+            small.push_back(make_int2((int)r0, (int)r1));
+        } else {
+            r1 = r0;
+            while (r1 < p->n_rows && r1 - r0 < 16 && ip[r1 + 1] - ip[r0] <= kGroupSlotsLarge / 2) ++r1;
+            if (r1 == r0) r1 = r0 + 1;  // single row above the budget (cannot happen below 256 columns)
+            large.push_back(make_int2((int)r0, (int)r1));
+        }
+        r = r1;
+    }
+    // Order the groups by the first element they reference, so that groups
+    // running at the same time touch a compact band of elements (their
+    // per-element data stays in L2).  Each group still owns a contiguous
+    // slot range, so the output writes stay coalesced.
+    {
+        DevBuf<int32_t> first(p->n_rows, s);
+        k_first_element<<<grid_for(p->n_rows, 256), 256, 0, s>>>(p->n_rows, p->inc_ptr.get(), p->inc.get(),
+                                                               p->row_local, first.get());
+        SKG_LAUNCH_CHECK("first_element");
+        std::vector<int32_t> fe(p->n_rows);
+        SKG_CUDA(cudaMemcpyAsync(fe.data(), first.get(), fe.size() * 4, cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        auto key = [&](const int2 &g) {
+            int32_t m = INT_MAX;
+            for (int32_t rr = g.x; rr < g.y; ++rr) m = std::min(m, fe[rr]);
+            return m;
+        };
+        for (auto *vec : {&small, &large}) {
+            std::vector<std::pair<int32_t, int2>> kv;
+            kv.reserve(vec->size());
+            for (const auto &g : *vec) kv.emplace_back(key(g), g);
+            std::stable_sort(kv.begin(), kv.end(),
+                             [](const std::pair<int32_t, int2> &x, const std::pair<int32_t, int2> &y) {
+                                 return x.first < y.first;
+                             });
+            for (size_t i = 0; i < kv.size(); ++i) (*vec)[i] = kv[i].second;
+        }
+    }
+    p->n_groups_small = (int32_t)small.size();
+    p->n_groups_large = (int32_t)large.size();
+    p->groups_small = DevBuf<int2>::owned(small.size());
+    p->groups_large = DevBuf<int2>::owned(large.size());
+    if (!small.empty())
+        SKG_CUDA(cudaMemcpyAsync(p->groups_small.get(), small.data(), small.size() * 8, cudaMemcpyHostToDevice, s));
+    if (!large.empty())
+        SKG_CUDA(cudaMemcpyAsync(p->groups_large.get(), large.data(), large.size() * 8, cudaMemcpyHostToDevice, s));
     SKG_CUDA(cudaStreamSynchronize(s));
+    p->max_row_len = longest;
 }
 
 }  // namespace skg
@@ -322,7 +377,7 @@ extern "C" int skg_pattern_create(const int32_t *d_row_dofs, const int32_t *d_co
                                                                  p->indices.get());
             SKG_LAUNCH_CHECK("row_columns_write");
             SKG_CUDA(cudaStreamSynchronize(s));
-            build_row_blocks(p, s);
+            build_records(p, s);
         } catch (...) {
             delete p;
             throw;
