@@ -235,6 +235,32 @@ int skg_linear_assemble_tabulated(const skg_pattern *pattern,
                                   const double *d_gradient, double *d_out,
                                   void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Adjoint of J = u^T K(kappa) v for P1 diffusion (no counterpart in    */
+/* the reference, which has no autograd; K(kappa) is the matrix of      */
+/* asm(w.kappa * ddot(grad u, grad v), basis), python/skfemntv/forms.py  */
+/* :276-374 with bilinear_form_assembler.cpp:79-105, assembled          */
+/* matrix-free).  d_t (4, E) vertex connectivity, d_dofs (E, 4) element */
+/* DOFs, kappa (E) or NULL = 1, u / v (N), wsum = sum of the quadrature  */
+/* weights.  Energy reduced in a fixed order into d_out (1 double).     */
+int skg_p1_energy(const double *d_p, int64_t npts, const int32_t *d_t,
+                  int64_t n_elements, const int32_t *d_dofs,
+                  const double *d_kappa, const double *d_u, const double *d_v,
+                  double wsum, double *d_out, void *stream);
+
+/* Gradients of grad_out * J: d_gkappa (E), d_gp (3, npts) (needs the
+ * incidence-only handle of the vertex connectivity, d_t^T with npts rows),
+ * d_gu / d_gv (N) (needs the incidence-only handle of the DOF map); any
+ * output may be NULL.  Geometry is recomputed, nothing is kept from the
+ * forward call. */
+int skg_p1_energy_grad(const skg_pattern *vertex_incidence,
+                       const skg_pattern *dof_incidence, const double *d_p,
+                       int64_t npts, const int32_t *d_t, int64_t n_elements,
+                       const int32_t *d_dofs, const double *d_kappa,
+                       const double *d_u, const double *d_v, double wsum,
+                       double grad_out, double *d_gkappa, double *d_gp,
+                       double *d_gu, double *d_gv, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,7 @@ the runtime controls and the memory preflight.  Assembly runs in hand-written
 CUDA kernels for sm_103a reached through the C ABI in
 ``include/skfem_gb300.h``.
 """
+from .adjoint import P1Energy
 from .basis import Basis, GeometryDiagnostics
 from .element import ElementTetP1, ElementTetP2, ElementVector
 from .errors import UnsupportedNativeForm
@@ -26,7 +27,7 @@ __version__ = "0.1.0"
 __all__ = [
     "AffineTetN1Basis", "AssemblyMemoryBudgetError", "AssemblyMemoryEstimate", "BACKEND", "Basis",
     "BilinearForm", "CAPABILITIES", "ElementTetP1", "ElementTetP2", "ElementVector", "GeometryDiagnostics",
-    "HcurlTetGeometryDiagnostics", "LinearForm", "MeshTet", "MeshTet2", "TetN1Assembler",
+    "HcurlTetGeometryDiagnostics", "LinearForm", "MeshTet", "MeshTet2", "P1Energy", "TetN1Assembler",
     "UnsupportedNativeForm", "asm", "available_num_threads", "ddot", "div", "dot", "enforce_memory_budget",
     "estimate_bilinear_memory", "estimate_tet_n1_assembly_memory", "format_bytes", "get_num_threads",
     "grad", "has_capability", "inner", "mul", "set_num_threads", "sym_grad", "thread_limit",

@@ -51,6 +51,9 @@ SIGNATURES = {
                         _i32, _vp, _vp],
     "skg_n1_assemble_pointwise": [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32,
                                   _i32, _vp, _vp],
+    "skg_p1_energy": [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp],
+    "skg_p1_energy_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double,
+                           ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
     "skg_linear_assemble_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp],
 }
