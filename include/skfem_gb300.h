@@ -178,6 +178,29 @@ int skg_h1_assemble_affine_profiled(const skg_pattern *pattern, const double *d_
                                     int32_t precision, double *d_values,
                                     float *h_kernel_ms, void *stream);
 
+/* Allocation-free variant of skg_h1_assemble_affine (no counterpart in
+ * the reference).  For callers that cannot let a library allocate device
+ * memory: applications that give all device memory to their own pool
+ * allocator and forbid other allocations, and solvers that re-assemble
+ * inside a time-stepping loop where cudaMalloc / cudaFree (which may
+ * synchronise the device) is not allowed.  Same arguments and results as
+ * skg_h1_assemble_affine; it calls no cudaMalloc, cudaFree or allocating
+ * library routine.  Its scratch is a fixed static device array of the
+ * library (32 MiB plus a small table), held on every GPU that loads the
+ * library until the process exits; meshes of more than
+ * SKG_NOALLOC_MAX_ELEMENTS elements are rejected with SKG_EINVAL.  The first
+ * call on a device looks up the array's device address on that device (so
+ * make that first call before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU (on different streams, or from
+ * different host threads) race and must be serialised by the caller. */
+#define SKG_NOALLOC_MAX_ELEMENTS 262144
+int skg_h1_assemble_affine_noalloc(const skg_pattern *pattern, const double *d_p,
+                                   int64_t npts, const int32_t *d_t, int32_t nodes,
+                                   int64_t n_elements, int32_t nq, const double *h_X,
+                                   const double *h_W, int32_t coef_kind,
+                                   const double *d_coef, int32_t precision,
+                                   double *d_values, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Nedelec N1 (lowest-order H(curl)) on affine tets.                    */
 

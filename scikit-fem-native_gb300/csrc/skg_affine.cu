@@ -40,6 +40,8 @@
 // range is detected in the element pass and re-run in FP64.
 #include <algorithm>
 #include <climits>
+#include <mutex>
+#include <string>
 #include <type_traits>
 #include <cmath>
 #include <vector>
@@ -805,5 +807,172 @@ extern "C" int skg_h1_assemble_affine_profiled(const skg_pattern *pat, const dou
             throw;
         }
         for (auto &e : ev) cudaEventDestroy(e);
+    });
+}
+
+// ----------------------------------------------------------------------------
+// Allocation-free variant of skg_h1_assemble_affine.
+//
+// Some callers cannot let a library call cudaMalloc: applications that hand
+// all device memory to their own pool allocator at start-up and forbid other
+// allocations, and time-stepping solvers that re-assemble inside a loop where
+// a cudaMalloc / cudaFree (which may synchronise the device) is not allowed.
+// This entry point computes exactly what skg_h1_assemble_affine computes, with
+// the same kernels, but its scratch (per-element G, the quadrature table, the
+// scale exponent and the range flag) lives in one file-scope device array of
+// fixed size instead of stream-ordered allocations.  The array is part of the
+// library's device image, so every GPU on which the library is loaded holds it
+// (kNoAllocBytes) until the process exits.
+namespace skg {
+namespace {
+
+constexpr int64_t kNoAllocMaxElements = 262144;  // SKG_NOALLOC_MAX_ELEMENTS
+constexpr size_t kNoAllocGBytes = (size_t)kNoAllocMaxElements * 16 * 8;
+constexpr size_t kNoAllocTBytes = 10 * 10 * 4 * 8;
+constexpr size_t kNoAllocBytes = kNoAllocGBytes + kNoAllocTBytes + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+unsigned char *g_noalloc_base[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device, looked up once
+// per device (host code cannot use the symbol itself: on the host its name
+// denotes a shadow variable, not device memory).
+unsigned char *noalloc_base() {
+    int dev = 0;
+    SKG_CUDA(cudaGetDevice(&dev));
+    require(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[dev]) {
+        void *ptr = nullptr;
+        SKG_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        g_noalloc_base[dev] = static_cast<unsigned char *>(ptr);
+    }
+    return g_noalloc_base[dev];
+}
+
+// The quadrature table T of affine_table, written into a caller array (no
+// host heap either).
+void affine_table_fixed(int nodes, int nq, const double *X, const double *W, double T[10 * 10 * 4]) {
+    for (int i = 0; i < 10 * 10 * 4; ++i) T[i] = 0.0;
+    auto coeff = [&](int a, int slot, int q) -> double {
+        const double x = X[q], y = X[nq + q], z = X[2 * nq + q];
+        const double lam[4] = {1.0 - x - y - z, x, y, z};
+        if (nodes == 4) return slot == 0 ? 1.0 : 0.0;
+        if (a < 4) return slot == 0 ? 4.0 * lam[a] - 1.0 : 0.0;
+        return slot == 0 ? 4.0 * lam[sup_hi(a)] : 4.0 * lam[sup_lo(a)];
+    };
+    for (int a = 0; a < nodes; ++a)
+        for (int b = 0; b < nodes; ++b)
+            for (int u = 0; u < 2; ++u)
+                for (int v = 0; v < 2; ++v) {
+                    if (u == 1 && sup_hi(a) == sup_lo(a)) continue;
+                    if (v == 1 && sup_hi(b) == sup_lo(b)) continue;
+                    double acc = 0.0;
+                    for (int q = 0; q < nq; ++q) acc += W[q] * coeff(a, u, q) * coeff(b, v, q);
+                    T[(a * nodes + b) * 4 + u * 2 + v] = acc;
+                }
+}
+
+bool p2_table_is_exact(const double *T) {
+    for (int a = 0; a < 10; ++a)
+        for (int b = 0; b < 10; ++b)
+            for (int sa = 0; sa < 2; ++sa)
+                for (int sb = 0; sb < 2; ++sb) {
+                    const bool used = (sa == 0 || sup_hi(a) != sup_lo(a)) && (sb == 0 || sup_hi(b) != sup_lo(b));
+                    const double want = used ? t30(a, b, sa, sb) / 30.0 : 0.0;
+                    if (std::fabs(T[(a * 10 + b) * 4 + sa * 2 + sb] - want) > 1e-13) return false;
+                }
+    return true;
+}
+
+}  // namespace
+}  // namespace skg
+
+extern "C" int skg_h1_assemble_affine_noalloc(const skg_pattern *pat, const double *d_p, int64_t npts,
+                                              const int32_t *d_t, int32_t nodes, int64_t ne, int32_t nq,
+                                              const double *h_X, const double *h_W, int32_t coef_kind,
+                                              const double *d_coef, int32_t precision, double *d_values,
+                                              void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(nodes == 4 || nodes == 10, "affine assembly supports P1 (4) and P2 (10) tetrahedra");
+        require(ne == pat->n_elements && pat->row_local == nodes && pat->col_local == nodes,
+                "mesh does not match the pattern");
+        require(ne <= kNoAllocMaxElements,
+                "allocation-free assembly supports at most " + std::to_string(kNoAllocMaxElements) +
+                    " elements (its scratch array is fixed); got " + std::to_string(ne) +
+                    ": use skg_h1_assemble_affine");
+        require(coef_kind == 0 || ((coef_kind == 1 || coef_kind == 2) && d_coef), "invalid coefficient kind");
+        require(precision == SKG_FP64 || precision == SKG_SPLIT_FP32 || precision == SKG_FP64_EMULATED,
+                "invalid precision");
+        require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+        require(d_p && d_t, "mesh arrays are NULL");
+        cudaStream_t s = as_stream(stream);
+        unsigned char *base = noalloc_base();
+        double *G = reinterpret_cast<double *>(base);
+        double *Tg = reinterpret_cast<double *>(base + kNoAllocGBytes);
+        int *misc = reinterpret_cast<int *>(base + kNoAllocGBytes + kNoAllocTBytes);
+        double T[10 * 10 * 4];
+        affine_table_fixed(nodes, nq, h_X, h_W, T);
+        // pageable source: the copy has read T before cudaMemcpyAsync returns
+        SKG_CUDA(cudaMemcpyAsync(Tg, T, (size_t)nodes * nodes * 4 * 8, cudaMemcpyHostToDevice, s));
+        const bool blocked = pat->max_row_len > 0;
+        const bool exact = nodes == 10 && blocked && precision != SKG_FP64 && p2_table_is_exact(T);
+        int mode = precision == SKG_FP64 ? MODE_FP64 : precision == SKG_SPLIT_FP32 ? MODE_SPLIT : MODE_DF64;
+        if (!blocked) mode = MODE_FP64;
+        if (mode != MODE_FP64) {
+            // the array keeps the previous call's contents: reset the scale and the flag
+            const int init[2] = {INT_MIN, 0};
+            SKG_CUDA(cudaMemcpyAsync(misc, init, sizeof(init), cudaMemcpyHostToDevice, s));
+            k_scale<<<64, 256, 0, s>>>(d_p, 3 * npts, misc);
+            SKG_LAUNCH_CHECK("scale");
+            if (ne) {
+                k_elem_df64<<<grid_for(ne, kElemBlock), kElemBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef, misc,
+                                                                           reinterpret_cast<float4 *>(G), misc + 1,
+                                                                           exact);
+                SKG_LAUNCH_CHECK("elem_df64");
+            }
+            int h_misc[2];
+            SKG_CUDA(cudaMemcpyAsync(h_misc, misc, sizeof(h_misc), cudaMemcpyDeviceToHost, s));
+            SKG_CUDA(cudaStreamSynchronize(s));
+            if (h_misc[1] != 0 || h_misc[0] == INT_MIN) mode = MODE_FP64;
+        }
+        if (mode == MODE_FP64 && ne) {
+            k_elem_fp64<<<grid_for(ne, kElemBlock), kElemBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
+                                                                       reinterpret_cast<float4 *>(G));
+            SKG_LAUNCH_CHECK("elem_fp64");
+        }
+        if (!blocked) {
+            Support sp{};
+            for (int a = 0; a < 10; ++a) { sp.sup[a][0] = sup_lo(a); sp.sup[a][1] = sup_hi(a); }
+            const unsigned grid = grid_for(pat->n_rows, 128);
+            if (nodes == 4)
+                k_rows_global<4><<<grid, 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
+                                                      pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(), G, Tg,
+                                                      sp, d_values);
+            else
+                k_rows_global<10><<<grid, 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
+                                                       pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(), G, Tg,
+                                                       sp, d_values);
+            SKG_LAUNCH_CHECK("rows_global");
+            return;
+        }
+        if (nodes == 4) {
+            if (mode == MODE_FP64) launch_rows_groups<4, MODE_FP64>(pat, G, Tg, misc, d_values, s);
+            else if (mode == MODE_SPLIT) launch_rows_groups<4, MODE_SPLIT>(pat, G, Tg, misc, d_values, s);
+            else launch_rows_groups<4, MODE_DF64>(pat, G, Tg, misc, d_values, s);
+        } else {
+            if (mode == MODE_FP64) launch_rows_groups<10, MODE_FP64>(pat, G, Tg, misc, d_values, s);
+            else if (mode == MODE_SPLIT) {
+                if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G, Tg, misc, d_values, s);
+                else launch_rows_groups<10, MODE_SPLIT>(pat, G, Tg, misc, d_values, s);
+            } else {
+                if (exact) launch_rows_groups<10, MODE_DF64, true>(pat, G, Tg, misc, d_values, s);
+                else launch_rows_groups<10, MODE_DF64>(pat, G, Tg, misc, d_values, s);
+            }
+        }
     });
 }

@@ -46,6 +46,8 @@ SIGNATURES = {
                                _i32, _vp, _vp],
     "skg_h1_assemble_affine_profiled": [_vp, _vp, _i64, _vp, _i32, _i64, _vp, _i32, _vp, _vp, _i32,
                                         _vp, _i32, _vp, ctypes.POINTER(ctypes.c_float), _vp],
+    "skg_h1_assemble_affine_noalloc": [_vp, _vp, _i64, _vp, _i32, _i64, _i32, _vp, _vp, _i32, _vp, _i32,
+                                       _vp, _vp],
     "skg_edge_topology": [_vp, _i64, _vp, _vp, _vp, _i64p, _i64p, _vp],
     "skg_n1_assemble": [_vp, _vp, _i64, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _i32,
                         _i32, _vp, _vp],
