@@ -81,14 +81,29 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.samples = []
+
+    def _reader(self):
+        for ln in self.proc.stdout:
+            if ln.strip():
+                self.samples.append((time.perf_counter(), ln))
 
     def __enter__(self):
+        """Starts sampling every 50 ms and returns once the first sample is in,
+        so that the sampler is live when the timed region starts."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._reader, daemon=True)
+        self.thread.start()
+        t_end = time.perf_counter() + 5.0
+        while not self.samples and time.perf_counter() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.t_start = time.perf_counter()
         return self
 
     def __exit__(self, *exc):
@@ -96,11 +111,12 @@ class ClockSampler:
         if self.proc is not None:
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                self.proc.wait()
+            self.thread.join(timeout=5)
+            self.lines = [ln for t, ln in self.samples if t >= self.t_start]
 
     def summary(self):
         sm, smax, reasons = [], None, set()
@@ -168,6 +184,15 @@ def run_reference(args, rank):
     if rank != 0:
         return
     threads = host_threads()
+    if args.workload != "p2_aniso":
+        cb = aux_cpu_baseline(args.workload, threads, reps=max(1, args.steps))
+        line = {"impl": "reference", "metric": AUX_METRIC[args.workload], "value": cb["value"], "unit": cb["unit"],
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": args.workload, "sample": cb["sample"]}, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     sample = OracleSample(REFERENCE_SAMPLE_CELLS, threads)
     for _ in range(args.warmup):
         sample.step()
@@ -197,11 +222,11 @@ def measured_peak():
 
 
 def profiled_traffic():
-    """DRAM bytes per launch of the row pass from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_affine_rows_p2_aniso_64.txt")
+    """DRAM bytes of one FP64 row pass (64^3) from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_affine_fp64_p2_aniso_48.md")
     try:
         for ln in open(path):
-            if ln.startswith("dram_bytes_per_launch_full:"):
+            if ln.startswith("dram_bytes_per_row_pass_full:"):
                 return float(ln.split(":")[1])
     except OSError:
         pass
@@ -219,7 +244,7 @@ def run_gpu(args, rank, world):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     rng = np.random.default_rng(np.random.SeedSequence(SEED))
-    p, t = jittered_cube(N_CELLS, rng, lambda *a: (lambda m: (m.p, m.t))(sk.MeshTet.init_tensor(*a)))
+    p, t = jittered_cube(args.cells, rng, lambda *a: (lambda m: (m.p, m.t))(sk.MeshTet.init_tensor(*a)))
     m2 = sk.MeshTet2.from_mesh(sk.MeshTet(p, t))
     X, W = rule4()
     basis = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(X, W))
@@ -273,7 +298,7 @@ def run_gpu(args, rank, world):
 
     results = {}
     reference_values = None
-    for mode in ("fp64", "fp64_emulated", "split_fp32"):
+    for mode in args.modes:
         ms, t_el, t_rows, clk = time_mode(mode)
         vals = form.target.d_values[:nnz].clone()
         if reference_values is None:
@@ -284,7 +309,7 @@ def run_gpu(args, rank, world):
         results[mode] = {"value": world * nnz / (ms * 1e-3), "ms_per_step": ms,
                          "kernel_ms": {"element_pass": t_el, "row_pass": t_rows},
                          "max_rel_err_vs_fp64": err, "clocks": clk}
-    head = results["fp64"]
+    head = results[args.modes[0]]
     ms, t_el, t_rows = head["ms_per_step"], head["kernel_ms"]["element_pass"], head["kernel_ms"]["row_pass"]
     value = head["value"]
 
@@ -303,18 +328,22 @@ def run_gpu(args, rank, world):
 
     # ---- roofline of the dominant kernel (headline mode)
     peak, peak_kind = measured_peak()
-    npts_vertex = (N_CELLS + 1) ** 3
+    npts_vertex = (args.cells + 1) ** 3
     bytes_elem = 24 * npts_vertex + 16 * E + 72 * E     # vertex coords + 4 vertex ids + A
     bytes_rows = 40 * E + 8 * nnz                       # 10 dof ids per element + CSR values
     dominant = ("k_rows_group", bytes_rows, t_rows) if t_rows >= t_el else ("k_elem_fp64", bytes_elem, t_el)
     achieved = dominant[1] / (dominant[2] * 1e-3) / 1e9
-    traffic = profiled_traffic() if dominant[0] == "k_rows_group" else None
+    traffic = profiled_traffic() if dominant[0] == "k_rows_group" and args.cells == N_CELLS else None
 
+    config = dict(CONFIG, cells=args.cells, parallelism=f"replicas x{world}" if world > 1 else "single GPU")
+    if args.cells != N_CELLS:
+        config.update(workload=f"P2-tet anisotropic diffusion, {args.cells}^3x6 jittered cube (profiling size)",
+                      elements=E, dofs=basis.N, nnz=nnz)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered cube, seeded SPD tensors)",
-        "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "config": config,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(A_cf.nbytes),
                 "d2h_bytes_per_step": int(8 * nnz), "ms_per_step": 1e3 * e2e_s},
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak,
@@ -337,14 +366,377 @@ def run_gpu(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- other rows of the path
+#
+# --workload selects one of the other assembly paths; each prints one JSON
+# line with the same keys.  Algorithmic bytes per call are the inputs read
+# plus the outputs written once (coordinates, connectivity, coefficients,
+# result values); the roofline is taken over the whole call.
+
+X1 = np.array([[0.25], [0.25], [0.25]])
+W1 = np.array([1.0 / 6.0])
+AUX_METRIC = {
+    "p1_laplace": "assembled CSR nnz/s (FP64 P1-tet Laplace)",
+    "n1_maxwell": "assembled CSR nnz/s (FP64 Nedelec N1 Maxwell)",
+    "p1_adjoint": "adjoint elements/s (J = u^T K(kappa) v with dJ/dkappa, dJ/dx, dJ/du, dJ/dv, P1)",
+    "nh": "neo-Hookean residual+tangent elements/s (FP64 plain law)",
+}
+
+
+def _timer(args, world):
+    import torch
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        barrier()
+        stream = torch.cuda.current_stream()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(torch.cuda.current_device()) as clocks:
+            barrier()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            ev1.record(stream)
+            barrier()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        if world > 1:
+            tt = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, clocks.summary()
+
+    def wall(fn):
+        for _ in range(2):
+            fn()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        barrier()
+        return (time.perf_counter() - t0) / args.steps
+
+    return timed, wall
+
+
+def _roofline(alg_bytes, ms):
+    peak, kind = measured_peak()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "whole call", "achieved": achieved, "peak": peak,
+            "peak_kind": f"{kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "algorithmic_bytes_per_launch": alg_bytes}
+
+
+def _relerr(a, b):
+    return float((a - b).abs().max() / b.abs().max())
+
+
+def sine_displacement(doflocs, seed=5, amplitude=0.05):
+    """Vector P1 displacement: 8 modes amplitude * d_m sin(pi k_m . x + phi_m)
+    with seeded unit directions d_m, phases phi_m and unit wavevectors
+    k_m = +-e_axis (node-major DOFs, component fastest)."""
+    rng = np.random.default_rng(np.random.SeedSequence(seed))
+    n = doflocs.shape[1]
+    u = np.zeros(n)
+    comp = np.arange(n) % 3
+    for _ in range(8):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        kv = np.zeros(3)
+        kv[rng.integers(0, 3)] = rng.choice([-1.0, 1.0])
+        ph = rng.uniform(0, 2 * np.pi)
+        u += amplitude * d[comp] * np.sin(np.pi * (kv @ doflocs) + ph)
+    return u
+
+
+def _p1_mesh(sk, n, comp=1):
+    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+    return m, sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=comp), quadrature=(X1, W1))
+
+
+def wl_p1_laplace(args, world, timed, wall):
+    """Plain P1 Laplace a(u,v) = grad u . grad v, 32^3 x 6 cube, 1-point rule, coefficient 1."""
+    import skfemntv_gb300 as sk
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    n = args.cells or 32
+    m, b = _p1_mesh(sk, n)
+    form = NativeBilinearForm(b)
+    nnz, E = form.pattern.nnz, m.nelements
+    variants, ref = {}, None
+    for mode in ("fp64", "fp64_emulated", "split_fp32"):
+        ms, clk = timed(lambda: form.assemble_device(gradient=1.0, precision=mode))
+        vals = form.target.d_values[:nnz].clone()
+        ref = vals if ref is None else ref
+        variants[mode] = {"value": world * nnz / (ms * 1e-3), "ms_per_step": ms,
+                          "max_rel_err_vs_fp64": _relerr(vals, ref), "clocks": clk}
+
+    @sk.BilinearForm
+    def lap(u, v, w):
+        return sk.ddot(sk.grad(u), sk.grad(v))
+
+    e2e_s = wall(lambda: sk.asm(lap, b))
+    alg = 24 * m.p.shape[1] + 16 * E + 8 * nnz
+    head = variants["fp64"]
+    return dict(
+        metric=AUX_METRIC["p1_laplace"], unit="nnz/s", value=head["value"],
+        ms_per_step=head["ms_per_step"], dtype="f64", clocks=head["clocks"],
+        config={"workload": f"P1-tet Laplace, {n}^3x6 cube ({E} tets), 1-point rule, coefficient 1",
+                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs smaller than L2 (latency-bound size)"},
+        e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 0,
+             "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
+        roofline=_roofline(alg, head["ms_per_step"]), precision_variants=variants,
+        gpu_launches=3 * args.steps)
+
+
+def wl_n1_maxwell(args, world, timed, wall):
+    """Nedelec N1 curl-curl + mass, 48^3 x 6 cube with seeded vertex relabelling,
+    mu_e = exp(N(0, 0.3^2)), curl coefficient 1/mu_e, mass coefficient 1."""
+    import skfemntv_gb300 as sk
+    from skfemntv_gb300 import _device as dev
+    from skfemntv_gb300._native import call
+
+    n = args.cells or 48
+    rng = np.random.default_rng(np.random.SeedSequence(3))
+    m0 = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+    perm = rng.permutation(m0.p.shape[1])
+    inv = np.argsort(perm)
+    mesh = sk.MeshTet(np.ascontiguousarray(m0.p[:, inv]), perm[m0.t].astype(m0.t.dtype))
+    mu = np.exp(rng.normal(0.0, 0.3, mesh.nelements))
+    nb = sk.AffineTetN1Basis(mesh)
+    asmb = sk.TetN1Assembler(nb)
+    E, Q = nb.mesh.nelements, len(nb.W)
+    nnz = asmb.pattern.nnz
+    dnu = dev.to_device(1.0 / mu, np.float64)
+
+    def step():
+        call("skg_n1_assemble", asmb.pattern.h, dev.ptr(nb.mesh._dev("p")), nb.mesh.p.shape[1], dev.ptr(nb._t4),
+             dev.ptr(nb._ee_dev), dev.ptr(nb._signs_dev), E, Q, dev.hptr(nb.X), dev.hptr(nb.W), None, dev.ptr(dnu),
+             1, 1, 0, dev.ptr(asmb.target.d_values), dev.stream_ptr())
+
+    ms, clk = timed(step)
+    curl = (1.0 / mu)[:, None]
+    e2e_s = wall(lambda: asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=curl))
+    alg = 24 * mesh.p.shape[1] + 16 * E + 24 * E + 8 * E + 8 * nnz
+    return dict(
+        metric=AUX_METRIC["n1_maxwell"], unit="nnz/s", value=world * nnz / (ms * 1e-3),
+        ms_per_step=ms, dtype="f64", clocks=clk,
+        config={"workload": f"N1 curl-curl + mass, {n}^3x6 cube ({E} tets), relabelled vertices, "
+                            f"{Q}-point Duffy rule, curl coefficient 1/mu_e, mass 1",
+                "elements": E, "dofs": nb.N, "nnz": nnz, "l2": "inputs larger than L2"},
+        e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 8 * E,
+             "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
+        roofline=_roofline(alg, ms), gpu_launches=2 * args.steps)
+
+
+def wl_p1_adjoint(args, world, timed, wall):
+    """J = u^T K(kappa) v on P1, 64^3 x 6 cube: J and dJ/dkappa, dJ/dx, dJ/du, dJ/dv."""
+    import torch
+
+    import skfemntv_gb300 as sk
+
+    n = args.cells or 64
+    rng = np.random.default_rng(np.random.SeedSequence(4))
+    m, b = _p1_mesh(sk, n)
+    E, npts = m.nelements, m.p.shape[1]
+    op = sk.P1Energy(b)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    kappa = torch.as_tensor(np.exp(rng.standard_normal(E)), **f64)
+    coords = torch.as_tensor(m.p, **f64).contiguous()
+    u = torch.as_tensor(rng.standard_normal(b.N), **f64)
+    v = torch.as_tensor(rng.standard_normal(b.N), **f64)
+
+    def step():
+        op.energy(kappa, coords, u, v)
+        op.gradients(kappa, coords, u, v)
+
+    ms, clk = timed(step)
+    hk, hu, hv = (x.cpu().numpy() for x in (kappa, u, v))
+    pin = [torch.empty(x.shape, dtype=torch.float64, pin_memory=True) for x in (hk, hu, hv)]
+    for dst, src in zip(pin, (hk, hu, hv)):
+        dst.numpy()[:] = src
+
+    def e2e():
+        k = pin[0].to("cuda", non_blocking=True).requires_grad_(True)
+        x = coords.detach().clone().requires_grad_(True)
+        J = op(k, x, pin[1].to("cuda", non_blocking=True), pin[2].to("cuda", non_blocking=True))
+        J.backward()
+        return float(J), k.grad.cpu(), x.grad.cpu()
+
+    e2e_s = wall(e2e)
+    alg = 24 * npts + 16 * E + 8 * E + 16 * b.N + 8 * E + 24 * npts
+    return dict(
+        metric=AUX_METRIC["p1_adjoint"], unit="elements/s",
+        value=world * E / (ms * 1e-3), ms_per_step=ms, dtype="f64", clocks=clk,
+        config={"workload": f"P1 energy adjoint, {n}^3x6 cube ({E} tets), kappa_e = exp(N(0,1)), u, v ~ N(0,1)",
+                "elements": E, "dofs": b.N, "l2": "inputs smaller than L2 (68 MB per call)"},
+        e2e={"value": world * E / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": 8 * (E + 2 * b.N),
+             "d2h_bytes_per_step": 8 * (E + 3 * npts), "ms_per_step": 1e3 * e2e_s},
+        roofline=_roofline(alg, ms), gpu_launches=5 * args.steps)
+
+
+def wl_nh(args, world, timed, wall):
+    """Vector P1 neo-Hookean residual + tangent, 64^3 x 6 cube, mu = 1, lambda = 10:
+    plain FP64 law against the GPU-trained MLP energy surrogate."""
+    import torch
+
+    import skfemntv_gb300 as sk
+    from skfemntv_gb300 import _device as dev
+
+    n = args.cells or 64
+    m, b = _p1_mesh(sk, n, comp=3)
+    E = m.nelements
+    nh = sk.NeoHookean(b, 1.0, 10.0)
+    nnz = nh.pattern.nnz
+    u = sine_displacement(b.doflocs)
+    du = dev.to_device(u, np.float64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sur = sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    ms_plain, clk = timed(lambda: nh.assemble_device(du))
+    r0 = nh.d_res[: b.N].clone()
+    k0 = nh.target.d_values[:nnz].clone()
+    ms_sur, clk_s = timed(lambda: nh.assemble_device(du, surrogate=sur, tol=1e-2, count_fallback=False))
+    nh.assemble_device(du, surrogate=sur, tol=1e-2)
+    fallback = nh.last_fallback
+    err_r = _relerr(nh.d_res[: b.N], r0)
+    err_k = _relerr(nh.target.d_values[:nnz], k0)
+    hu = torch.empty(b.N, dtype=torch.float64, pin_memory=True)
+    hu.numpy()[:] = u
+    e2e_s = wall(lambda: nh.assemble(hu.numpy()))
+    alg = 24 * m.p.shape[1] + 16 * E + 2 * 8 * b.N + 8 * nnz
+    return dict(
+        metric=AUX_METRIC["nh"], unit="elements/s",
+        value=world * E / (ms_plain * 1e-3), ms_per_step=ms_plain, dtype="f64", clocks=clk,
+        config={"workload": f"vector P1 neo-Hookean, {n}^3x6 cube ({E} tets), 8 sine modes amplitude 0.05, "
+                            "unit wavevectors, mu=1, lambda=10, 1-point rule",
+                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
+        e2e={"value": world * E / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": 8 * b.N,
+             "d2h_bytes_per_step": 8 * (b.N + nnz), "ms_per_step": 1e3 * e2e_s},
+        roofline=_roofline(alg, ms_plain),
+        learned_closure={"value": world * E / (ms_sur * 1e-3), "ms_per_step": ms_sur,
+                         "speedup_vs_plain": ms_plain / ms_sur, "max_rel_err_residual": err_r,
+                         "max_rel_err_tangent": err_k, "fallback_elements": fallback,
+                         "training_seconds": t_train, "training_history": sur.history[-2:],
+                         "roofline": _roofline(alg, ms_sur), "clocks": clk_s},
+        gpu_launches=3 * args.steps)
+
+
+AUX_WORKLOADS = {"p1_laplace": wl_p1_laplace, "n1_maxwell": wl_n1_maxwell, "p1_adjoint": wl_p1_adjoint,
+                 "nh": wl_nh}
+
+
+def run_aux(args, rank, world):
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    timed, wall = _timer(args, world)
+    r = AUX_WORKLOADS[args.workload](args, world, timed, wall)
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"), "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": r.pop("dtype"),
+            "data": "synthetic (seeded)"}
+    line.update(r)
+    line["config"]["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = aux_cpu_baseline(args.workload, host_threads())
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def aux_cpu_baseline(workload, threads, reps=3):
+    """The oracle (CPU restatement of the reference's assembly) on a bounded
+    sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    def mesh(n):
+        return O.mesh_tet_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+
+    if workload == "p1_laplace":
+        n = 32
+        p, t = mesh(n)
+        b = O.make_basis(p, t, False, quadrature=(X1, W1), threads=threads)
+        dofs = b.dofs3.reshape(b.dofs3.shape[0], -1)
+        pat = O.Pattern(dofs, dofs)
+        grad = np.ones(b.dx.shape)
+        run = lambda: O.bilinear_assemble(b, gradient=grad, threads=threads, pattern=pat)  # noqa: E731
+        units, unit, desc = pat.nnz, "nnz/s", f"P1 Laplace {n}^3x6 (full size), threaded colored assembly"
+    elif workload == "n1_maxwell":
+        n = 24
+        p, t = mesh(n)
+        b = O.make_n1_basis(p, t)
+        pat = O.Pattern(np.ascontiguousarray(b.element_dofs.T), nrows=b.N, coloring=False)
+        curl = np.ones(b.dx.shape)
+        run = lambda: O.n1_assemble_maxwell(b, 1.0, curl, threads=threads, pattern=pat)  # noqa: E731
+        units, unit, desc = pat.nnz, "nnz/s", f"N1 Maxwell {n}^3x6 sample, threaded element integration + scatter"
+    elif workload == "p1_adjoint":
+        n = 32
+        p, t = mesh(n)
+        rng = np.random.default_rng(4)
+        b = O.make_basis(p, t, False, quadrature=(X1, W1), threads=threads)
+        E = t.shape[1]
+        kappa = np.exp(rng.standard_normal(E))
+        u, v = rng.standard_normal(b.N), rng.standard_normal(b.N)
+        dofs = b.dofs3.reshape(E, -1)
+        pat = O.Pattern(dofs, dofs)
+
+        def run():
+            data, indptr, indices = O.bilinear_assemble(b, gradient=kappa[:, None], threads=threads, pattern=pat)
+            import scipy.sparse as sp
+            J = u @ (sp.csr_matrix((data, indices, indptr), shape=(b.N, b.N)) @ v)
+            gu = np.einsum("ea,eaj->ej", u[dofs], b.grad[:, 0])
+            gv = np.einsum("ea,eaj->ej", v[dofs], b.grad[:, 0])
+            return J, np.einsum("ej,ej->e", gu, gv) * b.dx[:, 0]
+
+        units, unit, desc = E, "elements/s", (f"P1 {n}^3x6 sample: J via assembled K and dJ/dkappa "
+                                              "(no coordinate gradient)")
+    else:
+        n = 24
+        p, t = mesh(n)
+        b = O.make_basis(p, t, False, comp=3, quadrature=(X1, W1), threads=threads)
+        u = sine_displacement(np.repeat(p, 3, axis=1))
+        dofs = b.dofs3.reshape(b.dofs3.shape[0], -1)
+        pat = O.Pattern(dofs, dofs)
+
+        def run():
+            Gu = O.displacement_gradient(b, u)
+            r = O.linear_assemble(b, gradient=O.nh_first_piola(Gu, 1.0, 10.0))
+            return r, O.cross_gradient_tensor_assemble(b, O.nh_tangent(Gu, 1.0, 10.0), threads=threads,
+                                                       pattern=pat)
+
+        units, unit, desc = t.shape[1], "elements/s", f"neo-Hookean {n}^3x6 sample: numpy law + oracle assembly"
+    run()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        run()
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": units / dt, "unit": unit, "cores": threads, "kind": "port", "sample": f"{desc}, {reps} runs"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="p2_aniso", choices=["p2_aniso"] + sorted(AUX_WORKLOADS),
+                    help="p2_aniso (headline) or another row of the assembly path")
+    ap.add_argument("--cells", type=int, default=None, help="cube cells per side (smaller cases for profiling)")
+    ap.add_argument("--modes", default="fp64,fp64_emulated,split_fp32",
+                    help="precision modes to time; the first is the headline")
     args = ap.parse_args()
+    args.modes = [m for m in args.modes.split(",") if m]
+    if args.workload == "p2_aniso" and args.cells is None:
+        args.cells = N_CELLS
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -357,7 +749,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     try:
-        run_gpu(args, rank, world)
+        if args.workload == "p2_aniso":
+            run_gpu(args, rank, world)
+        else:
+            run_aux(args, rank, world)
     finally:
         if world > 1:
             import torch

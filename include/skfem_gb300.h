@@ -284,6 +284,67 @@ int skg_p1_energy_grad(const skg_pattern *vertex_incidence,
                        double grad_out, double *d_gkappa, double *d_gp,
                        double *d_gu, double *d_gv, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Neo-Hookean residual and tangent on vector P1 tetrahedra.  Replaces   */
+/* the reference's oracle pipeline for the law of                        */
+/* benchmarks/skfem_neo_hookean.py:8-52: NativeLinearForm residual        */
+/* (linear_form_assembler.cpp:41-154) + NativeCrossBilinearForm tensor    */
+/* tangent (cross_bilinear_assembler.cpp:207-247).  Pattern: element DOFs */
+/* (E, 12), with CSR columns when the tangent is wanted.  u (N); outputs  */
+/* d_residual (N) and d_values (nnz), either may be NULL.                 */
+int skg_nh_assemble(const skg_pattern *pattern, const double *d_p, int64_t npts,
+                    const int32_t *d_t, int64_t n_elements, const double *d_u,
+                    double mu, double lmbda, double wsum, double *d_residual,
+                    double *d_values, void *stream);
+
+/* Learned closure (no counterpart in the reference): an MLP
+ * 3 -> 64 -> 64 -> 1 (tanh) with a linear input -> output skip, on the
+ * invariant features (I1-3, I2-3, ln J), predicts the strain energy; float32
+ * parameters, skg_mlp_param_count() floats (weights, then feature mean/std,
+ * output scale/shift and the stress-normalisation constant). */
+int skg_mlp_param_count(void);
+/* Training samples F = I + G, G_ij ~ N(0, sigma^2) from a counter-based
+ * generator; features (n, 3) and targets (n, 4) = W, dW/df (plain law). */
+int skg_mlp_dataset(int64_t n, uint64_t seed, double sigma, double mu,
+                    double lmbda, float *d_features, float *d_targets,
+                    void *stream);
+/* Loss (energy + beta * feature-gradient misfit, normalised units) and its
+ * gradient over samples perm[offset .. offset+batch) (mod n); fixed-order
+ * reduction. */
+int skg_mlp_loss_grad(const float *d_params, const float *d_features,
+                      const float *d_targets, int64_t n, const int64_t *d_perm,
+                      int64_t offset, int32_t batch, float beta, float *d_grad,
+                      float *d_loss, void *stream);
+/* `steps` Adam steps (cosine learning-rate schedule lr0 -> lr_min) on the
+ * device; h_last_loss receives the last batch loss.  Sets the
+ * stress-normalisation constant of the final weights. */
+int skg_mlp_train(float *d_params, const float *d_features,
+                  const float *d_targets, int64_t n, const int64_t *d_perm,
+                  int32_t steps, int32_t batch, float lr0, float lr_min,
+                  float beta, float *d_adam_m, float *d_adam_v, int32_t step0,
+                  float *h_last_loss, void *stream);
+/* L-BFGS refinement (history `history`, Armijo backtracking) over the fixed
+ * samples perm[offset .. offset+count) (mod n): loss and gradient on the
+ * device, two-loop recursion on the host in FP64; up to `iters` iterations,
+ * *h_loss receives the final loss.  Sets the stress-normalisation constant. */
+int skg_mlp_refine(float *d_params, const float *d_features,
+                   const float *d_targets, int64_t n, const int64_t *d_perm,
+                   int64_t offset, int32_t count, int32_t iters, int32_t history,
+                   float beta, double *h_loss, void *stream);
+/* psi, d psi/dx (3), d2 psi/dx2 (9) per normalised input x (n, 3) -> (n, 13). */
+int skg_mlp_eval(const float *d_params, const float *d_x, int64_t n,
+                 float *d_out, void *stream);
+/* Neo-Hookean residual / tangent with the MLP energy; elements whose
+ * features leave the trained box d_box = (min[3], max[3]) or whose stress
+ * differs from the plain law by more than tol (relative) use the FP64
+ * plain law; *h_fallback receives their number (synchronous when given). */
+int skg_nh_assemble_surrogate(const skg_pattern *pattern, const double *d_p,
+                              int64_t npts, const int32_t *d_t, int64_t n_elements,
+                              const double *d_u, double mu, double lmbda,
+                              double wsum, const float *d_params,
+                              const float *d_box, float tol, double *d_residual,
+                              double *d_values, int64_t *h_fallback, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

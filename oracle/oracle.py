@@ -534,3 +534,68 @@ def nh_energy(F, mu, lmbda):
     I1 = np.einsum("...ij,...ij->...", F, F)
     lnJ = np.log(J)
     return 0.5 * mu * (I1 - 3.0) - mu * lnJ + 0.5 * lmbda * lnJ ** 2
+
+
+# --------------------------------------------------------------------------
+# Energy surrogate network (no counterpart in the reference): FP64 numpy
+# restatement of the MLP 3 -> 64 -> 64 -> 1 (tanh) with a linear skip
+# (psi = w3 . z2 + b3 + c . x) and of its training loss, the checker for the
+# GPU network kernels.  Parameter layout: W1 (64,3), b1, W2 (64,64), b2,
+# w3 (64), b3, c (3), then f_mean (3), f_std (3), y_scale, y_shift, stress
+# shift.
+
+MLP_H = 64
+
+
+def mlp_unpack(params):
+    p = np.asarray(params, dtype=np.float64)
+    H = MLP_H
+    o = 0
+    W1 = p[o:o + 3 * H].reshape(H, 3); o += 3 * H
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    w3 = p[o:o + H]; o += H
+    b3 = p[o]; o += 1
+    c = p[o:o + 3]; o += 3
+    norm = p[o:o + 9]
+    return W1, b1, W2, b2, w3, b3, c, norm
+
+
+MLP_N_TRAINABLE = 3 * MLP_H + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1 + 3
+
+
+def mlp_eval(params, x):
+    """psi, grad psi (n,3), Hessian (n,3,3) at normalised inputs x (n,3)."""
+    W1, b1, W2, b2, w3, b3, c, _ = mlp_unpack(params)
+    x = np.asarray(x, dtype=np.float64)
+    z1 = np.tanh(x @ W1.T + b1)
+    s1 = 1 - z1 ** 2
+    z2 = np.tanh(z1 @ W2.T + b2)
+    s2 = 1 - z2 ** 2
+    psi = z2 @ w3 + b3 + x @ c
+    d2 = s2 * w3
+    u1 = d2 @ W2
+    d1 = s1 * u1
+    g = d1 @ W1 + c
+    Hm = np.empty((x.shape[0], 3, 3))
+    for m in range(3):
+        da1 = W1[:, m][None, :]
+        dz1 = s1 * da1
+        da2 = dz1 @ W2.T
+        dd2 = -2 * z2 * s2 * da2 * w3
+        du1 = dd2 @ W2
+        dd1 = -2 * z1 * s1 * da1 * u1 + s1 * du1
+        Hm[:, :, m] = dd1 @ W1
+    return psi, g, Hm
+
+
+def mlp_loss(params, feats, tgts, beta=1.0):
+    """Mean of (psi - t)^2 + beta |grad psi - t'|^2 in normalised units."""
+    norm = mlp_unpack(params)[-1]
+    fm, fs, ys, yc = norm[:3], norm[3:6], norm[6], norm[7]
+    x = (np.asarray(feats, np.float64) - fm) / fs
+    t = (np.asarray(tgts[:, 0], np.float64) - yc) / ys
+    tg = np.asarray(tgts[:, 1:], np.float64) * fs / ys
+    psi, g, _ = mlp_eval(params, x)
+    return float(np.mean((psi - t) ** 2 + beta * np.sum((g - tg) ** 2, axis=1)))

@@ -168,18 +168,24 @@ __device__ __forceinline__ bool df_in_range(df64 x) {
 }
 
 // Scale exponent s: vertex coordinates times 2^-s are at most 1 in magnitude.
+// The largest |x| is found on the bit patterns (for non-negative doubles the
+// integer order of the bits is the numeric order), so the scan runs on the
+// integer pipes; only the winner's exponent is decoded.
 __global__ void k_scale(const double *__restrict__ p, int64_t n, int *__restrict__ s_out) {
-    __shared__ int smax;
-    if (threadIdx.x == 0) smax = INT_MIN;
-    __syncthreads();
-    int m = INT_MIN;
+    unsigned long long m = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double a = fabs(p[i]);
-        if (a > 0.0) m = max(m, ilogb(a) + 1);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(p[i]) & 0x7fffffffffffffffULL;
+        if (b < 0x7ff0000000000000ULL) m = b > m ? b : m;  // finite values only
     }
-    atomicMax(&smax, m);
-    __syncthreads();
-    if (threadIdx.x == 0) atomicMax(s_out, smax);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long q = __shfl_xor_sync(0xffffffffu, m, o);
+        m = q > m ? q : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m != 0) {
+        const double a = __longlong_as_double((long long)m);
+        atomicMax(s_out, ilogb(a) + 1);
+    }
 }
 
 // Element pass in double-float.  G (scaled by 2^-s) as 16 df64.
@@ -712,7 +718,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     if (mode != MODE_FP64) {
         const int init[2] = {INT_MIN, 0};
         SKG_CUDA(cudaMemcpyAsync(misc.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
-        k_scale<<<64, 256, 0, s>>>(d_p, 3 * npts, misc.get());
+        k_scale<<<2 * kSmCount, 256, 0, s>>>(d_p, 3 * npts, misc.get());
         SKG_LAUNCH_CHECK("scale");
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
         if (ne) {
@@ -927,7 +933,7 @@ extern "C" int skg_h1_assemble_affine_noalloc(const skg_pattern *pat, const doub
             // the array keeps the previous call's contents: reset the scale and the flag
             const int init[2] = {INT_MIN, 0};
             SKG_CUDA(cudaMemcpyAsync(misc, init, sizeof(init), cudaMemcpyHostToDevice, s));
-            k_scale<<<64, 256, 0, s>>>(d_p, 3 * npts, misc);
+            k_scale<<<2 * kSmCount, 256, 0, s>>>(d_p, 3 * npts, misc);
             SKG_LAUNCH_CHECK("scale");
             if (ne) {
                 k_elem_df64<<<grid_for(ne, kElemBlock), kElemBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef, misc,

@@ -14,6 +14,9 @@
 
 namespace skg {
 
+// GB300: 152 SMs (two dies of 76); grid-stride kernels size their grids by it.
+constexpr int kSmCount = 152;
+
 // ---------------------------------------------------------------- errors
 
 struct Error : std::runtime_error {

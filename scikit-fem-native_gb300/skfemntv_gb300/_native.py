@@ -56,10 +56,23 @@ SIGNATURES = {
     "skg_p1_energy": [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp],
     "skg_p1_energy_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double,
                            ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
+    "skg_nh_assemble": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                        _vp, _vp, _vp],
+    "skg_mlp_param_count": [],
+    "skg_mlp_dataset": [_i64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
+    "skg_mlp_loss_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _i32, ctypes.c_float, _vp, _vp, _vp],
+    "skg_mlp_train": [_vp, _vp, _vp, _i64, _vp, _i32, _i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                      _vp, _vp, _i32, ctypes.POINTER(ctypes.c_float), _vp],
+    "skg_mlp_refine": [_vp, _vp, _vp, _i64, _vp, _i64, _i32, _i32, _i32, ctypes.c_float,
+                       ctypes.POINTER(ctypes.c_double), _vp],
+    "skg_mlp_eval": [_vp, _vp, _i64, _vp, _vp],
+    "skg_nh_assemble_surrogate": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double, _vp, _vp, ctypes.c_float, _vp, _vp, _i64p, _vp],
     "skg_linear_assemble_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp],
 }
 _RESTYPE = {"skg_last_error": ctypes.c_char_p}
+_NO_STATUS = {"skg_mlp_param_count", "skg_version"}
 
 _lib = None
 
@@ -113,4 +126,7 @@ def check(status: int):
 
 
 def call(name: str, *args):
-    check(getattr(load(), name)(*args))
+    result = getattr(load(), name)(*args)
+    if name not in _NO_STATUS:
+        check(result)
+    return result
