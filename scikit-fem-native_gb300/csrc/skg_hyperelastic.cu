@@ -12,15 +12,23 @@
 //   r_(a,c)          = V sum_j P_cj g_a,j
 //   K_(a,i),(b,k)    = V [ mu d_ik (g_a . g_b) + (mu - lambda ln J) h_b,i h_a,k
 //                          + lambda h_a,i h_b,k ]
-// (the contraction of A with g_a and g_b written out).  One thread per element
-// computes the 12 residual and 144 tangent entries; they are summed into the
-// residual vector and the CSR values by the fixed-order gathers (one thread
-// per DOF / CSR row, element order), so results are bitwise reproducible.
+// (the contraction of A with g_a and g_b written out).
+//
+// Fused path (patterns with row groups): one thread per element writes a
+// 36-double record (g, h = F^-T g, V P and three scaled moduli); the row pass
+// below evaluates each CSR row's 12 entries per incident element from the
+// records and sums them in shared-memory slots in element order, together
+// with the row's residual entry.  Nothing of size 144 per element is stored.
+// Without row groups, one thread per element writes the 144 tangent and 12
+// residual entries, summed by the fixed-order gathers.  Either way the results
+// are bitwise reproducible (no atomics).
 //
 // The surrogate entry point replaces the law by a small MLP on the
 // invariants (see skg_mlp.cu) with a per-element fallback to this law.
 #include "skg_common.cuh"
+#include "skg_df64.cuh"
 #include "skg_nh.cuh"
+#include "skg_nh_rows.cuh"
 
 namespace skg {
 
@@ -42,6 +50,230 @@ __global__ void k_nh_element(int64_t ne, const double *__restrict__ p, int64_t n
     write_nh_element(g, law, mu, lmbda, Ke ? Ke + e * 144 : nullptr, re ? re + e * 12 : nullptr);
 }
 
+// Plain records for the fused row pass.
+__global__ void k_nh_plain_record(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                  const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
+                                  const double *__restrict__ u, double mu, double lmbda, double wsum,
+                                  double *__restrict__ rec) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    NhGeom g;
+    nh_geometry(p, npts, t, ne, e, wsum, g);
+    double Gu[9];
+    displacement_gradient(g, dofs + e * 12, u, Gu);
+    NhLaw law;
+    nh_plain_law(Gu, mu, lmbda, law);
+    double r[kNhRecD];
+    write_plain_record(g, law, mu, lmbda, r);
+    double2 *out = reinterpret_cast<double2 *>(rec + e * kNhRecD);
+#pragma unroll
+    for (int k = 0; k < kNhRecD / 2; ++k) out[k] = make_double2(r[2 * k], r[2 * k + 1]);
+}
+
+// ------------------------------------------------------------------ row pass
+
+constexpr int kNhWarps = 4;
+
+// Row a_l = 3a + i of element e (plain record) -> val[12] and the residual term.
+__device__ __forceinline__ void nh_plain_row(const double *__restrict__ R, int a, int i, double val[12],
+                                             double &rr) {
+    double ga[3], ha[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        ga[j] = R[a * 3 + j];
+        ha[j] = R[12 + a * 3 + j];
+    }
+    const double muV = R[33], c2V = R[34], lamV = R[35];
+    double alpha[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) alpha[k] = c2V * ha[k];
+    const double beta = lamV * ha[i];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        double gb[3], hb[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            gb[j] = R[b * 3 + j];
+            hb[j] = R[12 + b * 3 + j];
+        }
+        const double gam = muV * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
+        double hbi = hb[0];
+        if (i == 1) hbi = hb[1];
+        if (i == 2) hbi = hb[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double v = alpha[k] * hbi + beta * hb[k];
+            if (k == i) v += gam;
+            val[b * 3 + k] = v;
+        }
+    }
+    const double *PV = R + 24 + 3 * i;
+    rr = PV[0] * ga[0] + PV[1] * ga[1] + PV[2] * ga[2];
+}
+
+// Row of element e from the surrogate record (FP32).
+__device__ __forceinline__ void nh_surrogate_row(const float *__restrict__ R, int a, int i, float val[12],
+                                                 float &rr) {
+    float gall[12];
+    const float4 *G4 = reinterpret_cast<const float4 *>(R + 84);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float4 v = __ldg(G4 + q);
+        gall[4 * q] = v.x; gall[4 * q + 1] = v.y; gall[4 * q + 2] = v.z; gall[4 * q + 3] = v.w;
+    }
+    float Ai[28];
+    const float4 *A4 = reinterpret_cast<const float4 *>(R + 28 * i);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const float4 v = __ldg(A4 + q);
+        Ai[4 * q] = v.x; Ai[4 * q + 1] = v.y; Ai[4 * q + 2] = v.z; Ai[4 * q + 3] = v.w;
+    }
+    float ga[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        ga[j] = a == 0 ? gall[j] : a == 1 ? gall[3 + j] : a == 2 ? gall[6 + j] : gall[9 + j];
+    }
+    // w_kL = sum_J g_a,J (V A)_iJkL
+    float w[9];
+#pragma unroll
+    for (int kl = 0; kl < 9; ++kl) w[kl] = ga[0] * Ai[kl] + ga[1] * Ai[9 + kl] + ga[2] * Ai[18 + kl];
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            val[b * 3 + k] = w[k * 3] * gall[b * 3] + w[k * 3 + 1] * gall[b * 3 + 1] + w[k * 3 + 2] * gall[b * 3 + 2];
+    const float *PV = R + 96 + 3 * i;
+    rr = __ldg(PV) * ga[0] + __ldg(PV + 1) * ga[1] + __ldg(PV + 2) * ga[2];
+}
+
+__device__ __forceinline__ df64 df_split(double v) {
+    const float h = (float)v;
+    return df64{h, (float)(v - (double)h)};
+}
+
+// Row groups as in the affine row pass: one warp per group of CSR rows, P
+// threads per row walking its incidences in element order, per-copy slot
+// sums in shared memory, summed in copy order and written coalesced.  SUR:
+// surrogate records (FP32 entries, double-float slot sums) with plain FP64
+// records for the elements flagged as fallback; otherwise plain records and
+// FP64 slot sums.
+template <bool SUR, int SLOTS, int P>
+__global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
+    int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
+    const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec_inc, const double *__restrict__ recd,
+    const float *__restrict__ recf, const unsigned char *__restrict__ flags, double *__restrict__ residual,
+    double *__restrict__ values) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kNhWarps + warp;
+    if (gi >= n_groups) return;
+    double *accd = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
+    df64 *accf = reinterpret_cast<df64 *>(accd);
+    const int2 grp = groups[gi];
+    const int32_t s0 = indptr[grp.x];
+    const int nslots = indptr[grp.y] - s0;
+    for (int j = lane; j < P * nslots; j += 32) {
+        if constexpr (SUR) accf[j] = df64{0.f, 0.f};
+        else accd[j] = 0.0;
+    }
+    __syncwarp();
+    const int ridx = lane / P, part = lane - (lane / P) * P;
+    const int32_t r = grp.x + ridx;
+    const bool live = ridx < 32 / P && r < grp.y;
+    double rd = 0.0;
+    df64 rf{0.f, 0.f};
+    if (live) {
+        const int base = indptr[r] - s0 + part * nslots;
+        const int32_t it1 = inc_ptr[r + 1];
+        for (int32_t it = inc_ptr[r] + part; it < it1; it += P) {
+            const int4 rc = rec_inc[it];
+            const int32_t e = rc.x / 12;
+            const int l = rc.x - e * 12;
+            const int a = l / 3, i = l - 3 * (l / 3);
+            const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+            int off[12];
+#pragma unroll
+            for (int bb = 0; bb < 12; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+            if (!SUR || flags[e]) {
+                double val[12], rr;
+                nh_plain_row(recd + (int64_t)e * kNhRecD, a, i, val, rr);
+                if constexpr (SUR) {
+                    df64 acc[12];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) accf[off[bb]] = df_add(acc[bb], df_split(val[bb]));
+                    rf = df_add(rf, df_split(rr));
+                } else {
+                    double acc[12];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accd[off[bb]];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) accd[off[bb]] = acc[bb] + val[bb];
+                    rd += rr;
+                }
+            } else {
+                float val[12], rr;
+                nh_surrogate_row(recf + (int64_t)e * kNhRecF, a, i, val, rr);
+                df64 acc[12];
+#pragma unroll
+                for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
+#pragma unroll
+                for (int bb = 0; bb < 12; ++bb) {
+                    const df64 sm = two_sum(acc[bb].hi, val[bb]);
+                    accf[off[bb]] = df64{sm.hi, acc[bb].lo + sm.lo};
+                }
+                const df64 sm = two_sum(rf.hi, rr);
+                rf = df64{sm.hi, rf.lo + sm.lo};
+            }
+        }
+    }
+    // residual: combine the P parts of each row (lane order), part 0 writes
+    if constexpr (P == 2) {
+        if constexpr (SUR) {
+            const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
+            rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
+        } else {
+            rd += __shfl_down_sync(0xffffffffu, rd, 1);
+        }
+    }
+    if (live && part == 0 && residual) {
+        if constexpr (SUR) residual[r] = (double)rf.hi + (double)rf.lo;
+        else residual[r] = rd;
+    }
+    __syncwarp();
+    if (values) {
+        for (int j = lane; j < nslots; j += 32) {
+            if constexpr (SUR) {
+                double v = (double)accf[j].hi + (double)accf[j].lo;
+#pragma unroll
+                for (int c = 1; c < P; ++c) v += (double)accf[c * nslots + j].hi + (double)accf[c * nslots + j].lo;
+                values[s0 + j] = v;
+            } else {
+                double v = accd[j];
+#pragma unroll
+                for (int c = 1; c < P; ++c) v += accd[c * nslots + j];
+                values[s0 + j] = v;
+            }
+        }
+    }
+}
+
+template <bool SUR, int SLOTS, int P>
+void launch_nh_rows(int n_groups, const int2 *groups, const skg_pattern *pat, const double *recd, const float *recf,
+                    const unsigned char *flags, double *residual, double *values, cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)kNhWarps * SLOTS * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_nh_rows<SUR, SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kNhWarps - 1) / kNhWarps);
+    k_nh_rows<SUR, SLOTS, P><<<grid, kNhWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
+                                                              pat->inc_ptr.get(), pat->rec.get(), recd, recf, flags,
+                                                              residual, values);
+    SKG_LAUNCH_CHECK("nh_rows");
+}
+
 // Residual gather: thread per DOF over its incidence list (element order).
 __global__ void k_vector_gather(int64_t n_rows, const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
                                 int L, const double *__restrict__ re, double *__restrict__ out) {
@@ -54,6 +286,21 @@ __global__ void k_vector_gather(int64_t n_rows, const int32_t *__restrict__ inc_
 }
 
 }  // namespace
+
+void nh_rows(const skg_pattern *pat, const double *recd, const float *recf, const unsigned char *flags,
+             double *d_residual, double *d_values, cudaStream_t s) {
+    if (recf) {
+        launch_nh_rows<true, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, recd, recf, flags,
+                                                  d_residual, d_values, s);
+        launch_nh_rows<true, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, recd, recf, flags,
+                                                  d_residual, d_values, s);
+    } else {
+        launch_nh_rows<false, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, recd, nullptr,
+                                                   nullptr, d_residual, d_values, s);
+        launch_nh_rows<false, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, recd, nullptr,
+                                                   nullptr, d_residual, d_values, s);
+    }
+}
 
 void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, double *d_residual, double *d_values,
                cudaStream_t s) {
@@ -78,6 +325,16 @@ extern "C" int skg_nh_assemble(const skg_pattern *pat, const double *d_p, int64_
         require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
         require(d_p && d_t && d_u, "mesh or displacement arrays are NULL");
         cudaStream_t s = as_stream(stream);
+        if (d_values && pat->max_row_len > 0) {  // fused path
+            DevBuf<double> rec((size_t)ne * kNhRecD, s);
+            if (ne) {
+                k_nh_plain_record<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
+                                                                   lmbda, wsum, rec.get());
+                SKG_LAUNCH_CHECK("nh_plain_record");
+            }
+            nh_rows(pat, rec.get(), nullptr, nullptr, d_residual, d_values, s);
+            return;
+        }
         DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
         if (ne) {
             k_nh_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda,

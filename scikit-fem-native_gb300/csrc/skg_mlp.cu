@@ -33,6 +33,8 @@
 
 #include "skg_common.cuh"
 #include "skg_nh.cuh"
+#include "skg_nh_rows.cuh"
+#include "skg_tc.cuh"
 
 namespace skg {
 
@@ -114,84 +116,121 @@ __global__ void k_dataset(int64_t n, unsigned long long seed, double sigma, doub
 
 // ---------------------------------------------------------------- network
 
-// Forward: z1, z2, psi; input gradient g = d psi / dx and (optionally) the
-// Hessian H = d2 psi / dx2 by forward-over-reverse along the 3 axes.
+// Evaluation of psi, its input gradient g = d psi/dx and Hessian
+// H = d2 psi/dx2 for one sample per thread, activations in registers.
+// With z1 = tanh(W1 x + b1), s1 = 1 - z1^2, z2 = tanh(W2 z1 + b2), s2 = 1 - z2^2,
+// d2 = s2 w3, u1 = W2^T d2:
+//   g = W1^T (s1 u1) + c
+//   H = W1^T diag(-2 z1 s1 u1) W1 + B^T diag(-2 z2 d2) B,  B = W2 diag(s1) W1.
+// The block keeps in shared memory WV[i][j] = (W2_ij, W2_ij W1_j0, W2_ij W1_j1,
+// W2_ij W1_j2), so one 16-byte broadcast load feeds the four products of the
+// forward sweep (a2 and the three columns of B); d2 goes through a per-thread
+// shared-memory column between the forward sweep and u1 = W2^T d2.
+constexpr int kEvalBlock = 128;
+constexpr int QW1 = 0, QB1 = 192, QB2 = 256, QW3 = 320, QB3 = 384, QC = 385, QNORM = 388, QSIZE = 400;
+constexpr size_t kEvalSmem = sizeof(float4) * H * H + sizeof(float) * QSIZE + sizeof(float) * H * kEvalBlock;
+
+struct EvalShared {
+    float4 *WV;
+    float *Q, *d2;
+};
+
+__device__ __forceinline__ EvalShared eval_shared(unsigned char *smem) {
+    EvalShared e;
+    e.WV = reinterpret_cast<float4 *>(smem);
+    e.Q = reinterpret_cast<float *>(smem + sizeof(float4) * H * H);
+    e.d2 = e.Q + QSIZE;
+    return e;
+}
+
+// Block-wide: fills the shared image from the parameter vector.
+__device__ __forceinline__ void load_eval_shared(const float *__restrict__ params, const EvalShared &e) {
+    for (int k = threadIdx.x; k < H * H; k += blockDim.x) {
+        const int j = k % H;
+        const float w = params[OW2 + k];
+        e.WV[k] = make_float4(w, w * params[OW1 + 3 * j], w * params[OW1 + 3 * j + 1], w * params[OW1 + 3 * j + 2]);
+    }
+    for (int k = threadIdx.x; k < QSIZE; k += blockDim.x) {
+        float v = 0.f;
+        if (k < QB2) v = params[OW1 + k];                       // W1, b1
+        else if (k < QB3 + 1) v = params[OB2 + (k - QB2)];      // b2, w3, b3
+        else if (k < QNORM) v = params[OC + (k - QC)];          // c
+        else if (k < QNORM + 9) v = params[ONORM + (k - QNORM)];
+        e.Q[k] = v;
+    }
+    __syncthreads();
+}
+
 template <bool HESS>
-__device__ __forceinline__ float mlp_eval(const float *__restrict__ P, const float x[3], float g[3], float Hm[9]) {
-    float z1[H], s1[H], z2[H], s2[H];
-#pragma unroll 8
-    for (int j = 0; j < H; ++j) {
-        const float a = P[OB1 + j] + P[OW1 + j * 3] * x[0] + P[OW1 + j * 3 + 1] * x[1] + P[OW1 + j * 3 + 2] * x[2];
-        z1[j] = tanhf(a);
-        s1[j] = 1.f - z1[j] * z1[j];
+__device__ __forceinline__ float mlp_eval(const EvalShared &e, const float x[3], float g[3], float Hm[9]) {
+    const float *Q = e.Q;
+    float *d2s = e.d2 + threadIdx.x;
+    float z1[H];
+    float psi = Q[QB3] + Q[QC] * x[0] + Q[QC + 1] * x[1] + Q[QC + 2] * x[2];
+    float h00 = 0.f, h01 = 0.f, h02 = 0.f, h11 = 0.f, h12 = 0.f, h22 = 0.f;
+    {
+        float s1[H];
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+            const float a = Q[QB1 + j] + Q[QW1 + 3 * j] * x[0] + Q[QW1 + 3 * j + 1] * x[1] + Q[QW1 + 3 * j + 2] * x[2];
+            z1[j] = tanhf(a);
+            s1[j] = 1.f - z1[j] * z1[j];
+        }
+#pragma unroll 1
+        for (int i = 0; i < H; ++i) {
+            const float4 *row = e.WV + i * H;
+            float a2 = Q[QB2 + i], b0 = 0.f, b1 = 0.f, b2 = 0.f;
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+                const float4 w = row[j];
+                a2 += w.x * z1[j];
+                if (HESS) {
+                    b0 += w.y * s1[j];
+                    b1 += w.z * s1[j];
+                    b2 += w.w * s1[j];
+                }
+            }
+            const float z2 = tanhf(a2), w3 = Q[QW3 + i];
+            const float d2 = (1.f - z2 * z2) * w3;
+            psi += w3 * z2;
+            d2s[i * kEvalBlock] = d2;
+            if (HESS) {
+                const float t2 = -2.f * z2 * d2;
+                const float tb0 = t2 * b0, tb1 = t2 * b1;
+                h00 += tb0 * b0; h01 += tb0 * b1; h02 += tb0 * b2;
+                h11 += tb1 * b1; h12 += tb1 * b2; h22 += t2 * b2 * b2;
+            }
+        }
     }
-    float psi = P[OB3];
-    for (int i = 0; i < H; ++i) {
-        float a = P[OB2 + i];
-#pragma unroll 8
-        for (int j = 0; j < H; ++j) a += P[OW2 + i * H + j] * z1[j];
-        z2[i] = tanhf(a);
-        s2[i] = 1.f - z2[i] * z2[i];
-        psi += P[OW3 + i] * z2[i];
-    }
-    psi += P[OC] * x[0] + P[OC + 1] * x[1] + P[OC + 2] * x[2];
-    // d2 = s2 * w3; u1 = W2^T d2; d1 = s1 * u1; g = W1^T d1 (+ c)
-    float d2[H], u1[H];
-#pragma unroll 8
-    for (int i = 0; i < H; ++i) d2[i] = s2[i] * P[OW3 + i];
-#pragma unroll 8
+    float u1[H];
+#pragma unroll
     for (int j = 0; j < H; ++j) u1[j] = 0.f;
+#pragma unroll 1
     for (int i = 0; i < H; ++i) {
-        const float di = d2[i];
-#pragma unroll 8
-        for (int j = 0; j < H; ++j) u1[j] += P[OW2 + i * H + j] * di;
+        const float d2 = d2s[i * kEvalBlock];
+        const float4 *row = e.WV + i * H;
+#pragma unroll
+        for (int j = 0; j < H; ++j) u1[j] += row[j].x * d2;
     }
-    g[0] = P[OC]; g[1] = P[OC + 1]; g[2] = P[OC + 2];
-#pragma unroll 8
+    g[0] = Q[QC]; g[1] = Q[QC + 1]; g[2] = Q[QC + 2];
+#pragma unroll
     for (int j = 0; j < H; ++j) {
-        const float d1 = s1[j] * u1[j];
-        g[0] += P[OW1 + j * 3] * d1;
-        g[1] += P[OW1 + j * 3 + 1] * d1;
-        g[2] += P[OW1 + j * 3 + 2] * d1;
+        const float s1 = 1.f - z1[j] * z1[j];
+        const float d1 = s1 * u1[j];
+        const float w0 = Q[QW1 + 3 * j], w1 = Q[QW1 + 3 * j + 1], w2 = Q[QW1 + 3 * j + 2];
+        g[0] += w0 * d1;
+        g[1] += w1 * d1;
+        g[2] += w2 * d1;
+        if (HESS) {
+            const float r = -2.f * z1[j] * d1;
+            h00 += r * w0 * w0; h01 += r * w0 * w1; h02 += r * w0 * w2;
+            h11 += r * w1 * w1; h12 += r * w1 * w2; h22 += r * w2 * w2;
+        }
     }
     if (HESS) {
-        for (int m = 0; m < 3; ++m) {
-            // directional derivative of g along e_m
-            float da1[H], dz1[H];
-#pragma unroll 8
-            for (int j = 0; j < H; ++j) {
-                da1[j] = P[OW1 + j * 3 + m];
-                dz1[j] = s1[j] * da1[j];
-            }
-            float dd2[H];
-            for (int i = 0; i < H; ++i) {
-                float da2 = 0.f;
-#pragma unroll 8
-                for (int j = 0; j < H; ++j) da2 += P[OW2 + i * H + j] * dz1[j];
-                // d2_i = s2_i w3_i, ds2_i = -2 z2_i s2_i da2_i
-                dd2[i] = -2.f * z2[i] * s2[i] * da2 * P[OW3 + i];
-            }
-            float du1[H];
-#pragma unroll 8
-            for (int j = 0; j < H; ++j) du1[j] = 0.f;
-            for (int i = 0; i < H; ++i) {
-                const float di = dd2[i];
-#pragma unroll 8
-                for (int j = 0; j < H; ++j) du1[j] += P[OW2 + i * H + j] * di;
-            }
-            float h0 = 0.f, h1 = 0.f, h2 = 0.f;
-#pragma unroll 8
-            for (int j = 0; j < H; ++j) {
-                // d1_j = s1_j u1_j, dd1_j = -2 z1_j s1_j da1_j u1_j + s1_j du1_j
-                const float dd1 = -2.f * z1[j] * s1[j] * da1[j] * u1[j] + s1[j] * du1[j];
-                h0 += P[OW1 + j * 3] * dd1;
-                h1 += P[OW1 + j * 3 + 1] * dd1;
-                h2 += P[OW1 + j * 3 + 2] * dd1;
-            }
-            Hm[0 * 3 + m] = h0;
-            Hm[1 * 3 + m] = h1;
-            Hm[2 * 3 + m] = h2;
-        }
+        Hm[0] = h00; Hm[1] = h01; Hm[2] = h02;
+        Hm[3] = h01; Hm[4] = h11; Hm[5] = h12;
+        Hm[6] = h02; Hm[7] = h12; Hm[8] = h22;
     }
     return psi;
 }
@@ -390,11 +429,14 @@ __global__ void k_sum_loss(int nblocks, const double *__restrict__ l, T *__restr
 // Stress normalisation: n = 2 dW/df1 + 4 dW/df2 + dW/df3 at f = 0, stored in
 // the parameter block (one thread; run once after training).
 __global__ void k_stress_shift(float *__restrict__ params) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const EvalShared e = eval_shared(smem);
+    load_eval_shared(params, e);
+    if (threadIdx.x != 0) return;
     float x[3], g[3], Hm[9];
 #pragma unroll
     for (int m = 0; m < 3; ++m) x[m] = (0.f - params[ONORM + m]) / params[ONORM + 3 + m];
-    mlp_eval<false>(params, x, g, Hm);
+    mlp_eval<false>(e, x, g, Hm);
     const float ys = params[ONORM + 6];
     float Wf[3];
 #pragma unroll
@@ -403,16 +445,16 @@ __global__ void k_stress_shift(float *__restrict__ params) {
 }
 
 // Evaluation: psi, dpsi/dx (3), d2psi/dx2 (9) per sample (normalised units).
-__global__ void k_mlp_eval(int64_t n, const float *__restrict__ x, const float *__restrict__ params,
-                           float *__restrict__ out) {
-    __shared__ float P[NTOTAL];
-    for (int i = threadIdx.x; i < NTOTAL; i += blockDim.x) P[i] = params[i];
-    __syncthreads();
+__global__ void __launch_bounds__(kEvalBlock) k_mlp_eval(int64_t n, const float *__restrict__ x,
+                                                         const float *__restrict__ params, float *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const EvalShared e = eval_shared(smem);
+    load_eval_shared(params, e);
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const float xs[3] = {x[s * 3], x[s * 3 + 1], x[s * 3 + 2]};
     float g[3], Hm[9];
-    const float psi = mlp_eval<true>(P, xs, g, Hm);
+    const float psi = mlp_eval<true>(e, xs, g, Hm);
     float *o = out + s * 13;
     o[0] = psi;
     for (int m = 0; m < 3; ++m) o[1 + m] = g[m];
@@ -426,15 +468,212 @@ __global__ void k_mlp_eval(int64_t n, const float *__restrict__ x, const float *
 //   d2I1 = 2 d_ik d_JL
 //   d2I2 = 2 [2 F_iJ F_kL + I1 d_ik d_JL - d_ik C_LJ - F_iL F_kJ - (F F^T)_ik d_JL]
 //   d2J  = J (F^-T_iJ F^-T_kL - F^-T_iL F^-T_kJ)
-__global__ void k_nh_surrogate_element(int64_t ne, const double *__restrict__ p, int64_t npts,
-                                       const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
-                                       const double *__restrict__ u, double mu, double lmbda, double wsum,
-                                       const float *__restrict__ params, const float *__restrict__ box, float tol,
-                                       double *__restrict__ Ke, double *__restrict__ re,
-                                       unsigned long long *__restrict__ fallback) {
-    __shared__ float P[NTOTAL];
-    for (int i = threadIdx.x; i < NTOTAL; i += blockDim.x) P[i] = params[i];
-    __syncthreads();
+
+// Deformation state of one element in FP32.
+struct SurState {
+    float F[9], C[9], FiT[9], I1, I2, J, lnJ;
+    bool ok;  // J > 0
+};
+
+__device__ __forceinline__ void surrogate_state(const float F[9], SurState &s) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) s.F[k] = F[k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) s.C[i * 3 + j] = F[i] * F[j] + F[3 + i] * F[3 + j] + F[6 + i] * F[6 + j];
+    s.I1 = s.C[0] + s.C[4] + s.C[8];
+    float trC2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) trC2 += s.C[k] * s.C[k];
+    s.I2 = 0.5f * (s.I1 * s.I1 - trC2);
+    const float a00 = F[4] * F[8] - F[5] * F[7], a01 = F[2] * F[7] - F[1] * F[8], a02 = F[1] * F[5] - F[2] * F[4];
+    const float a10 = F[5] * F[6] - F[3] * F[8], a11 = F[0] * F[8] - F[2] * F[6], a12 = F[2] * F[3] - F[0] * F[5];
+    const float a20 = F[3] * F[7] - F[4] * F[6], a21 = F[1] * F[6] - F[0] * F[7], a22 = F[0] * F[4] - F[1] * F[3];
+    s.J = F[0] * a00 + F[1] * a10 + F[2] * a20;
+    s.ok = s.J > 0.f;
+    s.lnJ = s.ok ? logf(s.J) : 0.f;
+    const float iJ = s.ok ? 1.f / s.J : 0.f;
+    // F^-1 = adj(F) / J; F^-T[i][j] = F^-1[j][i]
+    const float Fi[9] = {a00 * iJ, a01 * iJ, a02 * iJ, a10 * iJ, a11 * iJ, a12 * iJ, a20 * iJ, a21 * iJ, a22 * iJ};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) s.FiT[i * 3 + j] = Fi[j * 3 + i];
+}
+
+__device__ __forceinline__ bool in_box(const SurState &s, const float *__restrict__ box) {
+    const float fr[3] = {s.I1 - 3.f, s.I2 - 3.f, s.lnJ};
+    bool in = true;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) in = in && fr[m] >= box[m] && fr[m] <= box[3 + m];
+    return in;
+}
+
+__device__ __forceinline__ void normalised_input(const SurState &s, const float *__restrict__ Nrm, float x[3]) {
+    const float fr[3] = {s.I1 - 3.f, s.I2 - 3.f, s.lnJ};
+#pragma unroll
+    for (int m = 0; m < 3; ++m) x[m] = (fr[m] - Nrm[m]) / Nrm[3 + m];
+}
+
+// From the network's derivatives (gx, Hx, normalised units) to the stress,
+// the per-element check against the plain law (FP32) and the tangent.
+// Returns false when the element must fall back to the plain law.  FUSED:
+// writes the surrogate record `out`; otherwise the element tangent Ke and
+// residual re (already offset to the element).
+template <bool FUSED>
+__device__ __forceinline__ bool surrogate_finish(const SurState &st, const float *__restrict__ Nrm, const float gx[3],
+                                                 const float Hx[9], double mu, double lmbda, float tol, float Vf,
+                                                 const float ga[4][3], float4 *__restrict__ out, double *__restrict__ Ke,
+                                                 double *__restrict__ re, double V) {
+    const float *F = st.F, *C = st.C, *FiT = st.FiT;
+    const float I1 = st.I1, J = st.J, iJ = 1.f / st.J;
+    // derivatives of W with respect to the features f
+    const float ys = Nrm[6];
+    float Wf[3], Wff[9];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) Wf[m] = ys * gx[m] / Nrm[3 + m];
+    Wf[2] -= Nrm[8];  // stress-free reference state
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) Wff[m * 3 + l] = ys * Hx[m * 3 + l] / (Nrm[3 + m] * Nrm[3 + l]);
+    // features -> invariants: f3 = ln J: dW/dJ = W3 / J, d2W/dJ2 = (W33 - W3) / J^2, d2W/dIa dJ = Wa3 / J
+    float Wa[3], Wab[9];
+    Wa[0] = Wf[0]; Wa[1] = Wf[1]; Wa[2] = Wf[2] * iJ;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int l = 0; l < 2; ++l) Wab[m * 3 + l] = Wff[m * 3 + l];
+    Wab[0 * 3 + 2] = Wab[2 * 3 + 0] = Wff[0 * 3 + 2] * iJ;
+    Wab[1 * 3 + 2] = Wab[2 * 3 + 1] = Wff[1 * 3 + 2] * iJ;
+    Wab[8] = (Wff[8] - Wf[2]) * iJ * iJ;
+    float FC[9], FFt[9], dI[3][9], Pm[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            FC[i * 3 + j] = F[i * 3] * C[j] + F[i * 3 + 1] * C[3 + j] + F[i * 3 + 2] * C[6 + j];
+            FFt[i * 3 + j] = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+        }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        dI[0][k] = 2.f * F[k];
+        dI[1][k] = 2.f * (I1 * F[k] - FC[k]);
+        dI[2][k] = J * FiT[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Pm[k] = Wa[0] * dI[0][k] + Wa[1] * dI[1][k] + Wa[2] * dI[2][k];
+    // per-element check against the plain law in FP32: the stresses must agree
+    float diff = 0.f, nrm = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const float pl = (float)mu * (F[k] - FiT[k]) + (float)lmbda * st.lnJ * FiT[k];
+        diff = fmaxf(diff, fabsf(Pm[k] - pl));
+        nrm = fmaxf(nrm, fabsf(pl));
+    }
+    if (!(diff <= tol * fmaxf(nrm, 1e-3f))) return false;
+    // tangent A_iJkL, one row block i (27 entries) at a time
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float Ai[28];
+#pragma unroll
+        for (int Jj = 0; Jj < 3; ++Jj)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int L = 0; L < 3; ++L) {
+                    const int a = i * 3 + Jj, b = k * 3 + L;
+                    float v = 0.f;
+#pragma unroll
+                    for (int m = 0; m < 3; ++m)
+#pragma unroll
+                        for (int l = 0; l < 3; ++l) v += Wab[m * 3 + l] * dI[m][a] * dI[l][b];
+                    const float dik = i == k ? 1.f : 0.f, dJL = Jj == L ? 1.f : 0.f;
+                    v += Wa[0] * 2.f * dik * dJL;
+                    v += Wa[1] * 2.f * (2.f * F[a] * F[b] + I1 * dik * dJL - dik * C[L * 3 + Jj] -
+                                        F[i * 3 + L] * F[k * 3 + Jj] - FFt[i * 3 + k] * dJL);
+                    v += Wa[2] * J * (FiT[a] * FiT[b] - FiT[i * 3 + L] * FiT[k * 3 + Jj]);
+                    Ai[Jj * 9 + b] = v;
+                }
+        Ai[27] = 0.f;
+        if constexpr (FUSED) {
+#pragma unroll
+            for (int q = 0; q < 7; ++q)
+                out[7 * i + q] = make_float4(Vf * Ai[4 * q], Vf * Ai[4 * q + 1], Vf * Ai[4 * q + 2], Vf * Ai[4 * q + 3]);
+        } else if (Ke) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                // row (a, i): sum_JL ga[a][J] A[iJ][kL] ga[b][L]
+                float tmp[9];
+#pragma unroll
+                for (int kL = 0; kL < 9; ++kL)
+                    tmp[kL] = ga[a][0] * Ai[kL] + ga[a][1] * Ai[9 + kL] + ga[a][2] * Ai[18 + kL];
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        Ke[(a * 3 + i) * 12 + b * 3 + k] =
+                            V * (double)(tmp[k * 3] * ga[b][0] + tmp[k * 3 + 1] * ga[b][1] + tmp[k * 3 + 2] * ga[b][2]);
+            }
+        }
+    }
+    if constexpr (FUSED) {
+        out[21] = make_float4(ga[0][0], ga[0][1], ga[0][2], ga[1][0]);
+        out[22] = make_float4(ga[1][1], ga[1][2], ga[2][0], ga[2][1]);
+        out[23] = make_float4(ga[2][2], ga[3][0], ga[3][1], ga[3][2]);
+        out[24] = make_float4(Vf * Pm[0], Vf * Pm[1], Vf * Pm[2], Vf * Pm[3]);
+        out[25] = make_float4(Vf * Pm[4], Vf * Pm[5], Vf * Pm[6], Vf * Pm[7]);
+        out[26] = make_float4(Vf * Pm[8], 0.f, 0.f, 0.f);
+    } else if (re) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                re[a * 3 + c] = V * (double)(Pm[c * 3] * ga[a][0] + Pm[c * 3 + 1] * ga[a][1] + Pm[c * 3 + 2] * ga[a][2]);
+    }
+    return true;
+}
+
+// Plain-law fallback of one element (FP64 geometry and law).
+template <bool FUSED>
+__device__ __forceinline__ void surrogate_fallback(int64_t e, const double *__restrict__ p, int64_t npts,
+                                                   const int32_t *__restrict__ t, int64_t ne,
+                                                   const int32_t *__restrict__ dofs, const double *__restrict__ u,
+                                                   double mu, double lmbda, double wsum, double *__restrict__ Ke,
+                                                   double *__restrict__ re, double *__restrict__ recd,
+                                                   unsigned char *__restrict__ flags,
+                                                   unsigned long long *__restrict__ fallback) {
+    NhGeom g;
+    nh_geometry(p, npts, t, ne, e, wsum, g);
+    double Gu[9];
+    displacement_gradient(g, dofs + e * 12, u, Gu);
+    NhLaw law;
+    nh_plain_law(Gu, mu, lmbda, law);
+    if constexpr (FUSED) {
+        write_plain_record(g, law, mu, lmbda, recd + e * kNhRecD);
+        flags[e] = 1;
+    } else {
+        write_nh_element(g, law, mu, lmbda, Ke ? Ke + e * 144 : nullptr, re ? re + e * 12 : nullptr);
+    }
+    atomicAdd(fallback, 1ULL);
+}
+
+// One thread per element, network on the CUDA cores (mlp_eval).  FUSED:
+// writes the surrogate record (recf) or, for a fallback element, the plain
+// FP64 record (recd) and sets flags[e]; otherwise the element tangent and
+// residual (Ke, re) for the gathers.
+template <bool FUSED>
+__global__ void __launch_bounds__(kEvalBlock) k_nh_surrogate_element(
+    int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+    const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda, double wsum,
+    const float *__restrict__ params, const float *__restrict__ box, float tol, double *__restrict__ Ke,
+    double *__restrict__ re, float *__restrict__ recf, double *__restrict__ recd, unsigned char *__restrict__ flags,
+    unsigned long long *__restrict__ fallback) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const EvalShared ev = eval_shared(smem);
+    load_eval_shared(params, ev);
+    const float *Nrm = ev.Q + QNORM;  // f_mean[3], f_std[3], y_scale, y_shift, stress shift
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     NhGeom g;
@@ -444,140 +683,324 @@ __global__ void k_nh_surrogate_element(int64_t ne, const double *__restrict__ p,
     float F[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) F[k] = (float)Gu[k] + ((k % 4) == 0 ? 1.f : 0.f);
-    // invariants and F^-T in FP32
-    float C[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) C[i * 3 + j] = F[i] * F[j] + F[3 + i] * F[3 + j] + F[6 + i] * F[6 + j];
-    const float I1 = C[0] + C[4] + C[8];
-    float trC2 = 0.f;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) trC2 += C[k] * C[k];
-    const float I2 = 0.5f * (I1 * I1 - trC2);
-    const float a00 = F[4] * F[8] - F[5] * F[7], a01 = F[2] * F[7] - F[1] * F[8], a02 = F[1] * F[5] - F[2] * F[4];
-    const float a10 = F[5] * F[6] - F[3] * F[8], a11 = F[0] * F[8] - F[2] * F[6], a12 = F[2] * F[3] - F[0] * F[5];
-    const float a20 = F[3] * F[7] - F[4] * F[6], a21 = F[1] * F[6] - F[0] * F[7], a22 = F[0] * F[4] - F[1] * F[3];
-    const float J = F[0] * a00 + F[1] * a10 + F[2] * a20;
-    bool use = g.ok && J > 0.f;
-    float lnJ = use ? logf(J) : 0.f;
-    const float fr[3] = {I1 - 3.f, I2 - 3.f, lnJ};
-    // inside the trained box?
-#pragma unroll
-    for (int m = 0; m < 3; ++m) use = use && fr[m] >= box[m] && fr[m] <= box[3 + m];
-    float Pm[9], A[81];
+    SurState st;
+    surrogate_state(F, st);
+    bool use = g.ok && st.ok && in_box(st, box);
     if (use) {
-        const float iJ = 1.f / J;
-        const float Fi[9] = {a00 * iJ, a01 * iJ, a02 * iJ, a10 * iJ, a11 * iJ, a12 * iJ, a20 * iJ, a21 * iJ, a22 * iJ};
-        float FiT[9];
+        float x[3], gx[3], Hx[9], ga[4][3];
+        normalised_input(st, Nrm, x);
+        mlp_eval<true>(ev, x, gx, Hx);
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+        for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) FiT[i * 3 + j] = Fi[j * 3 + i];
-        float x[3], gx[3], Hx[9];
-#pragma unroll
-        for (int m = 0; m < 3; ++m) x[m] = (fr[m] - P[ONORM + m]) / P[ONORM + 3 + m];
-        mlp_eval<true>(P, x, gx, Hx);
-        // derivatives of W with respect to the features f
-        const float ys = P[ONORM + 6];
-        float Wf[3], Wff[9];
-#pragma unroll
-        for (int m = 0; m < 3; ++m) Wf[m] = ys * gx[m] / P[ONORM + 3 + m];
-        Wf[2] -= P[ONORM + 8];  // stress-free reference state
-#pragma unroll
-        for (int m = 0; m < 3; ++m)
-#pragma unroll
-            for (int l = 0; l < 3; ++l) Wff[m * 3 + l] = ys * Hx[m * 3 + l] / (P[ONORM + 3 + m] * P[ONORM + 3 + l]);
-        // features -> invariants: f3 = ln J: dW/dJ = W3 / J, d2W/dJ2 = (W33 - W3) / J^2, d2W/dIa dJ = Wa3 / J
-        const float Wa[3] = {Wf[0], Wf[1], Wf[2] * iJ};
-        float Wab[9];
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-#pragma unroll
-            for (int l = 0; l < 2; ++l) Wab[m * 3 + l] = Wff[m * 3 + l];
-        Wab[0 * 3 + 2] = Wab[2 * 3 + 0] = Wff[0 * 3 + 2] * iJ;
-        Wab[1 * 3 + 2] = Wab[2 * 3 + 1] = Wff[1 * 3 + 2] * iJ;
-        Wab[8] = (Wff[8] - Wf[2]) * iJ * iJ;
-        // dI/dF
-        float FC[9], FFt[9];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                FC[i * 3 + j] = F[i * 3] * C[j] + F[i * 3 + 1] * C[3 + j] + F[i * 3 + 2] * C[6 + j];
-                FFt[i * 3 + j] = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
-            }
-        float dI[3][9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            dI[0][k] = 2.f * F[k];
-            dI[1][k] = 2.f * (I1 * F[k] - FC[k]);
-            dI[2][k] = J * FiT[k];
-        }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Pm[k] = Wa[0] * dI[0][k] + Wa[1] * dI[1][k] + Wa[2] * dI[2][k];
-        for (int i = 0; i < 3; ++i)
-            for (int Jj = 0; Jj < 3; ++Jj)
-                for (int k = 0; k < 3; ++k)
-                    for (int L = 0; L < 3; ++L) {
-                        const int a = i * 3 + Jj, b = k * 3 + L;
-                        float v = 0.f;
-#pragma unroll
-                        for (int m = 0; m < 3; ++m)
-#pragma unroll
-                            for (int l = 0; l < 3; ++l) v += Wab[m * 3 + l] * dI[m][a] * dI[l][b];
-                        const float dik = i == k ? 1.f : 0.f, dJL = Jj == L ? 1.f : 0.f;
-                        v += Wa[0] * 2.f * dik * dJL;
-                        v += Wa[1] * 2.f * (2.f * F[a] * F[b] + I1 * dik * dJL - dik * C[L * 3 + Jj] -
-                                            F[i * 3 + L] * F[k * 3 + Jj] - FFt[i * 3 + k] * dJL);
-                        v += Wa[2] * J * (FiT[a] * FiT[b] - FiT[i * 3 + L] * FiT[k * 3 + Jj]);
-                        A[a * 9 + b] = v;
-                    }
-        // per-element check against the plain law in FP32: the stresses must agree
-        float diff = 0.f, nrm = 0.f;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const float pl = (float)mu * (F[k] - FiT[k]) + (float)lmbda * lnJ * FiT[k];
-            diff = fmaxf(diff, fabsf(Pm[k] - pl));
-            nrm = fmaxf(nrm, fabsf(pl));
-        }
-        use = diff <= tol * fmaxf(nrm, 1e-3f);
+            for (int j = 0; j < 3; ++j) ga[q][j] = (float)g.g[q][j];
+        use = surrogate_finish<FUSED>(st, Nrm, gx, Hx, mu, lmbda, tol, (float)g.V, ga,
+                                      FUSED ? reinterpret_cast<float4 *>(recf + e * kNhRecF) : nullptr,
+                                      Ke ? Ke + e * 144 : nullptr, re ? re + e * 12 : nullptr, g.V);
     }
     if (!use) {
-        // plain law in FP64 (outside the trained range or check failed)
-        NhLaw law;
-        nh_plain_law(Gu, mu, lmbda, law);
-        write_nh_element(g, law, mu, lmbda, Ke ? Ke + e * 144 : nullptr, re ? re + e * 12 : nullptr);
-        atomicAdd(fallback, 1ULL);
-        return;
+        surrogate_fallback<FUSED>(e, p, npts, t, ne, dofs, u, mu, lmbda, wsum, Ke, re, recd, flags, fallback);
+    } else if (FUSED) {
+        flags[e] = 0;
     }
-    if (re) {
+}
+
+// ------------------------------------------------- surrogate on tensor cores
+//
+// Tiles of 128 elements, one per CTA at a time (persistent CTAs, one per SM),
+// thread t = element row t = tensor-memory lane t.  The two 64 x 64 layers are
+// tcgen05 MMAs (kind::tf32) with FP32-accurate products: every operand is
+// split x = hi + lo in tf32 and D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
+//   GEMM 1: [a2 | B0 | B1 | B2] = [Z1 | Q0 | Q1 | Q2] W2^T    (TMEM columns 0..255)
+//           with Q_m[e][j] = s1[e][j] W1[j][m]  (B = W2 diag(s1) W1 per element)
+//   GEMM 2: u1 = D2 W2                                          (TMEM columns 0..63)
+// and everything elementwise (tanh, Hessian contractions, stress, tangent)
+// on the CUDA cores of the owning thread.  Shared memory: W2 and W2^T (hi,
+// lo) as B operands, two 128 x 64 A-operand buffers (hi, lo), small vectors.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 256;
+constexpr int kOpBytes = kTcRows * H * 4;  // one 128 x 64 tf32 operand
+constexpr int kWBytes = H * H * 4;
+constexpr int SM_W2B_HI = 0, SM_W2B_LO = kWBytes, SM_W2T_HI = 2 * kWBytes, SM_W2T_LO = 3 * kWBytes;
+constexpr int SM_OPA_HI = 4 * kWBytes, SM_OPA_LO = SM_OPA_HI + kOpBytes;
+constexpr int SM_OPB_HI = SM_OPA_LO + kOpBytes, SM_OPB_LO = SM_OPB_HI + kOpBytes;
+constexpr int SM_Q = SM_OPB_LO + kOpBytes;
+constexpr size_t kTcSmem = SM_Q + QSIZE * 4;
+constexpr uint32_t kTcWaitLimit = 1u << 24;
+
+// Writes 4 consecutive k of row `row` into an A operand (tf32 hi and lo parts).
+__device__ __forceinline__ void put_op4(unsigned char *hi, unsigned char *lo, int row, int k, float a, float b,
+                                        float c, float d) {
+    const uint32_t off = tc::operand_offset(kTcRows, row, k);
+    const float ha = tc::to_tf32(a), hb = tc::to_tf32(b), hc = tc::to_tf32(c), hd = tc::to_tf32(d);
+    *reinterpret_cast<float4 *>(hi + off) = make_float4(ha, hb, hc, hd);
+    *reinterpret_cast<float4 *>(lo + off) =
+        make_float4(tc::to_tf32(a - ha), tc::to_tf32(b - hb), tc::to_tf32(c - hc), tc::to_tf32(d - hd));
+}
+
+// D[tmem] = A (128 x 64) * B^T (B: 64 x 64), 3xTF32, single issuing thread.
+__device__ __forceinline__ void issue_gemm(uint32_t d_tmem, const unsigned char *a_hi, const unsigned char *a_lo,
+                                           const unsigned char *b_hi, const unsigned char *b_lo) {
+    const uint32_t idesc = tc::idesc_tf32(kTcRows, H);
+    const uint32_t ah0 = tc::smem_addr(a_hi), al0 = tc::smem_addr(a_lo);
+    const uint32_t bh0 = tc::smem_addr(b_hi), bl0 = tc::smem_addr(b_lo);
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                re[e * 12 + a * 3 + c] =
-                    g.V * (double)(Pm[c * 3] * (float)g.g[a][0] + Pm[c * 3 + 1] * (float)g.g[a][1] + Pm[c * 3 + 2] * (float)g.g[a][2]);
+    for (int s = 0; s < H / 8; ++s) {
+        const uint32_t ao = s * 2 * (kTcRows * 16), bo = s * 2 * (H * 16);
+        const uint64_t ah = tc::smem_desc(ah0 + ao, kTcRows * 16, 128), al = tc::smem_desc(al0 + ao, kTcRows * 16, 128);
+        const uint64_t bh = tc::smem_desc(bh0 + bo, H * 16, 128), bl = tc::smem_desc(bl0 + bo, H * 16, 128);
+        tc::mma_tf32(d_tmem, ah, bh, idesc, s > 0);
+        tc::mma_tf32(d_tmem, ah, bl, idesc, true);
+        tc::mma_tf32(d_tmem, al, bh, idesc, true);
     }
-    if (Ke) {
-        float ga[4][3];
-        for (int a = 0; a < 4; ++a)
-            for (int j = 0; j < 3; ++j) ga[a][j] = (float)g.g[a][j];
-        for (int a = 0; a < 4; ++a)
-            for (int i = 0; i < 3; ++i) {
-                // row (a, i): sum_JL ga[a][J] A[iJ][kL] ga[b][L]
-                float tmp[9];
+}
+
+// Operand writes -> tensor cores; tensor-memory reads of the previous phase
+// are ordered before the next MMAs.
+__device__ __forceinline__ void sync_for_mma() {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+// Element geometry and displacement gradient in FP32 (edge differences taken
+// in FP64 first).  Returns false for out-of-range vertices or a zero volume.
+__device__ __forceinline__ bool geometry_fp32(const double *__restrict__ p, int64_t npts,
+                                              const int32_t *__restrict__ t, int64_t ne, int64_t e,
+                                              const int32_t *__restrict__ dofs, const double *__restrict__ u,
+                                              double wsum, float ga[4][3], float &Vf, float F[9]) {
+    int32_t v[4];
+    bool ok = true;
 #pragma unroll
-                for (int kL = 0; kL < 9; ++kL)
-                    tmp[kL] = ga[a][0] * A[(i * 3 + 0) * 9 + kL] + ga[a][1] * A[(i * 3 + 1) * 9 + kL] +
-                              ga[a][2] * A[(i * 3 + 2) * 9 + kL];
-                for (int b = 0; b < 4; ++b)
+    for (int k = 0; k < 4; ++k) {
+        v[k] = t[k * ne + e];
+        ok = ok && v[k] >= 0 && v[k] < npts;
+    }
+    if (!ok) v[0] = v[1] = v[2] = v[3] = 0;
+    float J[9];
 #pragma unroll
-                    for (int k = 0; k < 3; ++k)
-                        Ke[e * 144 + (a * 3 + i) * 12 + b * 3 + k] =
-                            g.V * (double)(tmp[k * 3] * ga[b][0] + tmp[k * 3 + 1] * ga[b][1] + tmp[k * 3 + 2] * ga[b][2]);
+    for (int i = 0; i < 3; ++i) {
+        const double x0 = p[i * npts + v[0]];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) J[i * 3 + r] = (float)(p[i * npts + v[r + 1]] - x0);
+    }
+    const float c00 = J[4] * J[8] - J[5] * J[7], c01 = J[2] * J[7] - J[1] * J[8], c02 = J[1] * J[5] - J[2] * J[4];
+    const float c10 = J[5] * J[6] - J[3] * J[8], c11 = J[0] * J[8] - J[2] * J[6], c12 = J[2] * J[3] - J[0] * J[5];
+    const float c20 = J[3] * J[7] - J[4] * J[6], c21 = J[1] * J[6] - J[0] * J[7], c22 = J[0] * J[4] - J[1] * J[3];
+    const float det = J[0] * c00 + J[1] * c10 + J[2] * c20;
+    ok = ok && det != 0.f && isfinite(det);
+    const float id = ok ? 1.f / det : 0.f;
+    ga[1][0] = c00 * id; ga[1][1] = c01 * id; ga[1][2] = c02 * id;
+    ga[2][0] = c10 * id; ga[2][1] = c11 * id; ga[2][2] = c12 * id;
+    ga[3][0] = c20 * id; ga[3][1] = c21 * id; ga[3][2] = c22 * id;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ga[0][j] = -(ga[1][j] + ga[2][j] + ga[3][j]);
+    Vf = fabsf(det) * (float)wsum;
+    const int32_t *d = dofs + e * 12;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F[k] = (k % 4) == 0 ? 1.f : 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double u0 = u[d[c]];
+#pragma unroll
+        for (int r = 1; r < 4; ++r) {
+            const float du = (float)(u[d[r * 3 + c]] - u0);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) F[c * 3 + j] += du * ga[r][j];
+        }
+    }
+    return ok;
+}
+
+__global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
+    int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+    const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda, double wsum,
+    const float *__restrict__ params, const float *__restrict__ box, float tol, float *__restrict__ recf,
+    double *__restrict__ recd, unsigned char *__restrict__ flags, unsigned long long *__restrict__ counters) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float *Q = reinterpret_cast<float *>(smem + SM_Q);
+    unsigned char *opa_hi = smem + SM_OPA_HI, *opa_lo = smem + SM_OPA_LO;
+    unsigned char *opb_hi = smem + SM_OPB_HI, *opb_lo = smem + SM_OPB_LO;
+    const unsigned char *w2b_hi = smem + SM_W2B_HI, *w2b_lo = smem + SM_W2B_LO;
+    const unsigned char *w2t_hi = smem + SM_W2T_HI, *w2t_lo = smem + SM_W2T_LO;
+    for (int k = tid; k < H * H; k += kTcRows) {
+        const int i = k / H, j = k - (k / H) * H;
+        const float w = params[OW2 + k], hi = tc::to_tf32(w), lo = tc::to_tf32(w - hi);
+        *reinterpret_cast<float *>(smem + SM_W2B_HI + tc::operand_offset(H, i, j)) = hi;
+        *reinterpret_cast<float *>(smem + SM_W2B_LO + tc::operand_offset(H, i, j)) = lo;
+        *reinterpret_cast<float *>(smem + SM_W2T_HI + tc::operand_offset(H, j, i)) = hi;
+        *reinterpret_cast<float *>(smem + SM_W2T_LO + tc::operand_offset(H, j, i)) = lo;
+    }
+    for (int k = tid; k < QSIZE; k += kTcRows) {
+        float v = 0.f;
+        if (k < QB2) v = params[OW1 + k];
+        else if (k < QB3 + 1) v = params[OB2 + (k - QB2)];
+        else if (k < QNORM) v = params[OC + (k - QC)];
+        else if (k < QNORM + 9) v = params[ONORM + (k - QNORM)];
+        Q[k] = v;
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) tc::tmem_alloc(&tslot, kTcCols);
+    sync_for_mma();
+    const uint32_t tmem = tslot;
+    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+    const float *Nrm = Q + QNORM;
+    uint32_t phase = 0;
+    bool tc_ok = true;
+    for (int64_t tile = blockIdx.x; tile * kTcRows < ne; tile += gridDim.x) {
+        const int64_t e = tile * kTcRows + tid;
+        const bool valid = e < ne;
+        float ga[4][3], Vf = 0.f, F[9];
+        bool geo = false;
+        if (valid) geo = geometry_fp32(p, npts, t, ne, e, dofs, u, wsum, ga, Vf, F);
+        if (!geo) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) F[k] = (k % 4) == 0 ? 1.f : 0.f;
+        }
+        SurState st;
+        surrogate_state(F, st);
+        bool use = valid && geo && st.ok && in_box(st, box);
+        float x[3] = {0.f, 0.f, 0.f};
+        if (use) normalised_input(st, Nrm, x);
+        float psi = Q[QB3] + Q[QC] * x[0] + Q[QC + 1] * x[1] + Q[QC + 2] * x[2];
+        float z1[H];
+        if (tc_ok) {
+            // ---- layer 1; A operands Z1 and Q0
+#pragma unroll
+            for (int j0 = 0; j0 < H; j0 += 4) {
+                float zz[4], q0[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int j = j0 + c;
+                    const float a = Q[QB1 + j] + Q[QW1 + 3 * j] * x[0] + Q[QW1 + 3 * j + 1] * x[1] +
+                                    Q[QW1 + 3 * j + 2] * x[2];
+                    z1[j] = tanhf(a);
+                    zz[c] = z1[j];
+                    q0[c] = (1.f - z1[j] * z1[j]) * Q[QW1 + 3 * j];
+                }
+                put_op4(opa_hi, opa_lo, tid, j0, zz[0], zz[1], zz[2], zz[3]);
+                put_op4(opb_hi, opb_lo, tid, j0, q0[0], q0[1], q0[2], q0[3]);
             }
+            sync_for_mma();
+            if (tid == 0) {
+                issue_gemm(tmem + 0, opa_hi, opa_lo, w2b_hi, w2b_lo);
+                issue_gemm(tmem + 64, opb_hi, opb_lo, w2b_hi, w2b_lo);
+                tc::mma_commit(&mbar);
+            }
+            tc_ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kTcWaitLimit));
+            phase ^= 1;
+        }
+        if (tc_ok) {
+            // ---- A operands Q1 and Q2
+#pragma unroll
+            for (int j0 = 0; j0 < H; j0 += 4) {
+                float q1[4], q2[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int j = j0 + c;
+                    const float s1 = 1.f - z1[j] * z1[j];
+                    q1[c] = s1 * Q[QW1 + 3 * j + 1];
+                    q2[c] = s1 * Q[QW1 + 3 * j + 2];
+                }
+                put_op4(opa_hi, opa_lo, tid, j0, q1[0], q1[1], q1[2], q1[3]);
+                put_op4(opb_hi, opb_lo, tid, j0, q2[0], q2[1], q2[2], q2[3]);
+            }
+            sync_for_mma();
+            if (tid == 0) {
+                issue_gemm(tmem + 128, opa_hi, opa_lo, w2b_hi, w2b_lo);
+                issue_gemm(tmem + 192, opb_hi, opb_lo, w2b_hi, w2b_lo);
+                tc::mma_commit(&mbar);
+            }
+            tc_ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kTcWaitLimit));
+            phase ^= 1;
+        }
+        float h00 = 0.f, h01 = 0.f, h02 = 0.f, h11 = 0.f, h12 = 0.f, h22 = 0.f;
+        if (tc_ok) {
+            // ---- layer 2 and the second Hessian term; A operand D2
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ch = 0; ch < H / 16; ++ch) {
+                float a2[16], b0[16], b1[16], b2[16], dv[16];
+                tc::tmem_ld16(tl + ch * 16, a2);
+                tc::tmem_ld16(tl + 64 + ch * 16, b0);
+                tc::tmem_ld16(tl + 128 + ch * 16, b1);
+                tc::tmem_ld16(tl + 192 + ch * 16, b2);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int i = ch * 16 + q;
+                    const float z2 = tanhf(a2[q] + Q[QB2 + i]), w3 = Q[QW3 + i];
+                    const float d2 = (1.f - z2 * z2) * w3;
+                    psi += w3 * z2;
+                    dv[q] = d2;
+                    const float t2 = -2.f * z2 * d2;
+                    const float tb0 = t2 * b0[q], tb1 = t2 * b1[q];
+                    h00 += tb0 * b0[q]; h01 += tb0 * b1[q]; h02 += tb0 * b2[q];
+                    h11 += tb1 * b1[q]; h12 += tb1 * b2[q]; h22 += t2 * b2[q] * b2[q];
+                }
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    put_op4(opa_hi, opa_lo, tid, ch * 16 + 4 * r, dv[4 * r], dv[4 * r + 1], dv[4 * r + 2], dv[4 * r + 3]);
+            }
+            sync_for_mma();
+            if (tid == 0) {
+                issue_gemm(tmem + 0, opa_hi, opa_lo, w2t_hi, w2t_lo);
+                tc::mma_commit(&mbar);
+            }
+            tc_ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kTcWaitLimit));
+            phase ^= 1;
+        }
+        float gx[3] = {Q[QC], Q[QC + 1], Q[QC + 2]}, Hx[9];
+        if (tc_ok) {
+            // ---- u1 = W2^T d2: gradient and first Hessian term
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ch = 0; ch < H / 16; ++ch) {
+                float u1[16];
+                tc::tmem_ld16(tl + ch * 16, u1);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int j = ch * 16 + q;
+                    const float d1 = (1.f - z1[j] * z1[j]) * u1[q];
+                    const float w0 = Q[QW1 + 3 * j], w1 = Q[QW1 + 3 * j + 1], w2 = Q[QW1 + 3 * j + 2];
+                    gx[0] += w0 * d1;
+                    gx[1] += w1 * d1;
+                    gx[2] += w2 * d1;
+                    const float r = -2.f * z1[j] * d1;
+                    h00 += r * w0 * w0; h01 += r * w0 * w1; h02 += r * w0 * w2;
+                    h11 += r * w1 * w1; h12 += r * w1 * w2; h22 += r * w2 * w2;
+                }
+            }
+        } else {
+            use = false;  // tensor-core phase gave up: plain law for the rest
+        }
+        Hx[0] = h00; Hx[1] = h01; Hx[2] = h02;
+        Hx[3] = h01; Hx[4] = h11; Hx[5] = h12;
+        Hx[6] = h02; Hx[7] = h12; Hx[8] = h22;
+        (void)psi;
+        if (use)
+            use = surrogate_finish<true>(st, Nrm, gx, Hx, mu, lmbda, tol, Vf, ga,
+                                         reinterpret_cast<float4 *>(recf + e * kNhRecF), nullptr, nullptr, 0.0);
+        if (valid) {
+            if (!use) surrogate_fallback<true>(e, p, npts, t, ne, dofs, u, mu, lmbda, wsum, nullptr, nullptr, recd,
+                                               flags, counters);
+            else flags[e] = 0;
+        }
+        // tensor-memory reads and operand buffers are free for the next tile
+        tc::fence_before_sync();
+        __syncthreads();
     }
+    if (!tc_ok && tid == 0) atomicAdd(counters + 1, 1ULL);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTcCols);
 }
 
 }  // namespace
@@ -640,7 +1063,8 @@ extern "C" int skg_mlp_train(float *d_params, const float *d_features, const flo
             SKG_LAUNCH_CHECK("mlp_adam");
             offset = (offset + batch) % n;
         }
-        k_stress_shift<<<1, 32, 0, s>>>(d_params);
+        SKG_CUDA(cudaFuncSetAttribute(k_stress_shift, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem));
+        k_stress_shift<<<1, kEvalBlock, kEvalSmem, s>>>(d_params);
         SKG_LAUNCH_CHECK("mlp_stress_shift");
         if (h_last_loss) {
             k_sum_loss<float><<<1, 32, 0, s>>>(nb, lb.get(), lsum.get());
@@ -757,7 +1181,8 @@ extern "C" int skg_mlp_refine(float *d_params, const float *d_features, const fl
         }
         for (int k = 0; k < NPARAM; ++k) hp[k] = (float)x[k];
         SKG_CUDA(cudaMemcpyAsync(d_params, hp.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice, s));
-        k_stress_shift<<<1, 32, 0, s>>>(d_params);
+        SKG_CUDA(cudaFuncSetAttribute(k_stress_shift, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem));
+        k_stress_shift<<<1, kEvalBlock, kEvalSmem, s>>>(d_params);
         SKG_LAUNCH_CHECK("mlp_stress_shift");
         SKG_CUDA(cudaStreamSynchronize(s));
         if (h_loss) *h_loss = f;
@@ -768,7 +1193,8 @@ extern "C" int skg_mlp_eval(const float *d_params, const float *d_x, int64_t n, 
     return guarded([&] {
         require(d_params && d_x && d_out && n >= 0, "invalid evaluation arguments");
         if (!n) return;
-        k_mlp_eval<<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(n, d_x, d_params, d_out);
+        SKG_CUDA(cudaFuncSetAttribute(k_mlp_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem));
+        k_mlp_eval<<<grid_for(n, kEvalBlock), kEvalBlock, kEvalSmem, as_stream(stream)>>>(n, d_x, d_params, d_out);
         SKG_LAUNCH_CHECK("mlp_eval");
     });
 }
@@ -783,21 +1209,41 @@ extern "C" int skg_nh_assemble_surrogate(const skg_pattern *pat, const double *d
         require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
         require(d_p && d_t && d_u && d_params && d_box, "invalid surrogate arguments");
         cudaStream_t s = as_stream(stream);
-        DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
-        DevBuf<unsigned long long> fb(1, s);
-        SKG_CUDA(cudaMemsetAsync(fb.get(), 0, 8, s));
-        if (ne) {
-            k_nh_surrogate_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
-                                                                    lmbda, wsum, d_params, d_box, tol, Ke.get(),
-                                                                    re.get(), fb.get());
-            SKG_LAUNCH_CHECK("nh_surrogate_element");
+        DevBuf<unsigned long long> fb(2, s);  // [0] fallback elements, [1] tensor-core waits given up
+        SKG_CUDA(cudaMemsetAsync(fb.get(), 0, 16, s));
+        if (d_values && pat->max_row_len > 0) {  // fused path, network on the tensor cores
+            DevBuf<float> recf((size_t)ne * kNhRecF, s);
+            DevBuf<double> recd((size_t)ne * kNhRecD, s);
+            DevBuf<unsigned char> flags((size_t)ne, s);
+            if (ne) {
+                SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)kTcSmem));
+                const int64_t tiles = (ne + kTcRows - 1) / kTcRows;
+                const unsigned grid = (unsigned)(tiles < kSmCount ? tiles : kSmCount);
+                k_nh_surrogate_tc<<<grid, kTcRows, kTcSmem, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
+                                                                 lmbda, wsum, d_params, d_box, tol, recf.get(),
+                                                                 recd.get(), flags.get(), fb.get());
+                SKG_LAUNCH_CHECK("nh_surrogate_tc");
+            }
+            nh_rows(pat, recd.get(), recf.get(), flags.get(), d_residual, d_values, s);
+        } else {
+            DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
+            if (ne) {
+                SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_element<false>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem));
+                k_nh_surrogate_element<false><<<grid_for(ne, kEvalBlock), kEvalBlock, kEvalSmem, s>>>(
+                    ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum, d_params, d_box, tol, Ke.get(),
+                    re.get(), nullptr, nullptr, nullptr, fb.get());
+                SKG_LAUNCH_CHECK("nh_surrogate_element");
+            }
+            nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
         }
-        nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
         if (h_fallback) {
-            unsigned long long h = 0;
-            SKG_CUDA(cudaMemcpyAsync(&h, fb.get(), 8, cudaMemcpyDeviceToHost, s));
+            unsigned long long h[2] = {0, 0};
+            SKG_CUDA(cudaMemcpyAsync(h, fb.get(), 16, cudaMemcpyDeviceToHost, s));
             SKG_CUDA(cudaStreamSynchronize(s));
-            *h_fallback = (int64_t)h;
+            *h_fallback = (int64_t)h[0];
+            require(h[1] == 0, "tensor-core MMA wait timed out (elements fell back to the plain law)", SKG_ECUDA);
         }
     });
 }

@@ -1,0 +1,45 @@
+// Fused neo-Hookean row pass: per-element records in, CSR tangent values and
+// the residual vector out, no element matrices in memory.
+//
+// Plain record (FP64, kNhRecD doubles per element):
+//   [0, 12)  g_a = grad lambda_a          [12, 24) h_a = F^-T g_a
+//   [24, 33) V P (first Piola times measure)
+//   33: mu V    34: (mu - lambda ln J) V    35: lambda V
+// so that K_(a,i),(b,k) = mu V d_ik g_a.g_b + c2 V h_b,i h_a,k + lambda V h_a,i h_b,k
+// and r_(a,i) = sum_j (V P)_ij g_a,j.
+//
+// Surrogate record (FP32, kNhRecF floats per element):
+//   [0, 84)  V A_iJkL, row i at 28 i (27 entries + pad), A the tangent tensor
+//   [84, 96) g_a                 [96, 105) V P
+// so that K_(a,i),(b,k) = sum_JL g_a,J (V A)_iJkL g_b,L.
+#pragma once
+
+#include "skg_common.cuh"
+#include "skg_df64.cuh"
+#include "skg_nh.cuh"
+
+namespace skg {
+
+constexpr int kNhRecD = 36;
+constexpr int kNhRecF = 108;
+
+__device__ __forceinline__ void write_plain_record(const NhGeom &g, const NhLaw &L, double mu, double lmbda,
+                                                   double *__restrict__ r) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            r[a * 3 + j] = g.g[a][j];
+            r[12 + a * 3 + j] = L.FiT[j * 3] * g.g[a][0] + L.FiT[j * 3 + 1] * g.g[a][1] + L.FiT[j * 3 + 2] * g.g[a][2];
+        }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r[24 + k] = g.V * L.P[k];
+    r[33] = mu * g.V;
+    r[34] = (mu - lmbda * L.lnJ) * g.V;
+    r[35] = lmbda * g.V;
+}
+
+void nh_rows(const skg_pattern *pat, const double *recd, const float *recf, const unsigned char *flags,
+             double *d_residual, double *d_values, cudaStream_t s);
+
+}  // namespace skg

@@ -122,10 +122,11 @@ def test_surrogate_assembly_accuracy_and_fallback(surrogate):
     er, ek = relerr(r1, r0), relerr(K1.data, d0)
     print(f"surrogate max relative error: residual {er:.3e}, tangent {ek:.3e}")
     assert er < SURROGATE_RTOL and ek < SURROGATE_RTOL
-    # every element failing the stress check: the plain law everywhere, bit for bit
+    # every element failing the stress check: the FP64 plain law everywhere
+    # (summed in double-float slots on the surrogate path)
     r2, K2 = nh.assemble(u, surrogate=surrogate, tol=-1.0)
     assert nh.last_fallback == m.nelements
-    assert np.array_equal(r2, r0) and np.array_equal(K2.data, d0)
+    assert relerr(r2, r0) < 1e-13 and relerr(K2.data, d0) < 1e-13
     # larger deformations: elements outside the trained range fall back
     u3 = sine_displacement(b, amplitude=0.2)
     r3, K3 = nh.assemble(u3)
