@@ -525,7 +525,8 @@ template <bool FUSED>
 __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float *__restrict__ Nrm, const float gx[3],
                                                  const float Hx[9], double mu, double lmbda, float tol, float Vf,
                                                  const float ga[4][3], float4 *__restrict__ out, double *__restrict__ Ke,
-                                                 double *__restrict__ re, double V) {
+                                                 double *__restrict__ re, double V, int i_begin = 0, int i_end = 3,
+                                                 bool tail = true) {
     const float *F = st.F, *C = st.C, *FiT = st.FiT;
     const float I1 = st.I1, J = st.J, iJ = 1.f / st.J;
     // derivatives of W with respect to the features f
@@ -573,9 +574,19 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
         nrm = fmaxf(nrm, fabsf(pl));
     }
     if (!(diff <= tol * fmaxf(nrm, 1e-3f))) return false;
-    // tangent A_iJkL, one row block i (27 entries) at a time
+    // tangent A_iJkL, one row block i (27 entries) at a time; the row-i
+    // quantities are selected once so that the block body is compiled once
+#pragma unroll 1
+    for (int i = i_begin; i < i_end; ++i) {
+        float dIr[3][3], Fr[3], FiTr[3], FFtr[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
+        for (int c = 0; c < 3; ++c) {
+#pragma unroll
+            for (int m = 0; m < 3; ++m) dIr[m][c] = i == 0 ? dI[m][c] : i == 1 ? dI[m][3 + c] : dI[m][6 + c];
+            Fr[c] = i == 0 ? F[c] : i == 1 ? F[3 + c] : F[6 + c];
+            FiTr[c] = i == 0 ? FiT[c] : i == 1 ? FiT[3 + c] : FiT[6 + c];
+            FFtr[c] = i == 0 ? FFt[c] : i == 1 ? FFt[3 + c] : FFt[6 + c];
+        }
         float Ai[28];
 #pragma unroll
         for (int Jj = 0; Jj < 3; ++Jj)
@@ -583,17 +594,17 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
             for (int k = 0; k < 3; ++k)
 #pragma unroll
                 for (int L = 0; L < 3; ++L) {
-                    const int a = i * 3 + Jj, b = k * 3 + L;
+                    const int b = k * 3 + L;
                     float v = 0.f;
 #pragma unroll
                     for (int m = 0; m < 3; ++m)
 #pragma unroll
-                        for (int l = 0; l < 3; ++l) v += Wab[m * 3 + l] * dI[m][a] * dI[l][b];
+                        for (int l = 0; l < 3; ++l) v += Wab[m * 3 + l] * dIr[m][Jj] * dI[l][b];
                     const float dik = i == k ? 1.f : 0.f, dJL = Jj == L ? 1.f : 0.f;
                     v += Wa[0] * 2.f * dik * dJL;
-                    v += Wa[1] * 2.f * (2.f * F[a] * F[b] + I1 * dik * dJL - dik * C[L * 3 + Jj] -
-                                        F[i * 3 + L] * F[k * 3 + Jj] - FFt[i * 3 + k] * dJL);
-                    v += Wa[2] * J * (FiT[a] * FiT[b] - FiT[i * 3 + L] * FiT[k * 3 + Jj]);
+                    v += Wa[1] * 2.f * (2.f * Fr[Jj] * F[b] + I1 * dik * dJL - dik * C[L * 3 + Jj] -
+                                        Fr[L] * F[k * 3 + Jj] - FFtr[k] * dJL);
+                    v += Wa[2] * J * (FiTr[Jj] * FiT[b] - FiTr[L] * FiT[k * 3 + Jj]);
                     Ai[Jj * 9 + b] = v;
                 }
         Ai[27] = 0.f;
@@ -618,6 +629,7 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
             }
         }
     }
+    if (!tail) return true;
     if constexpr (FUSED) {
         out[21] = make_float4(ga[0][0], ga[0][1], ga[0][2], ga[1][0]);
         out[22] = make_float4(ga[1][1], ga[1][2], ga[2][0], ga[2][1]);
@@ -708,16 +720,22 @@ __global__ void __launch_bounds__(kEvalBlock) k_nh_surrogate_element(
 // ------------------------------------------------- surrogate on tensor cores
 //
 // Tiles of 128 elements, one per CTA at a time (persistent CTAs, one per SM),
-// thread t = element row t = tensor-memory lane t.  The two 64 x 64 layers are
-// tcgen05 MMAs (kind::tf32) with FP32-accurate products: every operand is
-// split x = hi + lo in tf32 and D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
+// element row r = tensor-memory lane r.  The two 64 x 64 layers are tcgen05
+// MMAs (kind::tf32) with FP32-accurate products: every operand is split
+// x = hi + lo in tf32 and D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
 //   GEMM 1: [a2 | B0 | B1 | B2] = [Z1 | Q0 | Q1 | Q2] W2^T    (TMEM columns 0..255)
 //           with Q_m[e][j] = s1[e][j] W1[j][m]  (B = W2 diag(s1) W1 per element)
 //   GEMM 2: u1 = D2 W2                                          (TMEM columns 0..63)
-// and everything elementwise (tanh, Hessian contractions, stress, tangent)
-// on the CUDA cores of the owning thread.  Shared memory: W2 and W2^T (hi,
-// lo) as B operands, two 128 x 64 A-operand buffers (hi, lo), small vectors.
+// Two threads per element row (warps w and w + 4 share the row's lane
+// quarter): each owns half of the hidden units for the elementwise work
+// (tanh, operand writes, Hessian contractions); their partial gradient and
+// Hessian sums are exchanged through shared memory and added in the same
+// order by both.  The tangent's row blocks are split between the two.
+// Shared memory: W2 and W2^T (hi, lo) as B operands, two 128 x 64 A-operand
+// buffers (hi, lo), small vectors, the partial sums.
 constexpr int kTcRows = 128;
+constexpr int kTcThreads = 2 * kTcRows;
+constexpr int kHalf = H / 2;
 constexpr uint32_t kTcCols = 256;
 constexpr int kOpBytes = kTcRows * H * 4;  // one 128 x 64 tf32 operand
 constexpr int kWBytes = H * H * 4;
@@ -725,8 +743,16 @@ constexpr int SM_W2B_HI = 0, SM_W2B_LO = kWBytes, SM_W2T_HI = 2 * kWBytes, SM_W2
 constexpr int SM_OPA_HI = 4 * kWBytes, SM_OPA_LO = SM_OPA_HI + kOpBytes;
 constexpr int SM_OPB_HI = SM_OPA_LO + kOpBytes, SM_OPB_LO = SM_OPB_HI + kOpBytes;
 constexpr int SM_Q = SM_OPB_LO + kOpBytes;
-constexpr size_t kTcSmem = SM_Q + QSIZE * 4;
+constexpr int kPart = 9;  // gx (3) + H (6)
+constexpr int SM_PART = SM_Q + QSIZE * 4;
+constexpr size_t kTcSmem = SM_PART + sizeof(float) * 2 * kTcRows * kPart;
 constexpr uint32_t kTcWaitLimit = 1u << 24;
+
+// tanh(a) = 1 - 2 / (exp(2a) + 1) with the fast exponential and division;
+// absolute error ~1e-7, which is what the layer sums see.
+__device__ __forceinline__ float tanh_fast(float a) {
+    return 1.f - __fdividef(2.f, __expf(2.f * a) + 1.f);
+}
 
 // Writes 4 consecutive k of row `row` into an A operand (tf32 hi and lo parts).
 __device__ __forceinline__ void put_op4(unsigned char *hi, unsigned char *lo, int row, int k, float a, float b,
@@ -813,7 +839,7 @@ __device__ __forceinline__ bool geometry_fp32(const double *__restrict__ p, int6
     return ok;
 }
 
-__global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
+__global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
     int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
     const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda, double wsum,
     const float *__restrict__ params, const float *__restrict__ box, float tol, float *__restrict__ recf,
@@ -822,12 +848,14 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = tid & (kTcRows - 1), half = tid / kTcRows, jb = half * kHalf;
     float *Q = reinterpret_cast<float *>(smem + SM_Q);
+    float *part = reinterpret_cast<float *>(smem + SM_PART);  // [half][kPart][row]
     unsigned char *opa_hi = smem + SM_OPA_HI, *opa_lo = smem + SM_OPA_LO;
     unsigned char *opb_hi = smem + SM_OPB_HI, *opb_lo = smem + SM_OPB_LO;
     const unsigned char *w2b_hi = smem + SM_W2B_HI, *w2b_lo = smem + SM_W2B_LO;
     const unsigned char *w2t_hi = smem + SM_W2T_HI, *w2t_lo = smem + SM_W2T_LO;
-    for (int k = tid; k < H * H; k += kTcRows) {
+    for (int k = tid; k < H * H; k += kTcThreads) {
         const int i = k / H, j = k - (k / H) * H;
         const float w = params[OW2 + k], hi = tc::to_tf32(w), lo = tc::to_tf32(w - hi);
         *reinterpret_cast<float *>(smem + SM_W2B_HI + tc::operand_offset(H, i, j)) = hi;
@@ -835,7 +863,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
         *reinterpret_cast<float *>(smem + SM_W2T_HI + tc::operand_offset(H, j, i)) = hi;
         *reinterpret_cast<float *>(smem + SM_W2T_LO + tc::operand_offset(H, j, i)) = lo;
     }
-    for (int k = tid; k < QSIZE; k += kTcRows) {
+    for (int k = tid; k < QSIZE; k += kTcThreads) {
         float v = 0.f;
         if (k < QB2) v = params[OW1 + k];
         else if (k < QB3 + 1) v = params[OB2 + (k - QB2)];
@@ -850,12 +878,12 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
     if (warp == 0) tc::tmem_alloc(&tslot, kTcCols);
     sync_for_mma();
     const uint32_t tmem = tslot;
-    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+    const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lane quarter
     const float *Nrm = Q + QNORM;
     uint32_t phase = 0;
     bool tc_ok = true;
     for (int64_t tile = blockIdx.x; tile * kTcRows < ne; tile += gridDim.x) {
-        const int64_t e = tile * kTcRows + tid;
+        const int64_t e = tile * kTcRows + row;
         const bool valid = e < ne;
         float ga[4][3], Vf = 0.f, F[9];
         bool geo = false;
@@ -869,24 +897,23 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
         bool use = valid && geo && st.ok && in_box(st, box);
         float x[3] = {0.f, 0.f, 0.f};
         if (use) normalised_input(st, Nrm, x);
-        float psi = Q[QB3] + Q[QC] * x[0] + Q[QC + 1] * x[1] + Q[QC + 2] * x[2];
-        float z1[H];
+        float z1[kHalf];  // hidden units jb .. jb + 31
         if (tc_ok) {
-            // ---- layer 1; A operands Z1 and Q0
+            // ---- layer 1; A operands Z1 and Q0 (own half of the columns)
 #pragma unroll
-            for (int j0 = 0; j0 < H; j0 += 4) {
+            for (int c0 = 0; c0 < kHalf; c0 += 4) {
                 float zz[4], q0[4];
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const int j = j0 + c;
+                    const int j = jb + c0 + c;
                     const float a = Q[QB1 + j] + Q[QW1 + 3 * j] * x[0] + Q[QW1 + 3 * j + 1] * x[1] +
                                     Q[QW1 + 3 * j + 2] * x[2];
-                    z1[j] = tanhf(a);
-                    zz[c] = z1[j];
-                    q0[c] = (1.f - z1[j] * z1[j]) * Q[QW1 + 3 * j];
+                    z1[c0 + c] = tanh_fast(a);
+                    zz[c] = z1[c0 + c];
+                    q0[c] = (1.f - zz[c] * zz[c]) * Q[QW1 + 3 * j];
                 }
-                put_op4(opa_hi, opa_lo, tid, j0, zz[0], zz[1], zz[2], zz[3]);
-                put_op4(opb_hi, opb_lo, tid, j0, q0[0], q0[1], q0[2], q0[3]);
+                put_op4(opa_hi, opa_lo, row, jb + c0, zz[0], zz[1], zz[2], zz[3]);
+                put_op4(opb_hi, opb_lo, row, jb + c0, q0[0], q0[1], q0[2], q0[3]);
             }
             sync_for_mma();
             if (tid == 0) {
@@ -900,17 +927,17 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
         if (tc_ok) {
             // ---- A operands Q1 and Q2
 #pragma unroll
-            for (int j0 = 0; j0 < H; j0 += 4) {
+            for (int c0 = 0; c0 < kHalf; c0 += 4) {
                 float q1[4], q2[4];
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const int j = j0 + c;
-                    const float s1 = 1.f - z1[j] * z1[j];
+                    const int j = jb + c0 + c;
+                    const float s1 = 1.f - z1[c0 + c] * z1[c0 + c];
                     q1[c] = s1 * Q[QW1 + 3 * j + 1];
                     q2[c] = s1 * Q[QW1 + 3 * j + 2];
                 }
-                put_op4(opa_hi, opa_lo, tid, j0, q1[0], q1[1], q1[2], q1[3]);
-                put_op4(opb_hi, opb_lo, tid, j0, q2[0], q2[1], q2[2], q2[3]);
+                put_op4(opa_hi, opa_lo, row, jb + c0, q1[0], q1[1], q1[2], q1[3]);
+                put_op4(opb_hi, opb_lo, row, jb + c0, q2[0], q2[1], q2[2], q2[3]);
             }
             sync_for_mma();
             if (tid == 0) {
@@ -921,32 +948,34 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
             tc_ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kTcWaitLimit));
             phase ^= 1;
         }
-        float h00 = 0.f, h01 = 0.f, h02 = 0.f, h11 = 0.f, h12 = 0.f, h22 = 0.f;
+        float pr[kPart];  // gx (3), H (6) partial sums of this half
+#pragma unroll
+        for (int k = 0; k < kPart; ++k) pr[k] = 0.f;
         if (tc_ok) {
-            // ---- layer 2 and the second Hessian term; A operand D2
+            // ---- layer 2 (own half of the outputs) and the second Hessian term; A operand D2
             tc::fence_after_sync();
 #pragma unroll
-            for (int ch = 0; ch < H / 16; ++ch) {
+            for (int ch = 0; ch < kHalf / 16; ++ch) {
+                const int c0 = jb + ch * 16;
                 float a2[16], b0[16], b1[16], b2[16], dv[16];
-                tc::tmem_ld16(tl + ch * 16, a2);
-                tc::tmem_ld16(tl + 64 + ch * 16, b0);
-                tc::tmem_ld16(tl + 128 + ch * 16, b1);
-                tc::tmem_ld16(tl + 192 + ch * 16, b2);
+                tc::tmem_ld16(tl + c0, a2);
+                tc::tmem_ld16(tl + 64 + c0, b0);
+                tc::tmem_ld16(tl + 128 + c0, b1);
+                tc::tmem_ld16(tl + 192 + c0, b2);
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
-                    const int i = ch * 16 + q;
-                    const float z2 = tanhf(a2[q] + Q[QB2 + i]), w3 = Q[QW3 + i];
+                    const int i = c0 + q;
+                    const float z2 = tanh_fast(a2[q] + Q[QB2 + i]), w3 = Q[QW3 + i];
                     const float d2 = (1.f - z2 * z2) * w3;
-                    psi += w3 * z2;
                     dv[q] = d2;
                     const float t2 = -2.f * z2 * d2;
                     const float tb0 = t2 * b0[q], tb1 = t2 * b1[q];
-                    h00 += tb0 * b0[q]; h01 += tb0 * b1[q]; h02 += tb0 * b2[q];
-                    h11 += tb1 * b1[q]; h12 += tb1 * b2[q]; h22 += t2 * b2[q] * b2[q];
+                    pr[3] += tb0 * b0[q]; pr[4] += tb0 * b1[q]; pr[5] += tb0 * b2[q];
+                    pr[6] += tb1 * b1[q]; pr[7] += tb1 * b2[q]; pr[8] += t2 * b2[q] * b2[q];
                 }
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
-                    put_op4(opa_hi, opa_lo, tid, ch * 16 + 4 * r, dv[4 * r], dv[4 * r + 1], dv[4 * r + 2], dv[4 * r + 3]);
+                    put_op4(opa_hi, opa_lo, row, c0 + 4 * r, dv[4 * r], dv[4 * r + 1], dv[4 * r + 2], dv[4 * r + 3]);
             }
             sync_for_mma();
             if (tid == 0) {
@@ -956,43 +985,49 @@ __global__ void __launch_bounds__(kTcRows, 1) k_nh_surrogate_tc(
             tc_ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kTcWaitLimit));
             phase ^= 1;
         }
-        float gx[3] = {Q[QC], Q[QC + 1], Q[QC + 2]}, Hx[9];
         if (tc_ok) {
-            // ---- u1 = W2^T d2: gradient and first Hessian term
+            // ---- u1 = W2^T d2 (own half): gradient and first Hessian term
             tc::fence_after_sync();
 #pragma unroll
-            for (int ch = 0; ch < H / 16; ++ch) {
+            for (int ch = 0; ch < kHalf / 16; ++ch) {
                 float u1[16];
-                tc::tmem_ld16(tl + ch * 16, u1);
+                tc::tmem_ld16(tl + jb + ch * 16, u1);
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
-                    const int j = ch * 16 + q;
-                    const float d1 = (1.f - z1[j] * z1[j]) * u1[q];
+                    const int jl = ch * 16 + q, j = jb + jl;
+                    const float d1 = (1.f - z1[jl] * z1[jl]) * u1[q];
                     const float w0 = Q[QW1 + 3 * j], w1 = Q[QW1 + 3 * j + 1], w2 = Q[QW1 + 3 * j + 2];
-                    gx[0] += w0 * d1;
-                    gx[1] += w1 * d1;
-                    gx[2] += w2 * d1;
-                    const float r = -2.f * z1[j] * d1;
-                    h00 += r * w0 * w0; h01 += r * w0 * w1; h02 += r * w0 * w2;
-                    h11 += r * w1 * w1; h12 += r * w1 * w2; h22 += r * w2 * w2;
+                    pr[0] += w0 * d1;
+                    pr[1] += w1 * d1;
+                    pr[2] += w2 * d1;
+                    const float rr = -2.f * z1[jl] * d1;
+                    pr[3] += rr * w0 * w0; pr[4] += rr * w0 * w1; pr[5] += rr * w0 * w2;
+                    pr[6] += rr * w1 * w1; pr[7] += rr * w1 * w2; pr[8] += rr * w2 * w2;
                 }
             }
         } else {
             use = false;  // tensor-core phase gave up: plain law for the rest
         }
-        Hx[0] = h00; Hx[1] = h01; Hx[2] = h02;
-        Hx[3] = h01; Hx[4] = h11; Hx[5] = h12;
-        Hx[6] = h02; Hx[7] = h12; Hx[8] = h22;
-        (void)psi;
+        // ---- combine the two halves (same order in both: bitwise equal sums)
+#pragma unroll
+        for (int k = 0; k < kPart; ++k) part[(half * kPart + k) * kTcRows + row] = pr[k];
+        __syncthreads();
+        float tot[kPart];
+#pragma unroll
+        for (int k = 0; k < kPart; ++k)
+            tot[k] = part[(0 * kPart + k) * kTcRows + row] + part[(1 * kPart + k) * kTcRows + row];
+        const float gx[3] = {Q[QC] + tot[0], Q[QC + 1] + tot[1], Q[QC + 2] + tot[2]};
+        const float Hx[9] = {tot[3], tot[4], tot[5], tot[4], tot[6], tot[7], tot[5], tot[7], tot[8]};
         if (use)
             use = surrogate_finish<true>(st, Nrm, gx, Hx, mu, lmbda, tol, Vf, ga,
-                                         reinterpret_cast<float4 *>(recf + e * kNhRecF), nullptr, nullptr, 0.0);
-        if (valid) {
+                                         reinterpret_cast<float4 *>(recf + e * kNhRecF), nullptr, nullptr, 0.0,
+                                         half == 0 ? 0 : 2, half == 0 ? 2 : 3, half == 1);
+        if (valid && half == 1) {
             if (!use) surrogate_fallback<true>(e, p, npts, t, ne, dofs, u, mu, lmbda, wsum, nullptr, nullptr, recd,
                                                flags, counters);
             else flags[e] = 0;
         }
-        // tensor-memory reads and operand buffers are free for the next tile
+        // tensor-memory reads, operand buffers and partial sums are free for the next tile
         tc::fence_before_sync();
         __syncthreads();
     }
@@ -1220,7 +1255,7 @@ extern "C" int skg_nh_assemble_surrogate(const skg_pattern *pat, const double *d
                                               (int)kTcSmem));
                 const int64_t tiles = (ne + kTcRows - 1) / kTcRows;
                 const unsigned grid = (unsigned)(tiles < kSmCount ? tiles : kSmCount);
-                k_nh_surrogate_tc<<<grid, kTcRows, kTcSmem, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
+                k_nh_surrogate_tc<<<grid, kTcThreads, kTcSmem, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
                                                                  lmbda, wsum, d_params, d_box, tol, recf.get(),
                                                                  recd.get(), flags.get(), fb.get());
                 SKG_LAUNCH_CHECK("nh_surrogate_tc");
