@@ -597,7 +597,11 @@ def wl_nh(args, world, timed, wall):
     du = dev.to_device(u, np.float64)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sur = sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)
+    if args.quick_train:  # profiling runs: a short schedule (accuracy not representative)
+        sur = sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, n_samples=200_000, steps=300, refine_iters=300,
+                                       refine_samples=65536, seed=1)
+    else:
+        sur = sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     ms_plain, clk = timed(lambda: nh.assemble_device(du))
@@ -617,6 +621,8 @@ def wl_nh(args, world, timed, wall):
         value=world * E / (ms_plain * 1e-3), ms_per_step=ms_plain, dtype="f64", clocks=clk,
         config={"workload": f"vector P1 neo-Hookean, {n}^3x6 cube ({E} tets), 8 sine modes amplitude 0.05, "
                             "unit wavevectors, mu=1, lambda=10, 1-point rule",
+                "training": "short profiling schedule" if args.quick_train else
+                            "2M samples, 3000 Adam steps, L-BFGS on 524,288 samples",
                 "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
         e2e={"value": world * E / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": 8 * b.N,
              "d2h_bytes_per_step": 8 * (b.N + nnz), "ms_per_step": 1e3 * e2e_s},
@@ -731,6 +737,8 @@ def main():
     ap.add_argument("--workload", default="p2_aniso", choices=["p2_aniso"] + sorted(AUX_WORKLOADS),
                     help="p2_aniso (headline) or another row of the assembly path")
     ap.add_argument("--cells", type=int, default=None, help="cube cells per side (smaller cases for profiling)")
+    ap.add_argument("--quick-train", action="store_true",
+                    help="nh workload: short surrogate training (profiling runs only)")
     ap.add_argument("--modes", default="fp64,fp64_emulated,split_fp32",
                     help="precision modes to time; the first is the headline")
     args = ap.parse_args()

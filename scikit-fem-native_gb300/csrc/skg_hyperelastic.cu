@@ -238,17 +238,19 @@ __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
         }
     }
     if (live && part == 0 && residual) {
-        if constexpr (SUR) residual[r] = (double)rf.hi + (double)rf.lo;
+        if constexpr (SUR) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
         else residual[r] = rd;
     }
     __syncwarp();
     if (values) {
         for (int j = lane; j < nslots; j += 32) {
             if constexpr (SUR) {
-                double v = (double)accf[j].hi + (double)accf[j].lo;
+                // copies summed in double-float, converted by integer arithmetic (no FP64 pipe)
+                df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
 #pragma unroll
-                for (int c = 1; c < P; ++c) v += (double)accf[c * nslots + j].hi + (double)accf[c * nslots + j].lo;
-                values[s0 + j] = v;
+                for (int c = 1; c < P; ++c)
+                    v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
+                values[s0 + j] = df_to_double(v, 0);
             } else {
                 double v = accd[j];
 #pragma unroll
