@@ -9,10 +9,11 @@ A = Q diag(exp(N(0, 0.5^2))) Q^T, 4-point quadrature (seeded synthetic data).
   value  assembled CSR nonzeros per second, inputs resident in HBM (both
          kernels of the fused affine path, CUDA events on the launching
          stream); inputs (~670 MB per step) exceed the 129 MB L2.
-  e2e    same metric through the assembler's host-facing API: per step the
-         coefficient A (3,3,E) goes host->device from page-locked memory and
-         the CSR values come back device->host into the page-locked buffer
-         that backs the returned scipy matrix.
+  e2e    same metric through the assembler's host-facing API
+         (NativeTensorForm.assemble): per step the coefficient A (3,3,E) is
+         read from host memory and the CSR values are written into the
+         page-locked buffer behind the returned scipy matrix (on Grace-
+         Blackwell the kernels do both directly over NVLink-C2C).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -313,15 +314,15 @@ def run_gpu(args, rank, world):
     ms, t_el, t_rows = head["ms_per_step"], head["kernel_ms"]["element_pass"], head["kernel_ms"]["row_pass"]
     value = head["value"]
 
-    # ---- e2e (native FP64): host (page-locked) A in, host CSR values out, through the assembler API
+    # ---- e2e (native FP64) through the assembler's host API: A from host memory in,
+    # the CSR values out into the host matrix (kernels read / write host memory
+    # over NVLink-C2C where the device allows it, else staged copies)
     for _ in range(2):
-        form.assemble_device(A_pub)
-        form.target.download()
+        form.assemble(A_pub, copy=False)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        form.assemble_device(A_pub)
-        form.target.download()
+        form.assemble(A_pub, copy=False)
     barrier()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     e2e_value = world * nnz / e2e_s

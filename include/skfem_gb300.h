@@ -54,6 +54,13 @@ int skg_version(void);
 /* Message of the last failure on the calling thread ("" when none). */
 const char *skg_last_error(void);
 
+/* 1 when kernels on the current device may read and write pageable host
+ * memory directly (Grace-Blackwell: address translation over NVLink-C2C).
+ * The host side then lets kernels read coefficients from, and write CSR
+ * values to, host buffers without staging copies.  No counterpart in the
+ * reference (CPU-only). */
+int skg_device_pageable_access(int32_t *out);
+
 /* ------------------------------------------------------------------ */
 /* Sparsity pattern.                                                    */
 /* Replaces the pattern build of BilinearFormAssembler                  */
@@ -80,6 +87,10 @@ int skg_pattern_destroy(skg_pattern *pattern);
 /* nnz and shape of the pattern. */
 int skg_pattern_info(const skg_pattern *pattern, int64_t *nnz, int64_t *n_rows,
                      int64_t *n_cols);
+/* Longest row of a pattern with row groups (the fused row passes, which
+ * write each CSR value exactly once), 0 when the pattern has none.  No
+ * counterpart in the reference. */
+int skg_pattern_row_groups(const skg_pattern *pattern, int32_t *max_row_len);
 /* Copy the CSR structure out: d_indptr (n_rows+1) int64, d_indices (nnz) int32.
  * Either may be NULL.  (BilinearFormAssembler.indptr / .indices views.) */
 int skg_pattern_export(const skg_pattern *pattern, int64_t *d_indptr,

@@ -1,4 +1,5 @@
-// Library-wide C ABI entry points: version and per-thread last error.
+// Library-wide C ABI entry points: version, per-thread last error, device
+// capabilities the host side needs.
 #include <string>
 
 #include "skg_common.cuh"
@@ -13,3 +14,13 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 extern "C" int skg_version(void) { return 100; }
 
 extern "C" const char *skg_last_error(void) { return skg::g_last_error.c_str(); }
+
+extern "C" int skg_device_pageable_access(int32_t *out) {
+    return skg::guarded([&] {
+        skg::require(out != nullptr, "output pointer is NULL");
+        int dev = 0, v = 0;
+        SKG_CUDA(cudaGetDevice(&dev));
+        SKG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev));
+        *out = v;
+    });
+}

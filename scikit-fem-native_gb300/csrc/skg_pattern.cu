@@ -421,3 +421,10 @@ extern "C" int skg_pattern_export(const skg_pattern *p, int64_t *d_indptr, int32
             SKG_CUDA(cudaMemcpyAsync(d_indices, p->indices.get(), p->nnz * 4, cudaMemcpyDeviceToDevice, s));
     });
 }
+
+extern "C" int skg_pattern_row_groups(const skg_pattern *p, int32_t *max_row_len) {
+    return guarded([&] {
+        require(p != nullptr && max_row_len != nullptr, "pattern or output is NULL");
+        *max_row_len = p->max_row_len;
+    });
+}

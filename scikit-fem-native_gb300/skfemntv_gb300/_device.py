@@ -74,3 +74,51 @@ def pinned_empty(n, dtype=np.float64):
     t = require_cuda()
     buf = t.empty(n, dtype=getattr(t, _TORCH_DTYPES[np.dtype(dtype)]), pin_memory=True)
     return buf, buf.numpy()
+
+
+_PAGEABLE = {}
+
+
+def pageable_access():
+    """True when kernels on the current device can read / write pageable host
+    memory directly (Grace-Blackwell address translation over NVLink-C2C)."""
+    require_cuda()
+    d = torch.cuda.current_device()
+    if d not in _PAGEABLE:
+        from ._native import call
+
+        v = ctypes.c_int32(0)
+        call("skg_device_pageable_access", ctypes.byref(v))
+        _PAGEABLE[d] = bool(v.value)
+    return _PAGEABLE[d]
+
+
+def host_readable(a):
+    """Pointer a kernel can read `a` (float64, C order) through, without a
+    copy, or None: needs pageable access and a C-contiguous float64 array.
+    The caller keeps `a` alive and synchronises before returning."""
+    if a is None or not pageable_access():
+        return None
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        return None
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def host_tensor(a):
+    """CPU torch view of a C-contiguous host array (no copy; read-only arrays
+    are viewed as well, the view is only read)."""
+    import warnings
+
+    t = require_cuda()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        return t.from_numpy(np.ascontiguousarray(a))
+
+
+def host_copy(a):
+    """Multithreaded copy of a host array (torch's parallel CPU copy)."""
+    t = require_cuda()
+    out = np.empty(a.shape, dtype=a.dtype)
+    if a.size:
+        t.from_numpy(out).copy_(host_tensor(a))
+    return out

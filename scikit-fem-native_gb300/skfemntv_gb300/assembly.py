@@ -47,6 +47,10 @@ class Pattern:
         call("skg_pattern_info", h, ctypes.byref(nnz), None, None)
         self.nnz = nnz.value
         self.n_rows, self.n_cols = n_rows, n_cols
+        mrl = ctypes.c_int32(0)
+        call("skg_pattern_row_groups", h, ctypes.byref(mrl))
+        # fused row passes write every CSR value once, so they may write host memory directly
+        self.blocked = mrl.value > 0
 
     def host_csr(self):
         indptr = dev.empty(self.n_rows + 1, np.int64)
@@ -146,7 +150,7 @@ class _Staging:
             self.h, self.hv = dev.pinned_empty(n)
             self.d = dev.empty(n, np.float64)
             self.n = n
-        np.copyto(self.hv[:n].reshape(a.shape), a)
+        self.h[:n].view(a.shape).copy_(dev.host_tensor(a))  # parallel CPU copy
         self.d[:n].copy_(self.h[:n], non_blocking=True)
         self.done = torch.cuda.Event()
         self.done.record()
@@ -170,6 +174,26 @@ class _MatrixTarget:
         torch.cuda.current_stream().synchronize()
         return self.matrix
 
+    def host_out(self):
+        """Pointer kernels can write the host matrix's values through (page-locked
+        memory), when the device can write host memory and the pattern's row pass
+        writes every value once; else None."""
+        if not (self.pattern.blocked and dev.pageable_access()):
+            return None
+        return ctypes.c_void_p(self._pinned.data_ptr())
+
+    def finish_direct(self):
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        return self.matrix
+
+    def copy_matrix(self):
+        """Independent copy of the host matrix (multithreaded copies)."""
+        m = self.matrix
+        return csr_matrix((dev.host_copy(m.data), dev.host_copy(m.indices), dev.host_copy(m.indptr)), shape=m.shape,
+                          copy=False)
+
 
 class NativeBilinearForm:
     """value / gradient / symmetric-gradient / divergence assembly on one basis."""
@@ -187,23 +211,43 @@ class NativeBilinearForm:
     def matrix(self):
         return self.target.matrix
 
+    def _affine_coefficient(self, value, gradient, symmetric_gradient, divergence):
+        """(E,) gradient coefficient when the fused affine path applies, else None."""
+        b = self.basis
+        E, Q = b._coefficient_shape
+        if value is None and gradient is None and symmetric_gradient is None and divergence is None:
+            raise ValueError("at least one coefficient is required")
+        if (b._comp == 1 and value is None and symmetric_gradient is None and divergence is None
+                and b.is_affine):
+            return per_element(gradient, E, Q, "gradient")
+        return None
+
+    def _affine(self, fast, prec, out, host):
+        """Fused affine assembly into `out` (device or, with `host`, page-locked host
+        memory); the coefficient is read in place from host memory when possible
+        (the caller then synchronises before `fast` goes away)."""
+        b = self.basis
+        E, Q = b._coefficient_shape
+        coef = keep = None
+        if not np.all(fast == 1.0):
+            coef = dev.host_readable(fast) if host else None
+            if coef is None:
+                keep = dev.to_device(fast, np.float64)
+                coef = dev.ptr(keep)
+        call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+             dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+             dev.hptr(b.W), 0, coef, prec, out, dev.stream_ptr())
+        return keep
+
     def assemble_device(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
                         precision="fp64"):
         """Assemble into the device values (no host copy); returns the device tensor."""
         b = self.basis
         E, Q = b._coefficient_shape
         prec = _precision(precision)
-        if value is None and gradient is None and symmetric_gradient is None and divergence is None:
-            raise ValueError("at least one coefficient is required")
-        fast = None
-        if (b._comp == 1 and value is None and symmetric_gradient is None and divergence is None
-                and b.is_affine):
-            fast = per_element(gradient, E, Q, "gradient")
+        fast = self._affine_coefficient(value, gradient, symmetric_gradient, divergence)
         if fast is not None:
-            coef = None if np.all(fast == 1.0) else dev.to_device(fast, np.float64)
-            call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
-                 dev.hptr(b.W), 0, dev.ptr(coef), prec, dev.ptr(self.target.d_values), dev.stream_ptr())
+            self._affine(fast, prec, dev.ptr(self.target.d_values), host=False)
             return self.target.d_values
         if prec != SKG_FP64:
             raise UnsupportedNativeForm("split precision is available on the affine scalar gradient path")
@@ -218,6 +262,13 @@ class NativeBilinearForm:
 
     def assemble(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
                  num_threads=0, precision="fp64"):
+        """Host CSR matrix (reused between calls, as the reference's).  On the fused
+        path the kernels write the values straight into its page-locked buffer."""
+        fast = self._affine_coefficient(value, gradient, symmetric_gradient, divergence)
+        out = self.target.host_out() if fast is not None else None
+        if out is not None:
+            self._affine(fast, _precision(precision), out, host=True)
+            return self.target.finish_direct()
         self.assemble_device(value=value, gradient=gradient, symmetric_gradient=symmetric_gradient,
                              divergence=divergence, precision=precision)
         return self.target.download()
@@ -243,35 +294,52 @@ class NativeTensorForm:
         """Assemble into the device values.  ``tensor_device``: a per-element
         float64 device tensor already resident, (3,3,E) for tensor_kind 2 or
         (E,3,3) for tensor_kind 1 (skips the host upload)."""
+        self._run(raw, precision, tensor_device, tensor_kind, None)
+        return self.target.d_values
+
+    def _run(self, raw, precision, tensor_device, tensor_kind, out):
+        """Launch the assembly; with `out` (host values pointer) the fused path
+        writes there and reads a per-element tensor in place from host memory.
+        Returns True when the values went to `out`."""
         b = self.basis
         E, Q = b._coefficient_shape
         prec = _precision(precision)
         kind = tensor_kind
-        d_coef = tensor_device
-        if d_coef is None and b.is_affine:
+        coef = keep = None
+        if tensor_device is not None:
+            coef = dev.ptr(tensor_device)
+        elif b.is_affine:
             pe = tensor_per_element(raw, E, Q)
             if pe is not None:
                 arr, kind = pe
-                d_coef = self._staging.upload(arr)
-        if d_coef is not None:
+                coef = dev.host_readable(arr) if out is not None else None
+                if coef is None:
+                    keep = self._staging.upload(arr)
+                    coef = dev.ptr(keep)
+        if coef is not None:
+            direct = out is not None
             call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
                  dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
-                 dev.hptr(b.W), kind, dev.ptr(d_coef), prec, dev.ptr(self.target.d_values),
+                 dev.hptr(b.W), kind, coef, prec, out if direct else dev.ptr(self.target.d_values),
                  dev.stream_ptr())
-            return self.target.d_values
+            return direct
         if prec != SKG_FP64:
             raise UnsupportedNativeForm("split precision is available on the affine tensor path")
         T = anisotropic_tensor(raw, E, Q)
         tab = b._device_tabulation()
-        coef = self._staging.upload(T)
+        d = self._staging.upload(T)
         call("skg_h1_assemble_tensor_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, 1, Q,
-             dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(coef), dev.ptr(self.target.d_values), None,
+             dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(d), dev.ptr(self.target.d_values), None,
              dev.stream_ptr())
-        return self.target.d_values
+        return False
 
-    def assemble(self, raw, precision="fp64"):
-        self.assemble_device(raw, precision)
-        return self.target.download().copy()
+    def assemble(self, raw, precision="fp64", copy=True):
+        """Host CSR matrix.  ``copy=True`` (the reference's behaviour,
+        bilinear_form.py:367) returns an independent matrix; ``copy=False`` the
+        reused one whose page-locked values the fused kernels write directly."""
+        direct = self._run(raw, precision, None, 2, self.target.host_out())
+        m = self.target.finish_direct() if direct else self.target.download()
+        return self.target.copy_matrix() if copy else m
 
 
 class NativeLinearForm:

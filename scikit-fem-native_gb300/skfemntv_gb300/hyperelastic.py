@@ -138,30 +138,50 @@ class NeoHookean:
         self.d_res = dev.empty(max(1, basis.N), np.float64)
         self.wsum = float(np.sum(basis.W))
         self.last_fallback = 0
+        self._res_pinned = self._res_host = None
+
+    def _launch(self, u_ptr, surrogate, tol, res_ptr, val_ptr, count_fallback):
+        b = self.basis
+        if surrogate is None:
+            self.last_fallback = 0
+            call("skg_nh_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, u_ptr, self.mu, self.lmbda, self.wsum, res_ptr,
+                 val_ptr, dev.stream_ptr())
+        else:
+            fb = ctypes.c_int64(-1)
+            call("skg_nh_assemble_surrogate", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, u_ptr, self.mu, self.lmbda, self.wsum,
+                 dev.ptr(surrogate.params), dev.ptr(surrogate.box), ctypes.c_float(tol), res_ptr, val_ptr,
+                 ctypes.byref(fb) if count_fallback else None, dev.stream_ptr())
+            self.last_fallback = int(fb.value)
 
     def assemble_device(self, u, surrogate=None, tol=1e-3, residual=True, tangent=True, count_fallback=True):
         """Residual / tangent into device buffers.  With ``count_fallback`` the
         number of plain-law elements is read back (a host synchronisation)."""
-        b = self.basis
         du = u if hasattr(u, "data_ptr") else dev.to_device(np.asarray(u, dtype=np.float64), np.float64)
         r = self.d_res if residual else None
         k = self.target.d_values if tangent else None
-        if surrogate is None:
-            self.last_fallback = 0
-            call("skg_nh_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, dev.ptr(du), self.mu, self.lmbda, self.wsum, dev.ptr(r),
-                 dev.ptr(k), dev.stream_ptr())
-        else:
-            fb = ctypes.c_int64(-1)
-            call("skg_nh_assemble_surrogate", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, dev.ptr(du), self.mu, self.lmbda, self.wsum,
-                 dev.ptr(surrogate.params), dev.ptr(surrogate.box), ctypes.c_float(tol), dev.ptr(r), dev.ptr(k),
-                 ctypes.byref(fb) if count_fallback else None, dev.stream_ptr())
-            self.last_fallback = int(fb.value)
+        self._launch(dev.ptr(du), surrogate, tol, dev.ptr(r), dev.ptr(k), count_fallback)
         return r, k
 
     def assemble(self, u, surrogate=None, tol=1e-3):
-        """(residual vector, tangent csr_matrix) at displacement u (N,)."""
-        self.assemble_device(u, surrogate=surrogate, tol=tol)
-        K = self.target.download()
-        return self.d_res[: self.basis.N].cpu().numpy(), K
+        """(residual vector, tangent csr_matrix) at displacement u (N,).  The
+        tangent matrix is reused between calls; on the fused path the kernels read
+        u from host memory and write the residual and the CSR values straight
+        into page-locked host buffers."""
+        out = self.target.host_out()
+        if out is None or hasattr(u, "data_ptr"):
+            self.assemble_device(u, surrogate=surrogate, tol=tol)
+            K = self.target.download()
+            return self.d_res[: self.basis.N].cpu().numpy(), K
+        ua = np.ascontiguousarray(np.asarray(u, dtype=np.float64))
+        u_ptr = dev.host_readable(ua)
+        keep = None
+        if u_ptr is None:
+            keep = dev.to_device(ua, np.float64)
+            u_ptr = dev.ptr(keep)
+        if self._res_pinned is None:
+            self._res_pinned, self._res_host = dev.pinned_empty(max(1, self.basis.N))
+        self._launch(u_ptr, surrogate, tol, ctypes.c_void_p(self._res_pinned.data_ptr()), out, True)
+        K = self.target.finish_direct()
+        return self._res_host[: self.basis.N].copy(), K
