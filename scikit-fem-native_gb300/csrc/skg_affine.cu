@@ -101,6 +101,64 @@ __device__ __forceinline__ void flush_stage(const float4 *stage, float4 *Gout, i
     for (int i = threadIdx.x; i < nvalid * 8; i += kElemBlock) dst[i] = stage[(i >> 3) * kStagePad + (i & 7)];
 }
 
+// G_kl = b_k . A b_l / |det J| of element e in FP64 (b: adjugate rows, the
+// scaled barycentric gradients).  Returns the element's symmetry (scalar
+// coefficient, or a tensor equal to its transpose).
+__device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                            const int32_t *__restrict__ t, int coef_kind,
+                                            const double *__restrict__ coef, int64_t e, double g[16]) {
+    int32_t v[4];
+    const bool ok = load_vertices(t, ne, e, npts, v);
+    double J[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double x0 = p[i * npts + v[0]];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
+    }
+    double b[4][3];
+    b[1][0] = J[4] * J[8] - J[5] * J[7];
+    b[1][1] = J[2] * J[7] - J[1] * J[8];
+    b[1][2] = J[1] * J[5] - J[2] * J[4];
+    b[2][0] = J[5] * J[6] - J[3] * J[8];
+    b[2][1] = J[0] * J[8] - J[2] * J[6];
+    b[2][2] = J[2] * J[3] - J[0] * J[5];
+    b[3][0] = J[3] * J[7] - J[4] * J[6];
+    b[3][1] = J[1] * J[6] - J[0] * J[7];
+    b[3][2] = J[0] * J[4] - J[1] * J[3];
+    const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
+    const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
+    if (coef_kind == 0) {
+        const double sc = (coef ? coef[e] : 1.0) * inv;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int l = k; l < 4; ++l) {
+                const double val = sc * (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]);
+                g[k * 4 + l] = val;
+                g[l * 4 + k] = val;
+            }
+        return true;
+    }
+    double A[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        double Ab[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Ab[i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g[k * 4 + l] = inv * (b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2]);
+    }
+    // symmetric to rounding (A built as Q D Q^T in floating point is not bitwise
+    // symmetric): mirroring K_ab into K_ba then changes entries by ~1e-16 relative
+    const double scale = 1e-14 * (fabs(A[0]) + fabs(A[4]) + fabs(A[8]) + fabs(A[1]) + fabs(A[2]) + fabs(A[5]));
+    return fabs(A[1] - A[3]) <= scale && fabs(A[2] - A[6]) <= scale && fabs(A[5] - A[7]) <= scale;
+}
+
 __global__ void __launch_bounds__(kElemBlock) k_elem_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                                           const int32_t *__restrict__ t, int coef_kind,
                                                           const double *__restrict__ coef, float4 *__restrict__ G) {
@@ -108,58 +166,90 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_fp64(int64_t ne, const doub
     const int64_t e0 = (int64_t)blockIdx.x * kElemBlock;
     const int64_t e = e0 + threadIdx.x;
     if (e < ne) {
-        int32_t v[4];
-        const bool ok = load_vertices(t, ne, e, npts, v);
-        double J[9];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const double x0 = p[i * npts + v[0]];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
-        }
-        double b[4][3];
-        b[1][0] = J[4] * J[8] - J[5] * J[7];
-        b[1][1] = J[2] * J[7] - J[1] * J[8];
-        b[1][2] = J[1] * J[5] - J[2] * J[4];
-        b[2][0] = J[5] * J[6] - J[3] * J[8];
-        b[2][1] = J[0] * J[8] - J[2] * J[6];
-        b[2][2] = J[2] * J[3] - J[0] * J[5];
-        b[3][0] = J[3] * J[7] - J[4] * J[6];
-        b[3][1] = J[1] * J[6] - J[0] * J[7];
-        b[3][2] = J[0] * J[4] - J[1] * J[3];
-        const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
-        const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
         double g[16];
-        if (coef_kind == 0) {
-            const double sc = (coef ? coef[e] : 1.0) * inv;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-                for (int l = k; l < 4; ++l) {
-                    const double val = sc * (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]);
-                    g[k * 4 + l] = val;
-                    g[l * 4 + k] = val;
-                }
-        } else {
-            double A[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                double Ab[3];
-#pragma unroll
-                for (int i = 0; i < 3; ++i) Ab[i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) g[k * 4 + l] = inv * (b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2]);
-            }
-        }
+        elem_g_fp64(ne, p, npts, t, coef_kind, coef, e, g);
         double2 *st = reinterpret_cast<double2 *>(stage + threadIdx.x * kStagePad);
 #pragma unroll
         for (int m = 0; m < 8; ++m) st[m] = make_double2(g[2 * m], g[2 * m + 1]);
     }
     flush_stage(stage, G, e0, ne);
+}
+
+// P2 element matrices in FP64 (the FP64 mode on row-grouped patterns): the
+// element pass evaluates K_ab = sum G T over the supports once per entry,
+// the 55 entries of the upper triangle only when the element's coefficient
+// is symmetric to rounding (then K is), and writes the full 10 x 10 matrix; the row
+// pass only adds rows.  This halves the FP64 multiply-adds of the
+// row-by-row evaluation, whose rows a and b each recompute K_ab.
+constexpr int kKeBlock = 128;
+constexpr int kKeChunk = 25;  // entries staged per round; 4 rounds cover the 100
+
+__host__ __device__ constexpr int tri10(int a, int b) {  // packed upper triangle, a <= b
+    return a * 10 - a * (a - 1) / 2 + (b - a);
+}
+
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                           const int32_t *__restrict__ t, int coef_kind,
+                                                           const double *__restrict__ coef,
+                                                           const double *__restrict__ Tg, double *__restrict__ Ke) {
+    __shared__ double Ts[10 * 10 * 4];
+    __shared__ double stage[kKeBlock * kKeChunk];
+    for (int i = threadIdx.x; i < 400; i += blockDim.x) Ts[i] = Tg[i];
+    __syncthreads();
+    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    const bool valid = e < ne;
+    double g[16];
+    bool sym = true;
+    if (valid) {
+        sym = elem_g_fp64(ne, p, npts, t, coef_kind, coef, e, g);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = 0.0;
+    }
+    auto entry = [&](int a, int bb) -> double {
+        const int ka0 = sup_lo(a), ka1 = sup_hi(a), kb0 = sup_lo(bb), kb1 = sup_hi(bb);
+        const double *T = Ts + (a * 10 + bb) * 4;
+        double v = g[ka0 * 4 + kb0] * T[0];
+        if (kb1 != kb0) v += g[ka0 * 4 + kb1] * T[1];
+        if (ka1 != ka0) {
+            v += g[ka1 * 4 + kb0] * T[2];
+            if (kb1 != kb0) v += g[ka1 * 4 + kb1] * T[3];
+        }
+        return v;
+    };
+    double U[55];
+    if (sym) {
+#pragma unroll
+        for (int a = 0; a < 10; ++a)
+#pragma unroll
+            for (int bb = a; bb < 10; ++bb) U[tri10(a, bb)] = entry(a, bb);
+    }
+    const int nvalid = (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock);
+    double *st = stage + threadIdx.x * kKeChunk;
+#pragma unroll
+    for (int r = 0; r < 100 / kKeChunk; ++r) {
+        if (sym) {
+#pragma unroll
+            for (int q = 0; q < kKeChunk; ++q) {
+                const int k = r * kKeChunk + q, a = k / 10, bb = k % 10;
+                st[q] = U[a <= bb ? tri10(a, bb) : tri10(bb, a)];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < kKeChunk; ++q) {
+                const int k = r * kKeChunk + q;
+                st[q] = entry(k / 10, k % 10);
+            }
+        }
+        __syncthreads();
+        // coalesced copy-out: element rows are 100 doubles apart
+        for (int i = threadIdx.x; i < nvalid * kKeChunk; i += kKeBlock) {
+            const int el = i / kKeChunk, q = i - el * kKeChunk;
+            Ke[(e0 + el) * 100 + r * kKeChunk + q] = stage[el * kKeChunk + q];
+        }
+        __syncthreads();
+    }
 }
 
 __device__ __forceinline__ bool df_in_range(df64 x) {
@@ -589,6 +679,91 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
     }
 }
 
+// Row pass over precomputed element matrices (FP64 P2): as k_rows_group,
+// with row a of K_e loaded (10 doubles, the next record's row one step
+// ahead) instead of evaluated.
+template <int SLOTS, int P>
+__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const int2 *__restrict__ groups,
+                                                           const int32_t *__restrict__ indptr,
+                                                           const int32_t *__restrict__ inc_ptr,
+                                                           const int4 *__restrict__ rec, const double *__restrict__ Ke,
+                                                           double *__restrict__ values) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kRowWarps + warp;
+    if (gi >= n_groups) return;
+    double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
+    const int2 grp = groups[gi];
+    const int32_t s0 = indptr[grp.x];
+    const int nslots = indptr[grp.y] - s0;
+    for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.0;
+    __syncwarp();
+    const int ridx = lane / P, part = lane - (lane / P) * P;
+    const int32_t r = grp.x + ridx;
+    if (ridx < 32 / P && r < grp.y) {
+        const int base = indptr[r] - s0 + part * nslots;
+        const int32_t it1 = inc_ptr[r + 1];
+        int32_t it = inc_ptr[r] + part;
+        if (it < it1) {
+            int4 rc = rec[it];
+            double2 cur[5];
+            {
+                const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rc.x * 10);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) cur[q] = __ldg(src + q);
+            }
+            for (; it < it1; it += P) {
+                const bool has_next = it + P < it1;
+                int4 rcn = make_int4(0, 0, 0, 0);
+                double2 nxt[5];
+                if (has_next) {
+                    rcn = rec[it + P];
+                    const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rcn.x * 10);
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) nxt[q] = __ldg(src + q);
+                }
+                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+                int off[10];
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+                double a[10];
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    acc[off[2 * q]] = a[2 * q] + cur[q].x;
+                    acc[off[2 * q + 1]] = a[2 * q + 1] + cur[q].y;
+                }
+                if (has_next) {
+                    rc = rcn;
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) cur[q] = nxt[q];
+                }
+            }
+        }
+    }
+    __syncwarp();
+    for (int j = lane; j < nslots; j += 32) {
+        double v = acc[j];
+#pragma unroll
+        for (int c = 1; c < P; ++c) v += acc[c * nslots + j];
+        values[s0 + j] = v;
+    }
+}
+
+template <int SLOTS, int P>
+void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, const double *Ke, double *values,
+                     cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)kRowWarps * SLOTS * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_rows_ke<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
+    k_rows_ke<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
+                                                           pat->rec.get(), Ke, values);
+    SKG_LAUNCH_CHECK("rows_ke");
+}
+
 // Fallback row pass (patterns without row blocks): thread per row, global
 // accumulation, FP64.
 template <int N>
@@ -731,6 +906,21 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_CUDA(cudaMemcpyAsync(h_misc, misc.get(), sizeof(h_misc), cudaMemcpyDeviceToHost, s));
         SKG_CUDA(cudaStreamSynchronize(s));
         if (h_misc[1] != 0 || h_misc[0] == INT_MIN) mode = MODE_FP64;  // out of FP32 range: FP64 instead
+    }
+    if (mode == MODE_FP64 && nodes == 10 && blocked) {
+        // FP64 P2: element matrices, then row sums
+        DevBuf<double> Ke((size_t)ne * 100, s);
+        if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
+        if (ne) {
+            k_elem_ke_fp64<<<grid_for(ne, kKeBlock), kKeBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
+                                                                       Tg.get(), Ke.get());
+            SKG_LAUNCH_CHECK("elem_ke_fp64");
+        }
+        if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
+        launch_ke_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Ke.get(), d_values, s);
+        launch_ke_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Ke.get(), d_values, s);
+        if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
+        return;
     }
     if (mode == MODE_FP64) {
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));

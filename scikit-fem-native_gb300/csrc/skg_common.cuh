@@ -69,6 +69,24 @@ int guarded(F &&body) {
 
 // ---------------------------------------------------------------- buffers
 
+// Stream-ordered scratch comes from the device's default memory pool.  Its
+// release threshold is raised once per device so that memory freed at the
+// end of one assembly stays reserved for the next (the default threshold
+// returns it to the driver at every synchronisation, and re-mapping
+// gigabytes of scratch per call costs milliseconds).  The pool belongs to
+// this process and ends with it.
+inline void retain_pool_memory() {
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    done[dev] = true;
+}
+
 // Device buffer.  Temporaries are stream-ordered (cudaMallocAsync /
 // cudaFreeAsync on the call's stream); buffers owned by handles, which may
 // outlive the stream that created them, use plain cudaMalloc / cudaFree.
@@ -80,7 +98,10 @@ struct DevBuf {
     bool async = false;
     DevBuf() = default;
     DevBuf(size_t count, cudaStream_t s) : n(count), stream(s), async(true) {
-        if (count) SKG_CUDA(cudaMallocAsync((void **)&ptr, count * sizeof(T), s));
+        if (count) {
+            retain_pool_memory();
+            SKG_CUDA(cudaMallocAsync((void **)&ptr, count * sizeof(T), s));
+        }
     }
     static DevBuf owned(size_t count) {
         DevBuf b;
