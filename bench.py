@@ -222,12 +222,12 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes of one FP64 row pass (64^3) from the committed ncu summary."""
+def profiled_traffic(key):
+    """DRAM bytes of one FP64 pass at 64^3 (element or row pass) from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_affine_fp64_p2_aniso_48.md")
     try:
         for ln in open(path):
-            if ln.startswith("dram_bytes_per_row_pass_full:"):
+            if ln.startswith(f"dram_bytes_per_{key}_pass_full:"):
                 return float(ln.split(":")[1])
     except OSError:
         pass
@@ -332,9 +332,12 @@ def run_gpu(args, rank, world):
     npts_vertex = (args.cells + 1) ** 3
     bytes_elem = 24 * npts_vertex + 16 * E + 72 * E     # vertex coords + 4 vertex ids + A
     bytes_rows = 40 * E + 8 * nnz                       # 10 dof ids per element + CSR values
-    dominant = ("k_rows_group", bytes_rows, t_rows) if t_rows >= t_el else ("k_elem_fp64", bytes_elem, t_el)
-    achieved = dominant[1] / (dominant[2] * 1e-3) / 1e9
-    traffic = profiled_traffic() if dominant[0] == "k_rows_group" and args.cells == N_CELLS else None
+    head_mode = args.modes[0]
+    names = (("k_elem_ke_fp64", "k_rows_ke") if head_mode == "fp64" else ("k_elem_df64", "k_rows_group"))
+    passes = [(names[0], "element", bytes_elem, t_el), (names[1], "row", bytes_rows, t_rows)]
+    dominant = max(passes, key=lambda q: q[3])
+    achieved = dominant[2] / (dominant[3] * 1e-3) / 1e9
+    traffic = (profiled_traffic(dominant[1]) if head_mode == "fp64" and args.cells == N_CELLS else None)
 
     config = dict(CONFIG, cells=args.cells, parallelism=f"replicas x{world}" if world > 1 else "single GPU")
     if args.cells != N_CELLS:
@@ -349,10 +352,14 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": int(8 * nnz), "ms_per_step": 1e3 * e2e_s},
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": dominant[1],
+                     "traffic": traffic, "algorithmic_bytes_per_launch": dominant[2],
+                     "limiter": ("FP64 pipe (ncu: 85% active in the element pass, 53-58% in the row pass)"
+                                 if head_mode == "fp64" else "CUDA-core issue / shared-memory latency"),
+                     "passes": {q[0]: {"ms": q[3], "algorithmic_bytes": q[2],
+                                       "achieved_gbs": q[2] / (q[3] * 1e-3) / 1e9} for q in passes},
                      "whole_assembly_hbm_frac": (bytes_elem + bytes_rows) / ((t_el + t_rows) * 1e-3) / 1e9 / peak},
         "precision_variants": results,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # element pass + one row pass per group class
         "clocks": head["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
