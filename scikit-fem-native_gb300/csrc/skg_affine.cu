@@ -279,6 +279,84 @@ __global__ void k_scale(const double *__restrict__ p, int64_t n, int *__restrict
 }
 
 // Element pass in double-float.  G (scaled by 2^-s) as 16 df64.
+// G (scaled by 2^-s, and by 1/30 for the exact-rule P2 path) in double-float
+// for element e; `ok` false when a value leaves the FP32 range.  Returns the
+// coefficient's symmetry (to 1e-14 of its size, as elem_g_fp64).
+__device__ __forceinline__ bool elem_g_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                            const int32_t *__restrict__ t, int coef_kind,
+                                            const double *__restrict__ coef, int s, bool div30, int64_t e,
+                                            df64 g[16], bool &ok) {
+    int32_t v[4];
+    ok = load_vertices(t, ne, e, npts, v);
+    df64 J[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double x0 = p[i * npts + v[0]];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) J[i * 3 + r] = df_from_double(p[i * npts + v[r + 1]] - x0, -s, ok);
+    }
+    df64 b[4][3];
+#define SKG_CROSS(a, bb, c, d) df_add_fast(df_mul(J[a], J[bb]), df_neg(df_mul(J[c], J[d])))
+    b[1][0] = SKG_CROSS(4, 8, 5, 7);
+    b[1][1] = SKG_CROSS(2, 7, 1, 8);
+    b[1][2] = SKG_CROSS(1, 5, 2, 4);
+    b[2][0] = SKG_CROSS(5, 6, 3, 8);
+    b[2][1] = SKG_CROSS(0, 8, 2, 6);
+    b[2][2] = SKG_CROSS(2, 3, 0, 5);
+    b[3][0] = SKG_CROSS(3, 7, 4, 6);
+    b[3][1] = SKG_CROSS(1, 6, 0, 7);
+    b[3][2] = SKG_CROSS(0, 4, 1, 3);
+#undef SKG_CROSS
+    df64 det = df_add_fast(df_add_fast(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add_fast(df_add_fast(b[1][i], b[2][i]), b[3][i]));
+    if (det.hi < 0.f) det = df_neg(det);
+    ok = ok && det.hi > 1e-30f;
+    df64 inv = df_recip(det);
+    // exact-rule P2 path: G / 30 (the integer table carries 30 T)
+    if (div30) inv = df_mul(inv, df64{0x1.111112p-5f, -0x1.dddddep-30f});
+    if (coef_kind == 0) {
+        df64 sc = inv;
+        if (coef) sc = df_mul(sc, df_from_double(coef[e], 0, ok));
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int l = k; l < 4; ++l) {
+                df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])),
+                                     df_mul(b[k][2], b[l][2]));
+                d = df_mul(sc, d);
+                ok = ok && df_in_range(d);
+                g[k * 4 + l] = d;
+                g[l * 4 + k] = d;
+            }
+        return true;
+    }
+    double Ad[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Ad[k] = load_coef(coef, coef_kind, ne, e, k);
+    df64 A[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) A[k] = df_from_double(Ad[k], 0, ok);
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        df64 Ab[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            Ab[i] = df_add_fast(df_add_fast(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
+                                df_mul(A[i * 3 + 2], b[l][2]));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], Ab[0]), df_mul(b[k][1], Ab[1])), df_mul(b[k][2], Ab[2]));
+            d = df_mul(inv, d);
+            ok = ok && df_in_range(d);
+            g[k * 4 + l] = d;
+        }
+    }
+    const double scale =
+        1e-14 * (fabs(Ad[0]) + fabs(Ad[4]) + fabs(Ad[8]) + fabs(Ad[1]) + fabs(Ad[2]) + fabs(Ad[5]));
+    return fabs(Ad[1] - Ad[3]) <= scale && fabs(Ad[2] - Ad[6]) <= scale && fabs(Ad[5] - Ad[7]) <= scale;
+}
+
 __global__ void __launch_bounds__(kElemBlock, 6) k_elem_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                                              const int32_t *__restrict__ t, int coef_kind,
                                                              const double *__restrict__ coef,
@@ -288,72 +366,12 @@ __global__ void __launch_bounds__(kElemBlock, 6) k_elem_df64(int64_t ne, const d
     const int64_t e0 = (int64_t)blockIdx.x * kElemBlock;
     const int64_t e = e0 + threadIdx.x;
     if (e < ne) {
-        const int s = *s_ptr;
-        int32_t v[4];
-        bool ok = load_vertices(t, ne, e, npts, v);
-        df64 J[9];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const double x0 = p[i * npts + v[0]];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) J[i * 3 + r] = df_from_double(p[i * npts + v[r + 1]] - x0, -s, ok);
-        }
-        df64 b[4][3];
-#define SKG_CROSS(a, bb, c, d) df_add_fast(df_mul(J[a], J[bb]), df_neg(df_mul(J[c], J[d])))
-        b[1][0] = SKG_CROSS(4, 8, 5, 7);
-        b[1][1] = SKG_CROSS(2, 7, 1, 8);
-        b[1][2] = SKG_CROSS(1, 5, 2, 4);
-        b[2][0] = SKG_CROSS(5, 6, 3, 8);
-        b[2][1] = SKG_CROSS(0, 8, 2, 6);
-        b[2][2] = SKG_CROSS(2, 3, 0, 5);
-        b[3][0] = SKG_CROSS(3, 7, 4, 6);
-        b[3][1] = SKG_CROSS(1, 6, 0, 7);
-        b[3][2] = SKG_CROSS(0, 4, 1, 3);
-#undef SKG_CROSS
-        df64 det = df_add_fast(df_add_fast(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
-#pragma unroll
-        for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add_fast(df_add_fast(b[1][i], b[2][i]), b[3][i]));
-        if (det.hi < 0.f) det = df_neg(det);
-        ok = ok && det.hi > 1e-30f;
-        df64 inv = df_recip(det);
-        // exact-rule P2 path: store G / 30 (the row pass multiplies by 30 T)
-        if (div30) inv = df_mul(inv, df64{0x1.111112p-5f, -0x1.dddddep-30f});
+        df64 g[16];
+        bool ok;
+        elem_g_df64(ne, p, npts, t, coef_kind, coef, *s_ptr, div30, e, g, ok);
         float2 *st = reinterpret_cast<float2 *>(stage + threadIdx.x * kStagePad);
-        if (coef_kind == 0) {
-            df64 sc = inv;
-            if (coef) sc = df_mul(sc, df_from_double(coef[e], 0, ok));
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-                for (int l = k; l < 4; ++l) {
-                    df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])),
-                                         df_mul(b[k][2], b[l][2]));
-                    d = df_mul(sc, d);
-                    ok = ok && df_in_range(d);
-                    st[k * 4 + l] = make_float2(d.hi, d.lo);
-                    st[l * 4 + k] = make_float2(d.hi, d.lo);
-                }
-        } else {
-            df64 A[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) A[k] = df_from_double(load_coef(coef, coef_kind, ne, e, k), 0, ok);
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                df64 Ab[3];
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-                    Ab[i] = df_add_fast(df_add_fast(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
-                                        df_mul(A[i * 3 + 2], b[l][2]));
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], Ab[0]), df_mul(b[k][1], Ab[1])),
-                                         df_mul(b[k][2], Ab[2]));
-                    d = df_mul(inv, d);
-                    ok = ok && df_in_range(d);
-                    st[k * 4 + l] = make_float2(d.hi, d.lo);
-                }
-            }
-        }
+        for (int k = 0; k < 16; ++k) st[k] = make_float2(g[k].hi, g[k].lo);
         if (!ok) atomicExch(range_flag, 1);
     }
     flush_stage(stage, G, e0, ne);
@@ -764,6 +782,174 @@ void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, c
     SKG_LAUNCH_CHECK("rows_ke");
 }
 
+// ------------------------------------------- element matrices, double-float
+// The double-float mode of P2 with an exact rule: the element pass evaluates
+// K_ab = sum t30 G/30 (integer factors, double-float G) once per entry (upper
+// triangle for a symmetric coefficient) and stores the 10 x 10 matrix as FP32
+// (hi, lo) pairs; the row pass adds rows into double-float slots.
+
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+template <int A, int BB, int MODE>
+__device__ __forceinline__ df64 exact_entry(const df64 g[16]) {
+    constexpr int ka0 = sup_lo(A), ka1 = sup_hi(A), kb0 = sup_lo(BB), kb1 = sup_hi(BB);
+    float S = 0.f, L = 0.f;
+    sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 0, 0)>(g[ka0 * 4 + kb0]));
+    if constexpr (kb1 != kb0) sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 0, 1)>(g[ka0 * 4 + kb1]));
+    if constexpr (ka1 != ka0) {
+        sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 1, 0)>(g[ka1 * 4 + kb0]));
+        if constexpr (kb1 != kb0) sum_term<MODE>(S, L, df_mul_int<t30(A, BB, 1, 1)>(g[ka1 * 4 + kb1]));
+    }
+    return fast_two_sum(S, L);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                           const int32_t *__restrict__ t, int coef_kind,
+                                                           const double *__restrict__ coef,
+                                                           const int *__restrict__ s_ptr, float2 *__restrict__ Ke,
+                                                           int *__restrict__ range_flag) {
+    __shared__ float2 stage[kKeBlock * kKeChunk];
+    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    const bool valid = e < ne;
+    df64 g[16];
+    bool ok = true, sym = true;
+    if (valid) {
+        sym = elem_g_df64(ne, p, npts, t, coef_kind, coef, *s_ptr, true, e, g, ok);
+        if (!ok) atomicExch(range_flag, 1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = df64{0.f, 0.f};
+    }
+    df64 U[55];
+    if (sym) {
+        static_for<0, 100>([&](auto kk) {
+            constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+            if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry<A, BB, MODE>(g);
+        });
+    }
+    const int nvalid = (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock);
+    float2 *st = stage + threadIdx.x * kKeChunk;
+    static_for<0, 100 / kKeChunk>([&](auto rr) {
+        constexpr int r = decltype(rr)::value;
+        if (sym) {
+            static_for<0, kKeChunk>([&](auto qq) {
+                constexpr int q = decltype(qq)::value, k = r * kKeChunk + q, A = k / 10, BB = k % 10;
+                const df64 v = U[A <= BB ? tri10(A, BB) : tri10(BB, A)];
+                st[q] = make_float2(v.hi, v.lo);
+            });
+        } else {
+            static_for<0, kKeChunk>([&](auto qq) {
+                constexpr int q = decltype(qq)::value, k = r * kKeChunk + q;
+                const df64 v = exact_entry<k / 10, k % 10, MODE>(g);
+                st[q] = make_float2(v.hi, v.lo);
+            });
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nvalid * kKeChunk; i += kKeBlock) {
+            const int el = i / kKeChunk, q = i - el * kKeChunk;
+            Ke[(e0 + el) * 100 + r * kKeChunk + q] = stage[el * kKeChunk + q];
+        }
+        __syncthreads();
+    });
+}
+
+// Row pass over double-float element matrices: rows of 10 (hi, lo) pairs added
+// into double-float slots, converted to FP64 at write-out.
+template <int SLOTS, int P>
+__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, const int2 *__restrict__ groups,
+                                                              const int32_t *__restrict__ indptr,
+                                                              const int32_t *__restrict__ inc_ptr,
+                                                              const int4 *__restrict__ rec,
+                                                              const float2 *__restrict__ Ke,
+                                                              const int *__restrict__ s_ptr,
+                                                              double *__restrict__ values) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kRowWarps + warp;
+    if (gi >= n_groups) return;
+    df64 *acc = reinterpret_cast<df64 *>(smem + (size_t)warp * SLOTS * 8);
+    const int2 grp = groups[gi];
+    const int32_t s0 = indptr[grp.x];
+    const int nslots = indptr[grp.y] - s0;
+    for (int j = lane; j < P * nslots; j += 32) acc[j] = df64{0.f, 0.f};
+    __syncwarp();
+    const int ridx = lane / P, part = lane - (lane / P) * P;
+    const int32_t r = grp.x + ridx;
+    if (ridx < 32 / P && r < grp.y) {
+        const int base = indptr[r] - s0 + part * nslots;
+        const int32_t it1 = inc_ptr[r + 1];
+        int32_t it = inc_ptr[r] + part;
+        if (it < it1) {
+            int4 rc = rec[it];
+            float4 cur[5];
+            {
+                const float4 *src = reinterpret_cast<const float4 *>(Ke + (int64_t)rc.x * 10);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) cur[q] = __ldg(src + q);
+            }
+            for (; it < it1; it += P) {
+                const bool has_next = it + P < it1;
+                int4 rcn = make_int4(0, 0, 0, 0);
+                float4 nxt[5];
+                if (has_next) {
+                    rcn = rec[it + P];
+                    const float4 *src = reinterpret_cast<const float4 *>(Ke + (int64_t)rcn.x * 10);
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) nxt[q] = __ldg(src + q);
+                }
+                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+                int off[10];
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+                df64 a[10];
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    df_acc(a[2 * q], df64{cur[q].x, cur[q].y});
+                    df_acc(a[2 * q + 1], df64{cur[q].z, cur[q].w});
+                }
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) acc[off[bb]] = a[bb];
+                if (has_next) {
+                    rc = rcn;
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) cur[q] = nxt[q];
+                }
+            }
+        }
+    }
+    __syncwarp();
+    const int sc = *s_ptr;
+    for (int j = lane; j < nslots; j += 32) {
+        df64 v = fast_two_sum(acc[j].hi, acc[j].lo);
+#pragma unroll
+        for (int c = 1; c < P; ++c) v = df_add(v, fast_two_sum(acc[c * nslots + j].hi, acc[c * nslots + j].lo));
+        values[s0 + j] = df_to_double(v, sc);
+    }
+}
+
+template <int SLOTS, int P>
+void launch_ke_df_class(int n_groups, const int2 *groups, const skg_pattern *pat, const float2 *Ke, const int *s_ptr,
+                        double *values, cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)kRowWarps * SLOTS * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_rows_ke_df<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
+    k_rows_ke_df<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
+                                                              pat->rec.get(), Ke, s_ptr, values);
+    SKG_LAUNCH_CHECK("rows_ke_df");
+}
+
 // Fallback row pass (patterns without row blocks): thread per row, global
 // accumulation, FP64.
 template <int N>
@@ -890,6 +1076,34 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     int mode = precision == SKG_FP64 ? MODE_FP64 : precision == SKG_SPLIT_FP32 ? MODE_SPLIT : MODE_DF64;
     if (!blocked) mode = MODE_FP64;
     DevBuf<int> misc(2, s);  // [0] scale exponent, [1] range flag
+    if (mode == MODE_DF64 && exact) {
+        // P2, exact rule, double-float: element matrices, then row sums (the
+        // split mode keeps the row-by-row evaluation, which is faster there)
+        const int init[2] = {INT_MIN, 0};
+        SKG_CUDA(cudaMemcpyAsync(misc.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+        k_scale<<<2 * kSmCount, 256, 0, s>>>(d_p, 3 * npts, misc.get());
+        SKG_LAUNCH_CHECK("scale");
+        DevBuf<float2> Kf((size_t)ne * 100, s);
+        if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
+        if (ne) {
+            k_elem_ke_df64<MODE_DF64><<<grid_for(ne, kKeBlock), kKeBlock, 0, s>>>(
+                ne, d_p, npts, d_t, coef_kind, d_coef, misc.get(), Kf.get(), misc.get() + 1);
+            SKG_LAUNCH_CHECK("elem_ke_df64");
+        }
+        int h_misc[2];
+        SKG_CUDA(cudaMemcpyAsync(h_misc, misc.get(), sizeof(h_misc), cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        if (h_misc[1] == 0 && h_misc[0] != INT_MIN) {
+            if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
+            launch_ke_df_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Kf.get(),
+                                                    misc.get(), d_values, s);
+            launch_ke_df_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Kf.get(),
+                                                    misc.get(), d_values, s);
+            if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
+            return;
+        }
+        mode = MODE_FP64;  // out of FP32 range: FP64 instead
+    }
     if (mode != MODE_FP64) {
         const int init[2] = {INT_MIN, 0};
         SKG_CUDA(cudaMemcpyAsync(misc.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
