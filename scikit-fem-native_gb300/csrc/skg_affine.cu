@@ -48,6 +48,7 @@
 
 #include "skg_common.cuh"
 #include "skg_df64.cuh"
+#include "skg_rows.cuh"
 
 namespace skg {
 namespace {
@@ -388,7 +389,6 @@ __device__ __forceinline__ void df_acc(df64 &a, df64 v) {
     a.lo += sm.lo + v.lo;
 }
 
-constexpr int kRowWarps = 4;  // warps per CTA in the row pass
 
 // Barycentric-support rows of G needed by local row a: g0 = G[ka0][:],
 // g1 = G[ka1][:] (zero for a single-vertex support).
@@ -695,91 +695,6 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
             values[s0 + j] = df_to_double(v, sc);
         }
     }
-}
-
-// Row pass over precomputed element matrices (FP64 P2): as k_rows_group,
-// with row a of K_e loaded (10 doubles, the next record's row one step
-// ahead) instead of evaluated.
-template <int SLOTS, int P>
-__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const int2 *__restrict__ groups,
-                                                           const int32_t *__restrict__ indptr,
-                                                           const int32_t *__restrict__ inc_ptr,
-                                                           const int4 *__restrict__ rec, const double *__restrict__ Ke,
-                                                           double *__restrict__ values) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gi = blockIdx.x * kRowWarps + warp;
-    if (gi >= n_groups) return;
-    double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
-    const int2 grp = groups[gi];
-    const int32_t s0 = indptr[grp.x];
-    const int nslots = indptr[grp.y] - s0;
-    for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.0;
-    __syncwarp();
-    const int ridx = lane / P, part = lane - (lane / P) * P;
-    const int32_t r = grp.x + ridx;
-    if (ridx < 32 / P && r < grp.y) {
-        const int base = indptr[r] - s0 + part * nslots;
-        const int32_t it1 = inc_ptr[r + 1];
-        int32_t it = inc_ptr[r] + part;
-        if (it < it1) {
-            int4 rc = rec[it];
-            double2 cur[5];
-            {
-                const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rc.x * 10);
-#pragma unroll
-                for (int q = 0; q < 5; ++q) cur[q] = __ldg(src + q);
-            }
-            for (; it < it1; it += P) {
-                const bool has_next = it + P < it1;
-                int4 rcn = make_int4(0, 0, 0, 0);
-                double2 nxt[5];
-                if (has_next) {
-                    rcn = rec[it + P];
-                    const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rcn.x * 10);
-#pragma unroll
-                    for (int q = 0; q < 5; ++q) nxt[q] = __ldg(src + q);
-                }
-                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
-                int off[10];
-#pragma unroll
-                for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                double a[10];
-#pragma unroll
-                for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
-#pragma unroll
-                for (int q = 0; q < 5; ++q) {
-                    acc[off[2 * q]] = a[2 * q] + cur[q].x;
-                    acc[off[2 * q + 1]] = a[2 * q + 1] + cur[q].y;
-                }
-                if (has_next) {
-                    rc = rcn;
-#pragma unroll
-                    for (int q = 0; q < 5; ++q) cur[q] = nxt[q];
-                }
-            }
-        }
-    }
-    __syncwarp();
-    for (int j = lane; j < nslots; j += 32) {
-        double v = acc[j];
-#pragma unroll
-        for (int c = 1; c < P; ++c) v += acc[c * nslots + j];
-        values[s0 + j] = v;
-    }
-}
-
-template <int SLOTS, int P>
-void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, const double *Ke, double *values,
-                     cudaStream_t s) {
-    if (n_groups == 0) return;
-    const size_t smem = (size_t)kRowWarps * SLOTS * 8;
-    if (smem > 48 * 1024)
-        SKG_CUDA(cudaFuncSetAttribute(k_rows_ke<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
-    k_rows_ke<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
-                                                           pat->rec.get(), Ke, values);
-    SKG_LAUNCH_CHECK("rows_ke");
 }
 
 // ------------------------------------------- element matrices, double-float
@@ -1131,8 +1046,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             SKG_LAUNCH_CHECK("elem_ke_fp64");
         }
         if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-        launch_ke_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Ke.get(), d_values, s);
-        launch_ke_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Ke.get(), d_values, s);
+        add_element_rows<10>(pat, Ke.get(), d_values, s);
         if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
         return;
     }

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "skg_common.cuh"
+#include "skg_rows.cuh"
 
 namespace skg {
 
@@ -116,6 +117,16 @@ __global__ void k_gather_rows(int64_t n_rows, const int32_t *__restrict__ indptr
 // Fixed-order gather of element matrices (E, Lr, Lc) into the pattern's CSR values.
 void gather_element_matrices(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
     if (!pat->n_rows) return;
+    if (pat->max_row_len > 0 && pat->row_local == pat->col_local) {
+        // row groups: shared-memory slot sums, each value written once
+        switch (pat->row_local) {
+            case 4: add_element_rows<4>(pat, Ke, values, s); return;
+            case 6: add_element_rows<6>(pat, Ke, values, s); return;
+            case 10: add_element_rows<10>(pat, Ke, values, s); return;
+            case 12: add_element_rows<12>(pat, Ke, values, s); return;
+            default: break;
+        }
+    }
     k_gather_rows<<<grid_for(pat->n_rows, 128), 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
                                                              pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(),
                                                              pat->row_local, pat->col_local, Ke, values);

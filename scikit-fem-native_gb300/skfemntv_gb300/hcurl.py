@@ -167,8 +167,11 @@ class TetN1Assembler:
         return None, dev.to_device(per_point(value, E, Q, name), np.float64)
 
     def assemble_device(self, *, mass_coefficient=None, curl_coefficient=None, include_mass=True,
-                        include_curl=True, precision="fp64"):
+                        include_curl=True, precision="fp64", _out=None):
+        """Assemble into the device values (or, with ``_out``, into the host
+        matrix's page-locked buffer); returns the device values tensor."""
         b = self.basis
+        out = _out if _out is not None else dev.ptr(self.target.d_values)
         E = b.mesh.nelements
         Q = len(b.W)
         prec = _precision(precision)
@@ -178,7 +181,7 @@ class TetN1Assembler:
             call("skg_n1_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
                  dev.ptr(b._t4), dev.ptr(b._ee_dev), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W),
                  dev.ptr(m_el), dev.ptr(c_el), int(include_mass), int(include_curl), prec,
-                 dev.ptr(self.target.d_values), dev.stream_ptr())
+                 out, dev.stream_ptr())
         else:
             if prec != SKG_FP64:
                 from .errors import UnsupportedNativeForm
@@ -191,19 +194,22 @@ class TetN1Assembler:
                 ones if c_el is None else dev.to_device(np.repeat(c_el.cpu().numpy()[:, None], Q, 1), np.float64))
             call("skg_n1_assemble_pointwise", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
                  dev.ptr(b._t4), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W), dev.ptr(mp),
-                 dev.ptr(cp), int(include_mass), int(include_curl), dev.ptr(self.target.d_values),
+                 dev.ptr(cp), int(include_mass), int(include_curl), out,
                  dev.stream_ptr())
         return self.target.d_values
 
+    def _host(self, **kw):
+        """Host matrix: values written straight into its page-locked buffer when
+        the device can write host memory (row-grouped pattern), else copied."""
+        out = self.target.host_out()
+        self.assemble_device(_out=out, **kw)
+        return self.target.finish_direct() if out is not None else self.target.download()
+
     def assemble_maxwell(self, *, mass_coefficient=None, curl_coefficient=None, precision="fp64"):
-        self.assemble_device(mass_coefficient=mass_coefficient, curl_coefficient=curl_coefficient,
-                             precision=precision)
-        return self.target.download()
+        return self._host(mass_coefficient=mass_coefficient, curl_coefficient=curl_coefficient, precision=precision)
 
     def assemble_mass(self, coefficient=None, precision="fp64"):
-        self.assemble_device(mass_coefficient=coefficient, include_curl=False, precision=precision)
-        return self.target.download()
+        return self._host(mass_coefficient=coefficient, include_curl=False, precision=precision)
 
     def assemble_curl_curl(self, coefficient=None, precision="fp64"):
-        self.assemble_device(curl_coefficient=coefficient, include_mass=False, precision=precision)
-        return self.target.download()
+        return self._host(curl_coefficient=coefficient, include_mass=False, precision=precision)
