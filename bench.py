@@ -528,6 +528,15 @@ def wl_n1_maxwell(args, world, timed, wall):
              1, 1, 0, dev.ptr(asmb.target.d_values), dev.stream_ptr())
 
     ms, clk = timed(step)
+    ref = asmb.target.d_values[:nnz].clone()
+
+    def step_split():
+        call("skg_n1_assemble", asmb.pattern.h, dev.ptr(nb.mesh._dev("p")), nb.mesh.p.shape[1], dev.ptr(nb._t4),
+             dev.ptr(nb._ee_dev), dev.ptr(nb._signs_dev), E, Q, dev.hptr(nb.X), dev.hptr(nb.W), None, dev.ptr(dnu),
+             1, 1, 1, dev.ptr(asmb.target.d_values), dev.stream_ptr())
+
+    ms_s, clk_s = timed(step_split)
+    err_s = _relerr(asmb.target.d_values[:nnz], ref)
     curl = (1.0 / mu)[:, None]
     e2e_s = wall(lambda: asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=curl))
     alg = 24 * mesh.p.shape[1] + 16 * E + 24 * E + 8 * E + 8 * nnz
@@ -539,7 +548,11 @@ def wl_n1_maxwell(args, world, timed, wall):
                 "elements": E, "dofs": nb.N, "nnz": nnz, "l2": "inputs larger than L2"},
         e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 8 * E,
              "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
-        roofline=_roofline(alg, ms), gpu_launches=2 * args.steps)
+        roofline=_roofline(alg, ms),
+        precision_variants={"fp64": {"value": world * nnz / (ms * 1e-3), "ms_per_step": ms},
+                            "split_fp32": {"value": world * nnz / (ms_s * 1e-3), "ms_per_step": ms_s,
+                                           "max_rel_err_vs_fp64": err_s, "clocks": clk_s}},
+        gpu_launches=3 * args.steps)
 
 
 def wl_p1_adjoint(args, world, timed, wall):

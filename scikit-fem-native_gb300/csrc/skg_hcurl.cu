@@ -141,9 +141,140 @@ __device__ __forceinline__ void n1_geometry(const double *__restrict__ p, int64_
 // Reference curls c_a = 2 ghat_i x ghat_j for the directed local edges.
 __constant__ double kRefCurl[6][3] = {{0, -2, 2}, {0, 0, 2}, {-2, 0, 2}, {-2, 2, 0}, {0, -2, 0}, {2, 0, 0}};
 
+// Local edges (i, j) and the reference curls c_a = 2 ghat_i x ghat_j as
+// compile-time functions (the fully unrolled element kernel folds them).
+__host__ __device__ constexpr int edge_v(int a, int k) {
+    return k == 0 ? (a == 0 ? 0 : a == 1 ? 1 : a == 2 ? 2 : a == 3 ? 0 : a == 4 ? 1 : 2)
+                  : (a == 0 ? 1 : a == 1 ? 2 : a == 2 ? 0 : 3);
+}
+__host__ __device__ constexpr double ref_curl(int a, int i) {
+    constexpr double c[6][3] = {{0, -2, 2}, {0, 0, 2}, {-2, 0, 2}, {-2, 2, 0}, {0, -2, 0}, {2, 0, 0}};
+    return c[a][i];
+}
+
+constexpr int kN1Block = 128;
+
+// Per-element coefficients, closed form: K_ac = s_a s_c (mu sum_uv G T + nu
+// (J c_a . J c_c) wsum / |det|) with G = b_k . b_l / |det|; the 21 entries of
+// the symmetric 6 x 6 matrix, stores staged through shared memory.  SPLIT: G,
+// J c and the table in FP64, converted to FP32 (hi, lo) pairs, the entries
+// contracted in FP32 with split products (hi hi + hi lo + lo hi) and FP32
+// accumulation; FP64 keeps the geometry and the CSR slot sums.
+template <bool SPLIT>
+__global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                            const int32_t *__restrict__ t,
+                                                            const int8_t *__restrict__ signs, N1Table tab,
+                                                            const double *__restrict__ mass,
+                                                            const double *__restrict__ curl, int inc_mass,
+                                                            int inc_curl, double *__restrict__ Ke) {
+    __shared__ double stage[kN1Block * 37];
+    const int64_t e0 = (int64_t)blockIdx.x * kN1Block;
+    const int64_t e = e0 + threadIdx.x;
+    if (e < ne) {
+        double J[9], b[4][3], det;
+        n1_geometry(p, npts, t, ne, e, J, b, det);
+        const double inv = 1.0 / fabs(det);
+        double Gm[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int l = k; l < 4; ++l) {
+                Gm[k][l] = (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]) * inv;
+                Gm[l][k] = Gm[k][l];
+            }
+        double Jc[6][3];
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                double v = 0.0;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    if (ref_curl(a, r) != 0.0) v += J[i * 3 + r] * ref_curl(a, r);
+                Jc[a][i] = v;
+            }
+        const double mu = inc_mass ? (mass ? mass[e] : 1.0) : 0.0;
+        const double nu = inc_curl ? (curl ? curl[e] : 1.0) * inv * tab.wsum : 0.0;
+        float sg[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) sg[a] = (float)signs[a * ne + e];
+        double *st = stage + threadIdx.x * 37;
+        if constexpr (!SPLIT) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int c = a; c < 6; ++c) {
+                    double m = 0.0;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+#pragma unroll
+                        for (int v = 0; v < 2; ++v) m += Gm[edge_v(a, u)][edge_v(c, v)] * tab.Tm[a][c][u * 2 + v];
+                    const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
+                    const double val = (double)(sg[a] * sg[c]) * (mu * m + nu * cc);
+                    st[a * 6 + c] = val;
+                    st[c * 6 + a] = val;
+                }
+        } else {
+            float2 G2[4][4], C2[6][3];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const float h = (float)Gm[k][l];
+                    G2[k][l] = make_float2(h, (float)(Gm[k][l] - (double)h));
+                }
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float h = (float)Jc[a][i];
+                    C2[a][i] = make_float2(h, (float)(Jc[a][i] - (double)h));
+                }
+            const float muh = (float)mu, mul = (float)(mu - (double)muh);
+            const float nuh = (float)nu, nul = (float)(nu - (double)nuh);
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int c = a; c < 6; ++c) {
+                    float mh = 0.f, ml = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+#pragma unroll
+                        for (int v = 0; v < 2; ++v) {
+                            const float2 g = G2[edge_v(a, u)][edge_v(c, v)];
+                            const double td = tab.Tm[a][c][u * 2 + v];
+                            const float th = (float)td, tl = (float)(td - (double)th);
+                            const float ph = g.x * th;
+                            mh += ph;
+                            ml += fmaf(g.x, th, -ph) + fmaf(g.x, tl, g.y * th);
+                        }
+                    float ch = 0.f, cl = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        const float2 x = C2[a][i], y = C2[c][i];
+                        const float ph = x.x * y.x;
+                        ch += ph;
+                        cl += fmaf(x.x, y.x, -ph) + fmaf(x.x, y.y, x.y * y.x);
+                    }
+                    const float m = mh + ml, cc = ch + cl;
+                    const float vh = muh * m + nuh * cc;
+                    const float vl = fmaf(muh, m, -muh * m) + fmaf(nuh, cc, -nuh * cc) + mul * m + nul * cc;
+                    const double val = (double)(sg[a] * sg[c]) * ((double)vh + (double)vl);
+                    st[a * 6 + c] = val;
+                    st[c * 6 + a] = val;
+                }
+        }
+    }
+    __syncthreads();
+    const int nvalid = (int)(ne - e0 < kN1Block ? ne - e0 : kN1Block);
+    for (int i = threadIdx.x; i < nvalid * 36; i += kN1Block) {
+        const int el = i / 36, q = i - el * 36;
+        Ke[(e0 + el) * 36 + q] = stage[el * 37 + q];
+    }
+}
+
 // Thread per element: Ke (E, 6, 6).  mass/curl: per element (qstride 0) or
 // per point (qstride 1, explicit quadrature loop); NULL = 1.
-template <bool SPLIT>
 __global__ void k_n1_element(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
                              const int8_t *__restrict__ signs, int nq, const double *__restrict__ Xq,
                              const double *__restrict__ Wq, N1Table tab, const double *__restrict__ mass,
@@ -296,13 +427,11 @@ extern "C" int skg_n1_assemble(const skg_pattern *pat, const double *d_p, int64_
         DevBuf<double> Ke((size_t)ne * 36, s);
         if (ne) {
             if (precision == SKG_SPLIT_FP32)
-                k_n1_element<true><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, nullptr, nullptr,
-                                                                    tab, d_mass, d_curl, 0, include_mass, include_curl,
-                                                                    Ke.get());
+                k_n1_elem_fast<true><<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(
+                    ne, d_p, npts, d_t, d_signs, tab, d_mass, d_curl, include_mass, include_curl, Ke.get());
             else
-                k_n1_element<false><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, nullptr,
-                                                                     nullptr, tab, d_mass, d_curl, 0, include_mass,
-                                                                     include_curl, Ke.get());
+                k_n1_elem_fast<false><<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(
+                    ne, d_p, npts, d_t, d_signs, tab, d_mass, d_curl, include_mass, include_curl, Ke.get());
             SKG_LAUNCH_CHECK("n1_element");
         }
         gather_element_matrices(pat, Ke.get(), d_values, s);
@@ -329,7 +458,7 @@ extern "C" int skg_n1_assemble_pointwise(const skg_pattern *pat, const double *d
         SKG_CUDA(cudaMemcpyAsync(dxw.get(), xw.data(), xw.size() * 8, cudaMemcpyHostToDevice, s));
         DevBuf<double> Ke((size_t)ne * 36, s);
         if (ne) {
-            k_n1_element<false><<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, dxw.get(),
+            k_n1_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, dxw.get(),
                                                                  dxw.get() + 3 * nq, tab, d_mass, d_curl, 1,
                                                                  include_mass, include_curl, Ke.get());
             SKG_LAUNCH_CHECK("n1_element_pointwise");

@@ -201,6 +201,18 @@ def test_n1_maxwell():
     assert relerr(Kp.data, g["data"]) < RTOL
 
 
+def test_n1_split_precision_error_bound():
+    """Split-FP32 element contraction (FP64 geometry and slot sums): <= 1e-7
+    relative to the reference's FP64 matrix."""
+    g = load_golden("n1_maxwell")
+    nb = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]))
+    asmb = sk.TetN1Assembler(nb)
+    K = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=(1.0 / g["mu"])[:, None], precision="split_fp32")
+    same_pattern(K, g)
+    err = relerr(K.data, g["data"])
+    assert 0 < err < 1e-7
+
+
 def test_n1_mass_and_curl_separately():
     g = load_golden("n1_maxwell")
     nb = O.make_n1_basis(g["p"], g["t"])
