@@ -254,6 +254,14 @@ int skg_n1_assemble_pointwise(const skg_pattern *pattern, const double *d_p,
                               const double *h_W, const double *d_mass,
                               const double *d_curl, int32_t include_mass,
                               int32_t include_curl, double *d_values, void *stream);
+/* N1 vector load r = int f . phi (TetN1LinearAssembler.assemble_vector_load,
+ * hcurl_assembler.py:218-246): f (3, E, Q) at the rule's points; pattern:
+ * element edge DOFs (E, 6), incidence only; d_out (N), summed per DOF in
+ * element order. */
+int skg_n1_vector_load(const skg_pattern *pattern, const double *d_p, int64_t npts,
+                       const int32_t *d_t, const int8_t *d_signs, int64_t n_elements,
+                       int32_t nq, const double *h_X, const double *h_W,
+                       const double *d_f, double *d_out, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Linear forms.  Replaces LinearFormAssembler.assemble                 */

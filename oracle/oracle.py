@@ -500,6 +500,24 @@ def n1_assemble_maxwell(b: OracleN1Basis, mass_coefficient=None, curl_coefficien
     return data, indptr, indices
 
 
+def n1_vector_load(b: OracleN1Basis, f):
+    """TetN1LinearAssembler.assemble_vector_load (hcurl_assembler.py:218-246):
+    local_eb = sum_iq phi_ebiq f_ieq dx_eq, summed into the edge DOFs in
+    (element, local edge) order."""
+    f = np.broadcast_to(np.asarray(f, dtype=np.float64), (3,) + b.dx.shape)
+    local = np.einsum("ebiq,ieq,eq->eb", b.values, f, b.dx)
+    out = np.zeros(b.N)
+    np.add.at(out, b.element_dofs.T.ravel(), local.ravel())
+    return out
+
+
+def n1_global_coordinates(p, t, X):
+    """Physical quadrature points (3, E, Q) of the affine map (hcurl_basis.py:435-440)."""
+    v = p[:, t[:4]]
+    J = np.stack([v[:, k] - v[:, 0] for k in (1, 2, 3)], axis=1)  # (3, 3, E): [i, r, e]
+    return v[:, 0][:, :, None] + np.einsum("ire,rq->ieq", J, X)
+
+
 # --------------------------------------------------------------------------
 # Neo-Hookean law: benchmarks/skfem_neo_hookean.py:8-52 (residual P and the
 # tangent tensor), with W = mu/2 (I1-3) - mu ln J + lambda/2 (ln J)^2.

@@ -112,9 +112,27 @@ __global__ void k_gather_rows(int64_t n_rows, const int32_t *__restrict__ indptr
     }
 }
 
+// Thread per DOF: out[r] = sum of the element vector entries incident on r,
+// in element order (the incidence lists are sorted by element).
+__global__ void k_gather_vector(int64_t n_rows, const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
+                                const double *__restrict__ le, double *__restrict__ out) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    double acc = 0.0;
+    for (int32_t it = inc_ptr[r]; it < inc_ptr[r + 1]; ++it) acc += le[inc[it]];
+    out[r] = acc;
+}
+
 }  // namespace
 
 // Fixed-order gather of element matrices (E, Lr, Lc) into the pattern's CSR values.
+void gather_element_vectors(const skg_pattern *pat, const double *le, double *out, cudaStream_t s) {
+    if (!pat->n_rows) return;
+    k_gather_vector<<<grid_for(pat->n_rows, 128), 128, 0, s>>>(pat->n_rows, pat->inc_ptr.get(), pat->inc.get(), le,
+                                                               out);
+    SKG_LAUNCH_CHECK("gather_vector");
+}
+
 void gather_element_matrices(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
     if (!pat->n_rows) return;
     if (pat->max_row_len > 0 && pat->row_local == pat->col_local) {

@@ -30,6 +30,7 @@
 namespace skg {
 
 void gather_element_matrices(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s);
+void gather_element_vectors(const skg_pattern *pat, const double *le, double *out, cudaStream_t s);
 
 namespace {
 
@@ -339,6 +340,37 @@ __global__ void k_n1_element(int64_t ne, const double *__restrict__ p, int64_t n
         }
 }
 
+// Vector load f . phi: local_a = s_a sum_q sum_i phi_a,i(x_q) f_i(e, q) |det| w_q
+// with phi_a = lambda_i grad lambda_j - lambda_j grad lambda_i (TetN1LinearAssembler).
+__global__ void k_n1_load(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+                          const int8_t *__restrict__ signs, int nq, const double *__restrict__ Xq,
+                          const double *__restrict__ Wq, const double *__restrict__ f, double *__restrict__ le) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    double J[9], b[4][3], det;
+    n1_geometry(p, npts, t, ne, e, J, b, det);
+    const double adet = fabs(det), idet = 1.0 / det;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const int64_t EQ = ne * (int64_t)nq;
+    for (int q = 0; q < nq; ++q) {
+        const double x = Xq[q], y = Xq[nq + q], z = Xq[2 * nq + q];
+        const double lam[4] = {1.0 - x - y - z, x, y, z};
+        const double dx = adet * Wq[q];
+        const double fx = f[e * nq + q], fy = f[EQ + e * nq + q], fz = f[2 * EQ + e * nq + q];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const int i = edge_v(a, 0), j = edge_v(a, 1);
+            double dot = 0.0;
+            dot += (lam[i] * b[j][0] - lam[j] * b[i][0]) * idet * fx;
+            dot += (lam[i] * b[j][1] - lam[j] * b[i][1]) * idet * fy;
+            dot += (lam[i] * b[j][2] - lam[j] * b[i][2]) * idet * fz;
+            acc[a] += dot * dx;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 6; ++a) le[e * 6 + a] = (double)signs[a * ne + e] * acc[a];
+}
+
 }  // namespace
 }  // namespace skg
 
@@ -464,5 +496,28 @@ extern "C" int skg_n1_assemble_pointwise(const skg_pattern *pat, const double *d
             SKG_LAUNCH_CHECK("n1_element_pointwise");
         }
         gather_element_matrices(pat, Ke.get(), d_values, s);
+    });
+}
+
+extern "C" int skg_n1_vector_load(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
+                                  const int8_t *d_signs, int64_t ne, int32_t nq, const double *h_X, const double *h_W,
+                                  const double *d_f, double *d_out, void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(ne == pat->n_elements && pat->row_local == 6, "mesh does not match the pattern");
+        require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+        require(d_p && d_t && d_signs && d_f && d_out, "mesh, load or output arrays are NULL");
+        cudaStream_t s = as_stream(stream);
+        std::vector<double> xw(4 * (size_t)nq);
+        for (int i = 0; i < 3 * nq; ++i) xw[i] = h_X[i];
+        for (int q = 0; q < nq; ++q) xw[3 * nq + q] = h_W[q];
+        DevBuf<double> dxw(xw.size(), s), le((size_t)ne * 6, s);
+        SKG_CUDA(cudaMemcpyAsync(dxw.get(), xw.data(), xw.size() * 8, cudaMemcpyHostToDevice, s));
+        if (ne) {
+            k_n1_load<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, dxw.get(), dxw.get() + 3 * nq,
+                                                       d_f, le.get());
+            SKG_LAUNCH_CHECK("n1_load");
+        }
+        gather_element_vectors(pat, le.get(), d_out, s);
     });
 }

@@ -15,7 +15,7 @@ from .element import ElementTetP1, ElementTetP2, ElementVector
 from .errors import UnsupportedNativeForm
 from .forms import BilinearForm, LinearForm, asm, ddot, div, dot, grad, inner, mul, sym_grad
 from .hyperelastic import EnergySurrogate, NeoHookean
-from .hcurl import (AffineTetN1Basis, HcurlTetGeometryDiagnostics, TetN1Assembler,
+from .hcurl import (AffineTetN1Basis, HcurlTetGeometryDiagnostics, TetN1Assembler, TetN1LinearAssembler,
                     estimate_tet_n1_assembly_memory)
 from .mesh import MeshTet, MeshTet2
 from .preflight import (AssemblyMemoryBudgetError, AssemblyMemoryEstimate, enforce_memory_budget,
@@ -28,7 +28,7 @@ __version__ = "0.1.0"
 __all__ = [
     "AffineTetN1Basis", "AssemblyMemoryBudgetError", "AssemblyMemoryEstimate", "BACKEND", "Basis",
     "BilinearForm", "CAPABILITIES", "ElementTetP1", "ElementTetP2", "ElementVector", "GeometryDiagnostics",
-    "HcurlTetGeometryDiagnostics", "LinearForm", "EnergySurrogate", "MeshTet", "MeshTet2", "NeoHookean", "P1Energy", "TetN1Assembler",
+    "HcurlTetGeometryDiagnostics", "LinearForm", "EnergySurrogate", "MeshTet", "MeshTet2", "NeoHookean", "P1Energy", "TetN1Assembler", "TetN1LinearAssembler",
     "UnsupportedNativeForm", "asm", "available_num_threads", "ddot", "div", "dot", "enforce_memory_budget",
     "estimate_bilinear_memory", "estimate_tet_n1_assembly_memory", "format_bytes", "get_num_threads",
     "grad", "has_capability", "inner", "mul", "set_num_threads", "sym_grad", "thread_limit",

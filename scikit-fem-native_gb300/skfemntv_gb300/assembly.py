@@ -52,6 +52,15 @@ class Pattern:
         # fused row passes write every CSR value once, so they may write host memory directly
         self.blocked = mrl.value > 0
 
+    def device_csr(self):
+        """(crow_indices, col_indices) int64 CUDA tensors of the pattern (cached)."""
+        if getattr(self, "_dev_csr", None) is None:
+            indptr = dev.empty(self.n_rows + 1, np.int64)
+            indices = dev.empty(max(1, self.nnz), np.int32)
+            call("skg_pattern_export", self.h, dev.ptr(indptr), dev.ptr(indices), dev.stream_ptr())
+            self._dev_csr = (indptr, indices[: self.nnz].long())
+        return self._dev_csr
+
     def host_csr(self):
         indptr = dev.empty(self.n_rows + 1, np.int64)
         indices = dev.empty(max(1, self.nnz), np.int32)
@@ -182,6 +191,18 @@ class _MatrixTarget:
             return None
         return ctypes.c_void_p(self._pinned.data_ptr())
 
+    def torch_csr(self):
+        """The device values as a CUDA ``torch.sparse_csr_tensor`` (no host copy;
+        the values buffer is reused by the next assembly, like the host matrix)."""
+        import warnings
+
+        import torch
+
+        crow, col = self.pattern.device_csr()
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore", UserWarning)  # torch marks sparse CSR as beta
+            return torch.sparse_csr_tensor(crow, col, self.d_values[: self.pattern.nnz], size=self.matrix.shape)
+
     def finish_direct(self):
         import torch
 
@@ -260,6 +281,13 @@ class NativeBilinearForm:
              dev.ptr(self.target.d_values), None, dev.stream_ptr())
         return self.target.d_values
 
+    def assemble_torch(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
+                       precision="fp64"):
+        """Device-resident result for GPU consumers: a CUDA sparse CSR tensor."""
+        self.assemble_device(value=value, gradient=gradient, symmetric_gradient=symmetric_gradient,
+                             divergence=divergence, precision=precision)
+        return self.target.torch_csr()
+
     def assemble(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
                  num_threads=0, precision="fp64"):
         """Host CSR matrix (reused between calls, as the reference's).  On the fused
@@ -332,6 +360,11 @@ class NativeTensorForm:
              dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(d), dev.ptr(self.target.d_values), None,
              dev.stream_ptr())
         return False
+
+    def assemble_torch(self, raw, precision="fp64"):
+        """Device-resident result for GPU consumers: a CUDA sparse CSR tensor."""
+        self.assemble_device(raw, precision)
+        return self.target.torch_csr()
 
     def assemble(self, raw, precision="fp64", copy=True):
         """Host CSR matrix.  ``copy=True`` (the reference's behaviour,

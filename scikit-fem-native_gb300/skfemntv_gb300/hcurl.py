@@ -120,6 +120,12 @@ class AffineTetN1Basis:
         return vals * s, curls * s
 
     @property
+    def global_coordinates(self):
+        """Physical quadrature coordinates as (component, cell, point) (hcurl_basis.py:435-440)."""
+        vertices = self.mesh.p[:, self.mesh.t[0]]
+        return vertices[:, :, None] + np.einsum("ire,rq->ieq", self.jacobians, self.X)
+
+    @property
     def values(self):
         """Mapped values as (basis, component, cell, quadrature)."""
         return self._mapped()[0].transpose(1, 2, 0, 3)
@@ -205,6 +211,12 @@ class TetN1Assembler:
         self.assemble_device(_out=out, **kw)
         return self.target.finish_direct() if out is not None else self.target.download()
 
+    def assemble_maxwell_torch(self, *, mass_coefficient=None, curl_coefficient=None, precision="fp64"):
+        """Device-resident Maxwell matrix: a CUDA sparse CSR tensor (values reused)."""
+        self.assemble_device(mass_coefficient=mass_coefficient, curl_coefficient=curl_coefficient,
+                             precision=precision)
+        return self.target.torch_csr()
+
     def assemble_maxwell(self, *, mass_coefficient=None, curl_coefficient=None, precision="fp64"):
         return self._host(mass_coefficient=mass_coefficient, curl_coefficient=curl_coefficient, precision=precision)
 
@@ -213,3 +225,39 @@ class TetN1Assembler:
 
     def assemble_curl_curl(self, coefficient=None, precision="fp64"):
         return self._host(curl_coefficient=coefficient, include_mass=False, precision=precision)
+
+
+class TetN1LinearAssembler:
+    """Reusable vector-load assembler for ``AffineTetN1Basis``
+    (hcurl_assembler.py:218-266): ``assemble_vector_load(field)`` returns the
+    reused load vector r_a = int f . phi_a."""
+
+    def __init__(self, basis):
+        if not isinstance(basis, AffineTetN1Basis):
+            raise TypeError("basis must be AffineTetN1Basis")
+        self.basis = basis
+        E = basis.mesh.nelements
+        self._dofs = basis._ee_dev.t().contiguous()  # (E, 6)
+        self.pattern = Pattern(self._dofs, None, E, 6, 0, basis.N, 0)
+        self._vector = np.zeros(basis.N, dtype=np.float64)
+        self._d_out = dev.empty(max(1, basis.N), np.float64)
+
+    def _values(self, field):
+        b = self.basis
+        values = field(b.global_coordinates) if callable(field) else field
+        values = np.asarray(values, dtype=np.float64)
+        expected = (3,) + b.dx.shape
+        try:
+            return np.broadcast_to(values, expected)
+        except ValueError as error:
+            raise ValueError(f"vector load must broadcast to {expected}") from error
+
+    def assemble_vector_load(self, field):
+        b = self.basis
+        E, Q = b.dx.shape
+        f = dev.to_device(self._values(field), np.float64)
+        call("skg_n1_vector_load", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1], dev.ptr(b._t4),
+             dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W), dev.ptr(f), dev.ptr(self._d_out),
+             dev.stream_ptr())
+        self._vector[:] = self._d_out[: b.N].cpu().numpy()
+        return self._vector

@@ -137,6 +137,15 @@ def main():
                              edges=topo.edges, element_edges=topo.element_edges,
                              signs=topo.element_edge_signs, detJ=nb.detJ)
 
+    # --- Nedelec N1 vector load f . phi on the same mesh (own seed) ---
+    rng_l = np.random.default_rng(np.random.SeedSequence(31))
+    la = sk.TetN1LinearAssembler(nb)
+    fq = rng_l.standard_normal((3,) + nb.dx.shape)
+    load_arr = la.assemble_vector_load(fq).copy()
+    load_fun = la.assemble_vector_load(
+        lambda x: np.stack([np.sin(3.0 * x[0]), x[1] * x[2], np.cos(2.0 * x[2]) - x[0]])).copy()
+    out["n1_load"] = dict(p=p_r, t=t_r, f=fq, load=load_arr, load_callable=load_fun, xq=nb.global_coordinates)
+
     # --- vector P1 elasticity terms: symmetric gradient + divergence + mass ---
     mv = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3)
     bv = sk.Basis(mv, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
@@ -183,7 +192,10 @@ def main():
     out["p2_load"] = dict(p=m2.p, t=m2.t, X=X4, W=W4, f=fq, rhs=np.asarray(rhs).copy())
 
     os.makedirs(HERE, exist_ok=True)
+    only = set(sys.argv[1:])  # fixture names to (re)write; all when empty
     for name, arrays in out.items():
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
         print(f"{name}: {os.path.getsize(path) / 1024:.1f} KiB")

@@ -213,6 +213,21 @@ def test_n1_split_precision_error_bound():
     assert 0 < err < 1e-7
 
 
+def test_n1_vector_load():
+    """TetN1LinearAssembler.assemble_vector_load vs the reference (array and callable fields)."""
+    g = load_golden("n1_load")
+    nb = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]))
+    la = sk.TetN1LinearAssembler(nb)
+    assert relerr(nb.global_coordinates, g["xq"]) < 1e-15
+    r = la.assemble_vector_load(g["f"])
+    assert relerr(r, g["load"]) < RTOL
+    r2 = la.assemble_vector_load(lambda x: np.stack([np.sin(3.0 * x[0]), x[1] * x[2], np.cos(2.0 * x[2]) - x[0]]))
+    assert r2 is r  # reused vector, as the reference's
+    assert relerr(r2, g["load_callable"]) < RTOL
+    with pytest.raises(ValueError, match="vector load must broadcast"):
+        la.assemble_vector_load(np.ones((2, 3)))
+
+
 def test_n1_mass_and_curl_separately():
     g = load_golden("n1_maxwell")
     nb = O.make_n1_basis(g["p"], g["t"])
@@ -308,3 +323,28 @@ def test_full_size_p1_laplace_vs_oracle():
     data, indptr, indices = O.bilinear_assemble(ob, gradient=1.0)
     assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
     assert relerr(K.data, data) < RTOL
+
+
+def test_device_resident_csr_handoff():
+    """assemble_torch returns the same matrix as a CUDA sparse CSR tensor."""
+    import torch
+    from skfemntv_gb300.assembly import NativeTensorForm
+
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    form = NativeTensorForm(b)
+    K = form.assemble(Apub, copy=True)
+    assert relerr(K.data, g["data"]) < RTOL
+    T = form.assemble_torch(Apub)
+    x = np.random.default_rng(0).standard_normal(K.shape[1])
+    y = (T @ torch.as_tensor(x, device="cuda")[:, None]).cpu().numpy()[:, 0]
+    assert relerr(y, K @ x) < 1e-13
+    gn = load_golden("n1_maxwell")
+    a = sk.TetN1Assembler(sk.AffineTetN1Basis(sk.MeshTet(gn["p"], gn["t"])))
+    Kn = a.assemble_maxwell(mass_coefficient=1.0).copy()
+    Tn = a.assemble_maxwell_torch(mass_coefficient=1.0)
+    xn = np.random.default_rng(1).standard_normal(Kn.shape[1])
+    yn = (Tn @ torch.as_tensor(xn, device="cuda")[:, None]).cpu().numpy()[:, 0]
+    assert relerr(yn, Kn @ xn) < 1e-13

@@ -96,6 +96,16 @@ def test_n1_maxwell():
     assert rel(data, g["data"]) < 1e-14
 
 
+def test_n1_vector_load():
+    g = load_golden("n1_load")
+    b = O.make_n1_basis(g["p"], g["t"])
+    assert rel(O.n1_vector_load(b, g["f"]), g["load"]) < 1e-14
+    xq = O.n1_global_coordinates(g["p"], g["t"], b.X)
+    assert rel(xq, g["xq"]) < 1e-15
+    fx = np.stack([np.sin(3.0 * xq[0]), xq[1] * xq[2], np.cos(2.0 * xq[2]) - xq[0]])
+    assert rel(O.n1_vector_load(b, fx), g["load_callable"]) < 1e-14
+
+
 def test_vector_p1_elasticity_terms():
     g = load_golden("vp1_elasticity")
     b = O.make_basis(g["p"], g["t"], False, comp=3, quadrature=(X1, W1))
