@@ -348,3 +348,37 @@ def test_device_resident_csr_handoff():
     xn = np.random.default_rng(1).standard_normal(Kn.shape[1])
     yn = (Tn @ torch.as_tensor(xn, device="cuda")[:, None]).cpu().numpy()[:, 0]
     assert relerr(yn, Kn @ xn) < 1e-13
+
+
+def _mixed_orientation_meshes():
+    axis = np.linspace(0.0, 1.0, 3)
+    original = sk.MeshTet.init_tensor(axis, axis, axis)
+    conn = original.t.copy()
+    sel = np.arange(original.nelements) % 2 == 0
+    first = conn[0, sel].copy()
+    conn[0, sel] = conn[1, sel]
+    conn[1, sel] = first
+    return original, sk.MeshTet(original.p, conn)
+
+
+def test_n1_orientation_invariance():
+    """As the reference's test_hcurl_tet_robustness.py:31-77: swapping two vertices of
+    every other tetrahedron (inverting it) leaves the Maxwell operator and the
+    vector load unchanged up to the edge permutation."""
+    original_mesh, mixed_mesh = _mixed_orientation_meshes()
+    ob = sk.AffineTetN1Basis(original_mesh, intorder=4)
+    mb = sk.AffineTetN1Basis(mixed_mesh, intorder=4)
+    assert ob.geometry_diagnostics.inverted_cell_count == 0
+    assert 0 < mb.geometry_diagnostics.inverted_cell_count < mixed_mesh.nelements
+    lookup = {tuple(e): i for i, e in enumerate(mb.dof_map.topology.edges.T)}
+    perm = np.array([lookup[tuple(e)] for e in ob.dof_map.topology.edges.T])
+    Ko = sk.TetN1Assembler(ob).assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2).toarray()
+    Km = sk.TetN1Assembler(mb).assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2).toarray()[perm][:, perm]
+    np.testing.assert_allclose(Ko, Km, atol=4e-13)
+
+    def field(x):
+        return np.array((1.0 + x[1], x[0] * x[2], -0.25 + x[0] * x[1]))
+
+    lo = sk.TetN1LinearAssembler(ob).assemble_vector_load(field).copy()
+    lm = sk.TetN1LinearAssembler(mb).assemble_vector_load(field)[perm]
+    np.testing.assert_allclose(lo, lm, atol=4e-14)
