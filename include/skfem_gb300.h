@@ -150,6 +150,21 @@ int skg_h1_assemble_tensor_tabulated(const skg_pattern *pattern,
                                      const double *d_grad, const double *d_w,
                                      const double *d_coef, double *d_values,
                                      double *d_scratch, void *stream);
+/* Cross-basis (test x trial) assembly with a caller-supplied contraction
+ * tensor: NativeCrossBilinearForm.assemble_tensor(row_kind, column_kind, C)
+ * and .assemble(kind, c) (python/skfemntv/bilinear_form.py:102-367,
+ * cpp/src/assembly/cross_bilinear_assembler.cpp:55-107).  Kinds: 0 value,
+ * 1 gradient.  Test tabulation nt functions (shape (E,Q,nt) / grad
+ * (E,Q,nt,3)), Ct components; trial likewise; d_dx (E,Q); d_coef
+ * (E,Q,Ct,[3],Cc,[3]).  Pattern: test DOFs (E, nt*Ct) x trial DOFs
+ * (E, nc*Cc). */
+int skg_cross_assemble_tabulated(const skg_pattern *pattern, int64_t n_elements,
+                                 int32_t nq, int32_t nt, int32_t Ct, int32_t row_kind,
+                                 const double *d_t_shape, const double *d_t_grad,
+                                 int32_t nc, int32_t Cc, int32_t col_kind,
+                                 const double *d_c_shape, const double *d_c_grad,
+                                 const double *d_dx, const double *d_coef,
+                                 double *d_values, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Fused scalar P1/P2 assembly straight from mesh coordinates.          */

@@ -89,6 +89,43 @@ __global__ void k_h1_local_tensor(int64_t ne, int n, int C, int nq, const double
     }
 }
 
+// Test x trial local matrices with a full contraction tensor (cross bases):
+// thread per (element, test row i = a*Ct + r):
+//   K[(a,r),(b,c)] = sum_q dx sum_ii sum_jj R_a[ii] C[e,q,r,ii,c,jj] S_b[jj]
+// R_a = shape value (Rd = 1) or gradient (Rd = 3) of test function a; S_b
+// likewise for the trial function b.  C (E, Q, Ct, Rd, Cc, Sd) contiguous.
+__global__ void k_cross_local(int64_t ne, int nq, int nt, int Ct, int Rd, const double *__restrict__ t_shape,
+                              const double *__restrict__ t_grad, int nc, int Cc, int Sd,
+                              const double *__restrict__ c_shape, const double *__restrict__ c_grad,
+                              const double *__restrict__ dx, const double *__restrict__ coef,
+                              double *__restrict__ Ke) {
+    const int Lt = nt * Ct, Lc = nc * Cc;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= ne * Lt) return;
+    const int64_t e = tid / Lt;
+    const int i = (int)(tid % Lt);
+    const int a = i / Ct, r = i % Ct;
+    double *row = Ke + (e * Lt + i) * (int64_t)Lc;
+    for (int k = 0; k < Lc; ++k) {
+        const int b = k / Cc, c = k % Cc;
+        double acc = 0.;
+        for (int q = 0; q < nq; ++q) {
+            const int64_t eq = e * nq + q;
+            double R[3], S[3];
+            if (Rd == 1) R[0] = t_shape[eq * nt + a];
+            else for (int d = 0; d < 3; ++d) R[d] = t_grad[(eq * nt + a) * 3 + d];
+            if (Sd == 1) S[0] = c_shape[eq * nc + b];
+            else for (int d = 0; d < 3; ++d) S[d] = c_grad[(eq * nc + b) * 3 + d];
+            const double *Cq = coef + ((eq * Ct + r) * Rd) * (int64_t)(Cc * Sd) + c * Sd;
+            double s = 0.;
+            for (int ii = 0; ii < Rd; ++ii)
+                for (int jj = 0; jj < Sd; ++jj) s += R[ii] * Cq[ii * Cc * Sd + jj] * S[jj];
+            acc += dx[eq] * s;
+        }
+        row[k] = acc;
+    }
+}
+
 // Row-owner gather of element matrices Ke (E, Lr, Lc) into CSR values.
 __global__ void k_gather_rows(int64_t n_rows, const int32_t *__restrict__ indptr,
                               const int32_t *__restrict__ indices, const int32_t *__restrict__ inc_ptr,
@@ -182,10 +219,7 @@ extern "C" int skg_h1_assemble_tabulated(const skg_pattern *pat, const int32_t *
                                                                        d_value, d_gradient, d_symgrad, d_div, Ke);
             SKG_LAUNCH_CHECK("h1_local_tabulated");
         }
-        k_gather_rows<<<grid_for(pat->n_rows, 128), 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
-                                                                 pat->inc_ptr.get(), pat->inc.get(),
-                                                                 pat->col_dofs.get(), L, L, Ke, d_values);
-        SKG_LAUNCH_CHECK("gather_rows");
+        gather_element_matrices(pat, Ke, d_values, s);
     });
 }
 
@@ -212,10 +246,34 @@ extern "C" int skg_h1_assemble_tensor_tabulated(const skg_pattern *pat, const in
             k_h1_local_tensor<<<grid_for(ne * L, 128), 128, 0, s>>>(ne, nodes, comp, nq, d_grad, d_w, d_coef, Ke);
             SKG_LAUNCH_CHECK("h1_local_tensor");
         }
-        k_gather_rows<<<grid_for(pat->n_rows, 128), 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
-                                                                 pat->inc_ptr.get(), pat->inc.get(),
-                                                                 pat->col_dofs.get(), L, L, Ke, d_values);
-        SKG_LAUNCH_CHECK("gather_rows");
+        gather_element_matrices(pat, Ke, d_values, s);
     });
 }
 
+
+extern "C" int skg_cross_assemble_tabulated(const skg_pattern *pat, int64_t ne, int32_t nq, int32_t nt, int32_t Ct,
+                                            int32_t row_kind, const double *d_t_shape, const double *d_t_grad,
+                                            int32_t nc, int32_t Cc, int32_t col_kind, const double *d_c_shape,
+                                            const double *d_c_grad, const double *d_dx, const double *d_coef,
+                                            double *d_values, void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(nt > 0 && nc > 0 && Ct > 0 && Cc > 0 && nq > 0, "invalid local sizes");
+        require(ne == pat->n_elements && pat->row_local == nt * Ct && pat->col_local == nc * Cc,
+                "tabulated arrays do not match the pattern");
+        require((row_kind == 0 || row_kind == 1) && (col_kind == 0 || col_kind == 1),
+                "tensor kind must be value or gradient");
+        require((row_kind == 0 ? d_t_shape : d_t_grad) && (col_kind == 0 ? d_c_shape : d_c_grad) && d_dx && d_coef,
+                "tabulated geometry or coefficient arrays are NULL");
+        cudaStream_t s = as_stream(stream);
+        const int Lt = nt * Ct, Lc = nc * Cc;
+        DevBuf<double> Ke((size_t)ne * Lt * Lc, s);
+        if (ne) {
+            k_cross_local<<<grid_for(ne * Lt, 128), 128, 0, s>>>(ne, nq, nt, Ct, row_kind ? 3 : 1, d_t_shape, d_t_grad,
+                                                                nc, Cc, col_kind ? 3 : 1, d_c_shape, d_c_grad, d_dx,
+                                                                d_coef, Ke.get());
+            SKG_LAUNCH_CHECK("cross_local");
+        }
+        gather_element_matrices(pat, Ke.get(), d_values, s);
+    });
+}

@@ -375,6 +375,93 @@ class NativeTensorForm:
         return self.target.copy_matrix() if copy else m
 
 
+class NativeCrossBilinearForm:
+    """Test x trial assembly between two bases of one mesh and one quadrature
+    rule (NativeCrossBilinearForm, bilinear_form.py:102-367): value, gradient
+    and divergence kinds, and caller-supplied value / gradient contraction
+    tensors.  Each call returns a new matrix, as the reference's."""
+
+    def __init__(self, test_basis, trial_basis, *, memory_limit_bytes=None, memory_safety_factor=1.25):
+        if test_basis.dx.shape != trial_basis.dx.shape:
+            raise ValueError("trial and test quadrature shapes must match")
+        if not np.allclose(test_basis.dx, trial_basis.dx):
+            raise ValueError("trial and test quadrature weights must match")
+        self.memory_estimate = estimate_bilinear_memory(test_basis, trial_basis)
+        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
+        if not np.allclose(test_basis.global_coordinates, trial_basis.global_coordinates):
+            raise ValueError("trial and test quadrature coordinates must match")
+        self.test_basis, self.trial_basis = test_basis, trial_basis
+        E = test_basis.mesh.nelements
+        Lt, Lc = test_basis._nodes * test_basis._comp, trial_basis._nodes * trial_basis._comp
+        self.pattern = Pattern(test_basis._dev_dofs(), trial_basis._dev_dofs(), E, Lt, Lc, test_basis.N,
+                               trial_basis.N)
+        self.target = _MatrixTarget(self.pattern, (test_basis.N, trial_basis.N))
+        self.shape = (test_basis.N, trial_basis.N)
+        self.coefficient_shape = test_basis.dx.shape
+        self.test_components = test_basis._comp
+        self.trial_components = trial_basis._comp
+        self.dimension = 3
+
+    def assemble(self, kind, coefficient):
+        """kind: "value", "gradient", "row_divergence" (vector test, scalar
+        trial) or "column_divergence" (scalar test, vector trial); coefficient
+        broadcast to the (cell, point) shape."""
+        coefficient = np.asarray(coefficient, dtype=np.float64)
+        scalar = np.broadcast_to(coefficient, self.coefficient_shape)
+        Ct, Cc, d = self.test_components, self.trial_components, self.dimension
+        if kind in ("row_divergence", "column_divergence"):
+            if kind == "row_divergence":
+                if Ct != d or Cc != 1:
+                    raise ValueError("row divergence requires vector test and scalar trial")
+                tensor = np.zeros((Ct, d, Cc))
+                for comp in range(Ct):
+                    tensor[comp, comp, 0] = 1.0
+                row_kind, column_kind = "gradient", "value"
+            else:
+                if Cc != d or Ct != 1:
+                    raise ValueError("column divergence requires scalar test and vector trial")
+                tensor = np.zeros((Ct, Cc, d))
+                for comp in range(Cc):
+                    tensor[0, comp, comp] = 1.0
+                row_kind, column_kind = "value", "gradient"
+        else:
+            if Ct != Cc:
+                raise ValueError("value and gradient contractions require matching component counts")
+            if kind == "gradient":
+                tensor = np.einsum("rc,ij->ricj", np.eye(Ct), np.eye(d))
+                row_kind = column_kind = "gradient"
+            else:
+                tensor = np.eye(Ct)
+                row_kind = column_kind = "value"
+        full = scalar[(...,) + (None,) * tensor.ndim] * tensor
+        return self.assemble_tensor(row_kind, column_kind, full)
+
+    def assemble_tensor(self, row_kind, column_kind, coefficient, *, num_threads=0):
+        """Assemble a caller-supplied value / gradient contraction tensor
+        (cell, point) + row axes + column axes."""
+        valid = {"value", "gradient"}
+        if row_kind not in valid or column_kind not in valid:
+            raise ValueError("tensor kind must be value or gradient")
+        row_axes = (self.test_components,) + ((self.dimension,) if row_kind == "gradient" else ())
+        column_axes = (self.trial_components,) + ((self.dimension,) if column_kind == "gradient" else ())
+        expected = self.coefficient_shape + row_axes + column_axes
+        coefficient = np.asarray(coefficient, dtype=np.float64)
+        try:
+            coefficient = np.broadcast_to(coefficient, expected)
+        except ValueError as error:
+            raise ValueError(f"tensor coefficient must broadcast to {expected}") from error
+        tb, cb = self.test_basis, self.trial_basis
+        tt, ct = tb._device_tabulation(), cb._device_tabulation()
+        E, Q = self.coefficient_shape
+        d_coef = dev.to_device(coefficient, np.float64)
+        call("skg_cross_assemble_tabulated", self.pattern.h, E, Q, tb._nodes, tb._comp,
+             int(row_kind == "gradient"), dev.ptr(tt["shape"]), dev.ptr(tt["grad"]), cb._nodes, cb._comp,
+             int(column_kind == "gradient"), dev.ptr(ct["shape"]), dev.ptr(ct["grad"]), dev.ptr(tt["dx"]),
+             dev.ptr(d_coef), dev.ptr(self.target.d_values), dev.stream_ptr())
+        self.target.download()
+        return self.target.copy_matrix()
+
+
 class NativeLinearForm:
     """f.v + G:grad v on one basis (linear_form.py:17-107)."""
 

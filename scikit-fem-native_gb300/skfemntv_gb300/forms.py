@@ -154,6 +154,13 @@ class _Field:
                 return _Term("divergence", None, self.factor * other.factor)
             if self.kind == "value" and other.kind == "value" and self.role != other.role:
                 return _Term("value", None, self.factor * other.factor)
+            # cross-basis couplings: div(trial) * test value, div(test) * trial value
+            if self.kind == "div" and other.kind == "value" and self.role != other.role:
+                kind = "column_divergence" if self.role == "trial" else "row_divergence"
+                return _Term(kind, None, self.factor * other.factor)
+            if self.kind == "value" and other.kind == "div" and self.role != other.role:
+                kind = "column_divergence" if other.role == "trial" else "row_divergence"
+                return _Term(kind, None, self.factor * other.factor)
             raise UnsupportedNativeForm("unsupported product of form fields")
         if self.role == "test" and self.kind == "value" and _coefficient_like(other):
             return _LinearTerm("value", _coef(other), self.factor)
@@ -379,6 +386,7 @@ class _BilinearForm:
         self.function = function
         self._native_cache = WeakKeyDictionary()
         self._tensor_cache = WeakKeyDictionary()
+        self._cross_cache = WeakKeyDictionary()
 
     def assemble(self, *bases, **kwargs):
         return asm(self, *bases, **kwargs)
@@ -444,6 +452,30 @@ def _evaluate(coefficient, kwargs, factor):
     return v
 
 
+def _cross_assemble(form, trial_basis, test_basis, kwargs, memory_limit_bytes, memory_safety_factor):
+    """Cross-basis BilinearForm (forms.py:407-486): value, gradient and divergence
+    terms between a trial and a test basis on one mesh."""
+    from .assembly import NativeCrossBilinearForm
+
+    expr = _trace(form, (_Field("trial", "value"), _Field("test", "value")), test_basis, kwargs,
+                  "cross-basis BilinearForm")
+    terms = _terms(expr, _Term, _Sum, "cross-basis BilinearForm must reduce to value, gradient, or divergence "
+                   "contractions")
+    by_trial = form._cross_cache.setdefault(trial_basis, WeakKeyDictionary())
+    native = by_trial.get(test_basis)
+    if native is None:
+        native = NativeCrossBilinearForm(test_basis, trial_basis, memory_limit_bytes=memory_limit_bytes,
+                                         memory_safety_factor=memory_safety_factor)
+        by_trial[test_basis] = native
+    result = None
+    for t in terms:
+        if t.kind not in ("value", "gradient", "row_divergence", "column_divergence"):
+            raise UnsupportedNativeForm(f"unsupported cross-basis term kind {t.kind!r}")
+        m = native.assemble(t.kind, _evaluate(t.coefficient, kwargs, t.factor))
+        result = m if result is None else result + m
+    return result
+
+
 def asm(form, *bases, num_threads=None, memory_limit_bytes=None, memory_safety_factor=1.25,
         precision="fp64", **kwargs):
     """Assemble on the GPU (drop-in for skfemntv.asm, forms.py:667-785).
@@ -466,6 +498,10 @@ def asm(form, *bases, num_threads=None, memory_limit_bytes=None, memory_safety_f
                        "ddot(coefficient, grad(v)), or a sum of those terms")
         return assemble_linear(form, basis, [(t.kind, _evaluate(t.coefficient, kwargs, t.factor)) for t in terms])
     if isinstance(form, _BilinearForm):
+        if len(bases) == 2:
+            if num_threads is not None:
+                raise UnsupportedNativeForm("per-call threads are not yet supported for cross-basis BilinearForm")
+            return _cross_assemble(form, bases[0], bases[1], kwargs, memory_limit_bytes, memory_safety_factor)
         if len(bases) != 1:
             raise UnsupportedNativeForm("native BilinearForm currently requires one shared basis")
         basis = bases[0]

@@ -146,6 +146,38 @@ def main():
         lambda x: np.stack([np.sin(3.0 * x[0]), x[1] * x[2], np.cos(2.0 * x[2]) - x[0]])).copy()
     out["n1_load"] = dict(p=p_r, t=t_r, f=fq, load=load_arr, load_callable=load_fun, xq=nb.global_coordinates)
 
+    # --- cross-basis assembly: P2 vector test x P1 scalar trial (Stokes coupling),
+    #     P2 x P1 scalar mass, and a full gradient tensor on vector P1 ---
+    rng_c = np.random.default_rng(np.random.SeedSequence(41))
+    mc = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 3),) * 3)
+    mc2 = sk.MeshTet2.from_mesh(mc)
+    from skfemntv.forms import div as fdiv  # type: ignore
+    bv2 = sk.Basis(mc2, sk.ElementVector(sk.ElementTetP2(), dim=3), quadrature=(X4, W4))
+    bs1 = sk.Basis(mc2, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(X4, W4))
+    bs2 = sk.Basis(mc2, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(X4, W4))
+
+    @sk.BilinearForm
+    def coupling(u, v, w):
+        return fdiv(v) * u
+
+    @sk.BilinearForm
+    def cmass(u, v, w):
+        return w.c * dot(u, v)
+
+    Kb = sk.asm(coupling, bs1, bv2)          # trial P1 scalar, test P2 vector
+    cc = rng_c.uniform(0.5, 2.0, size=bs2.dx.shape)
+    Km = sk.asm(cmass, bs1, bs2, c=cc)       # trial P1 scalar, test P2 scalar
+    bvp1 = sk.Basis(mc, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X4, W4))
+    T6 = rng_c.standard_normal(bvp1.dx.shape + (3, 3, 3, 3))
+    Kt = sk.NativeCrossBilinearForm(bvp1, bvp1).assemble_tensor("gradient", "gradient", T6)
+    Tv = rng_c.standard_normal(bvp1.dx.shape + (3, 3))
+    Kv = sk.NativeCrossBilinearForm(bvp1, bvp1).assemble_tensor("value", "value", Tv)
+    out["cross"] = dict(p0=mc.p, t0=mc.t, p2=mc2.p, t2=mc2.t, X=X4, W=W4, c=cc, T6=T6, Tv=Tv,
+                        **{f"b_{k}": v for k, v in csr_parts(Kb).items()},
+                        **{f"m_{k}": v for k, v in csr_parts(Km).items()},
+                        **{f"t_{k}": v for k, v in csr_parts(Kt).items()},
+                        **{f"v_{k}": v for k, v in csr_parts(Kv).items()})
+
     # --- vector P1 elasticity terms: symmetric gradient + divergence + mass ---
     mv = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3)
     bv = sk.Basis(mv, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))

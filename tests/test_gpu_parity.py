@@ -382,3 +382,40 @@ def test_n1_orientation_invariance():
     lo = sk.TetN1LinearAssembler(ob).assemble_vector_load(field).copy()
     lm = sk.TetN1LinearAssembler(mb).assemble_vector_load(field)[perm]
     np.testing.assert_allclose(lo, lm, atol=4e-14)
+
+
+def test_cross_basis_assembly_matches_reference():
+    """Two-basis asm (Stokes-type coupling div(v) u, a weighted P2 x P1 mass) and
+    NativeCrossBilinearForm.assemble_tensor (gradient and value tensors on vector
+    P1) against the reference's own outputs."""
+    g = load_golden("cross")
+    m = sk.MeshTet(g["p0"], g["t0"])
+    m2 = sk.MeshTet2.from_mesh(m)
+    XW = (g["X"], g["W"])
+    bv2 = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=3), quadrature=XW)
+    bs1 = sk.Basis(m2, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=XW)
+    bs2 = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=XW)
+
+    @sk.BilinearForm
+    def coupling(u, v, w):
+        return div(v) * u
+
+    @sk.BilinearForm
+    def cmass(u, v, w):
+        return w.c * dot(u, v)
+
+    def check(K, prefix):
+        assert K.shape == tuple(g[f"{prefix}_shape"])
+        assert np.array_equal(K.indptr, g[f"{prefix}_indptr"]) and np.array_equal(K.indices, g[f"{prefix}_indices"])
+        assert relerr(K.data, g[f"{prefix}_data"]) < RTOL
+
+    check(sk.asm(coupling, bs1, bv2), "b")
+    check(sk.asm(cmass, bs1, bs2, c=g["c"]), "m")
+    bvp1 = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=XW)
+    cf = sk.NativeCrossBilinearForm(bvp1, bvp1)
+    check(cf.assemble_tensor("gradient", "gradient", g["T6"]), "t")
+    check(cf.assemble_tensor("value", "value", g["Tv"]), "v")
+    with pytest.raises(ValueError, match="tensor coefficient must broadcast"):
+        cf.assemble_tensor("gradient", "gradient", np.ones((2, 2)))
+    with pytest.raises(ValueError, match="row divergence requires"):
+        cf.assemble("row_divergence", 1.0)
