@@ -213,6 +213,17 @@ def run_reference(args, rank):
 
 # ----------------------------------------------------------------- GPU side
 
+def reduce_max(x, world, device="cuda"):
+    """Largest value over the ranks (the slowest rank's time); identity for one rank."""
+    if world <= 1:
+        return x
+    import torch
+
+    tt = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -268,11 +279,7 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if world > 1:
-            tt = torch.tensor([x], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            return float(tt.item())
-        return x
+        return reduce_max(x, world)
 
     def time_mode(mode):
         for _ in range(max(3, args.warmup)):
@@ -412,11 +419,7 @@ def _timer(args, world):
                 fn()
             ev1.record(stream)
             barrier()
-        ms = ev0.elapsed_time(ev1) / args.steps
-        if world > 1:
-            tt = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = reduce_max(ev0.elapsed_time(ev1) / args.steps, world)
         return ms, clocks.summary()
 
     def wall(fn):
@@ -427,7 +430,7 @@ def _timer(args, world):
         for _ in range(args.steps):
             fn()
         barrier()
-        return (time.perf_counter() - t0) / args.steps
+        return reduce_max((time.perf_counter() - t0) / args.steps, world)
 
     return timed, wall
 

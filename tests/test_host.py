@@ -61,6 +61,11 @@ def test_form_terms():
     assert t.kind == "gradient_tensor" and np.array_equal(t.coefficient, A)
     s = 2.0 * ddot(grad(u), grad(v)) + dot(u, v) - dot(u, v)
     assert isinstance(s, _Sum) and [x.factor for x in s.terms] == [2.0, 1.0, -1.0]
+    # cross-basis couplings (forms.py:407-486 of the reference)
+    assert div(v) * u == _Term("row_divergence", None, 1.0)
+    assert u * div(v) == _Term("row_divergence", None, 1.0)
+    assert div(u) * v == _Term("column_divergence", None, 1.0)
+    assert (2.0 * div(u)) * v == _Term("column_divergence", None, 2.0)
 
 
 def test_coefficients_and_parameters():
