@@ -11,9 +11,10 @@ A = Q diag(exp(N(0, 0.5^2))) Q^T, 4-point quadrature (seeded synthetic data).
          stream); inputs (~670 MB per step) exceed the 129 MB L2.
   e2e    same metric through the assembler's host-facing API
          (NativeTensorForm.assemble): per step the coefficient A (3,3,E) is
-         read from host memory and the CSR values are written into the
-         page-locked buffer behind the returned scipy matrix (on Grace-
-         Blackwell the kernels do both directly over NVLink-C2C).
+         read from host memory (by the element kernel over NVLink-C2C on
+         Grace-Blackwell) and the CSR values land in the page-locked buffer
+         behind the returned scipy matrix, copied in row chunks while the
+         row pass runs.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -322,8 +323,7 @@ def run_gpu(args, rank, world):
     value = head["value"]
 
     # ---- e2e (native FP64) through the assembler's host API: A from host memory in,
-    # the CSR values out into the host matrix (kernels read / write host memory
-    # over NVLink-C2C where the device allows it, else staged copies)
+    # the CSR values out into the host matrix (chunked copies overlapping the row pass)
     for _ in range(2):
         form.assemble(A_pub, copy=False)
     barrier()

@@ -203,6 +203,17 @@ int skg_h1_assemble_affine_profiled(const skg_pattern *pattern, const double *d_
                                     int32_t coef_kind, const double *d_coef,
                                     int32_t precision, double *d_values,
                                     float *h_kernel_ms, void *stream);
+/* As skg_h1_assemble_affine, the values also delivered to page-locked host
+ * memory h_values (nnz): the row pass runs in row chunks and each chunk's
+ * values are copied while the next chunk is assembled (d_values is the
+ * device staging buffer).  Stream-ordered; h_values is complete when the
+ * stream is.  No counterpart in the reference (host-only). */
+int skg_h1_assemble_affine_host(const skg_pattern *pattern, const double *d_p,
+                                int64_t npts, const int32_t *d_t, int32_t nodes,
+                                int64_t n_elements, const int32_t *d_dofs, int32_t nq,
+                                const double *h_X, const double *h_W, int32_t coef_kind,
+                                const double *d_coef, int32_t precision, double *d_values,
+                                double *h_values, void *stream);
 
 /* Allocation-free variant of skg_h1_assemble_affine (no counterpart in
  * the reference).  For callers that cannot let a library allocate device

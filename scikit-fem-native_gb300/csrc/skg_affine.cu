@@ -624,7 +624,7 @@ template <int N, int MODE, int SLOTS, int P, bool EXACT>
 __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
     int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
     const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec, const void *__restrict__ Gv,
-    const double *__restrict__ Tg, const int *__restrict__ s_ptr, double *__restrict__ values) {
+    const double *__restrict__ Tg, const int *__restrict__ s_ptr, double *__restrict__ values, RowRange rr) {
     using GT = typename std::conditional<MODE == MODE_FP64, double, df64>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     double *Td = reinterpret_cast<double *>(smem);
@@ -646,6 +646,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
     double *accd = reinterpret_cast<double *>(warp_area + (size_t)warp * SLOTS * 8);
     df64 *accf = reinterpret_cast<df64 *>(accd);
     const int2 grp = groups[gi];
+    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) {
@@ -785,13 +786,14 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
                                                               const int4 *__restrict__ rec,
                                                               const float2 *__restrict__ Ke,
                                                               const int *__restrict__ s_ptr,
-                                                              double *__restrict__ values) {
+                                                              double *__restrict__ values, RowRange rr) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gi = blockIdx.x * kRowWarps + warp;
     if (gi >= n_groups) return;
     df64 *acc = reinterpret_cast<df64 *>(smem + (size_t)warp * SLOTS * 8);
     const int2 grp = groups[gi];
+    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) acc[j] = df64{0.f, 0.f};
@@ -854,14 +856,14 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
 
 template <int SLOTS, int P>
 void launch_ke_df_class(int n_groups, const int2 *groups, const skg_pattern *pat, const float2 *Ke, const int *s_ptr,
-                        double *values, cudaStream_t s) {
+                        double *values, cudaStream_t s, RowRange rr) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
         SKG_CUDA(cudaFuncSetAttribute(k_rows_ke_df<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_ke_df<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
-                                                              pat->rec.get(), Ke, s_ptr, values);
+                                                              pat->rec.get(), Ke, s_ptr, values, rr);
     SKG_LAUNCH_CHECK("rows_ke_df");
 }
 
@@ -930,7 +932,7 @@ void affine_table(int nodes, int nq, const double *X, const double *W, std::vect
 
 template <int N, int MODE, int SLOTS, int P, bool EXACT>
 void launch_group_class(int n_groups, const int2 *groups, const skg_pattern *pat, const void *G, const double *Tg,
-                        const int *s_ptr, double *values, cudaStream_t s) {
+                        const int *s_ptr, double *values, cudaStream_t s, RowRange rr) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)N * N * 4 * 8 + (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
@@ -939,17 +941,17 @@ void launch_group_class(int n_groups, const int2 *groups, const skg_pattern *pat
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_group<N, MODE, SLOTS, P, EXACT><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
                                                                       pat->inc_ptr.get(), pat->rec.get(), G, Tg, s_ptr,
-                                                                      values);
+                                                                      values, rr);
     SKG_LAUNCH_CHECK("rows_group");
 }
 
 template <int N, int MODE, bool EXACT = false>
 void launch_rows_groups(const skg_pattern *pat, const void *G, const double *Tg, const int *s_ptr, double *values,
-                        cudaStream_t s) {
+                        cudaStream_t s, RowRange rr = RowRange()) {
     launch_group_class<N, MODE, kGroupSlotsSmall, 1, EXACT>(pat->n_groups_small, pat->groups_small.get(), pat, G, Tg,
-                                                            s_ptr, values, s);
+                                                            s_ptr, values, s, rr);
     launch_group_class<N, MODE, kGroupSlotsLarge, 2, EXACT>(pat->n_groups_large, pat->groups_large.get(), pat, G, Tg,
-                                                            s_ptr, values, s);
+                                                            s_ptr, values, s, rr);
 }
 
 // True when the caller's rule reproduces the exact P2 table (30 T integer).
@@ -968,9 +970,12 @@ bool p2_rule_is_exact(const std::vector<double> &T) {
 }  // namespace
 
 // Shared by the C ABI entry points below.
+// h_values (optional, page-locked host): the values also go there, copied in
+// row chunks overlapping the row pass (run_row_pass).
 void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t, int32_t nodes,
                      int64_t ne, int32_t nq, const double *h_X, const double *h_W, int32_t coef_kind,
-                     const double *d_coef, int32_t precision, double *d_values, cudaStream_t s, cudaEvent_t *ev) {
+                     const double *d_coef, int32_t precision, double *d_values, cudaStream_t s, cudaEvent_t *ev,
+                     double *h_values) {
     require(pat != nullptr, "pattern is NULL");
     require(nodes == 4 || nodes == 10, "affine assembly supports P1 (4) and P2 (10) tetrahedra");
     require(ne == pat->n_elements && pat->row_local == nodes && pat->col_local == nodes,
@@ -1010,10 +1015,12 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_CUDA(cudaStreamSynchronize(s));
         if (h_misc[1] == 0 && h_misc[0] != INT_MIN) {
             if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-            launch_ke_df_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Kf.get(),
-                                                    misc.get(), d_values, s);
-            launch_ke_df_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Kf.get(),
-                                                    misc.get(), d_values, s);
+            run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) {
+                launch_ke_df_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Kf.get(),
+                                                        misc.get(), d_values, s, rr);
+                launch_ke_df_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Kf.get(),
+                                                        misc.get(), d_values, s, rr);
+            });
             if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
             return;
         }
@@ -1046,7 +1053,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             SKG_LAUNCH_CHECK("elem_ke_fp64");
         }
         if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-        add_element_rows<10>(pat, Ke.get(), d_values, s);
+        run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) { add_element_rows<10>(pat, Ke.get(), d_values, s, rr); });
         if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
         return;
     }
@@ -1070,23 +1077,26 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
                                                    pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(), G.get(),
                                                    Tg.get(), sp, d_values);
         SKG_LAUNCH_CHECK("rows_global");
+        if (h_values && pat->nnz)
+            SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
     } else {
         const int *sp_ptr = misc.get();
-#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s)
-        if (nodes == 4) {
-            if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
-            else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
-            else SKG_ROWS(4, MODE_DF64);
-        } else {
-            if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
-            else if (mode == MODE_SPLIT) {
-                if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s);
-                else SKG_ROWS(10, MODE_SPLIT);
+        run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) {
+#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, rr)
+            if (nodes == 4) {
+                if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
+                else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
+                else SKG_ROWS(4, MODE_DF64);
             } else {
-                if (exact) launch_rows_groups<10, MODE_DF64, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s);
-                else SKG_ROWS(10, MODE_DF64);
+                if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
+                else if (mode == MODE_SPLIT) {
+                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, rr);
+                    else SKG_ROWS(10, MODE_SPLIT);
+                } else {
+                    SKG_ROWS(10, MODE_DF64);
+                }
             }
-        }
+        });
 #undef SKG_ROWS
     }
     if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
@@ -1103,7 +1113,20 @@ extern "C" int skg_h1_assemble_affine(const skg_pattern *pat, const double *d_p,
     return guarded([&] {
         (void)d_dofs;
         affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values,
-                        as_stream(stream), nullptr);
+                        as_stream(stream), nullptr, nullptr);
+    });
+}
+
+extern "C" int skg_h1_assemble_affine_host(const skg_pattern *pat, const double *d_p, int64_t npts,
+                                           const int32_t *d_t, int32_t nodes, int64_t ne, const int32_t *d_dofs,
+                                           int32_t nq, const double *h_X, const double *h_W, int32_t coef_kind,
+                                           const double *d_coef, int32_t precision, double *d_values,
+                                           double *h_values, void *stream) {
+    return guarded([&] {
+        (void)d_dofs;
+        require(h_values != nullptr, "host output is NULL");
+        affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values,
+                        as_stream(stream), nullptr, h_values);
     });
 }
 
@@ -1121,7 +1144,7 @@ extern "C" int skg_h1_assemble_affine_profiled(const skg_pattern *pat, const dou
         try {
             for (auto &e : ev) SKG_CUDA(cudaEventCreate(&e));
             affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values, s,
-                            ev);
+                            ev, nullptr);
             SKG_CUDA(cudaEventSynchronize(ev[2]));
             SKG_CUDA(cudaEventElapsedTime(&h_kernel_ms[0], ev[0], ev[1]));
             SKG_CUDA(cudaEventElapsedTime(&h_kernel_ms[1], ev[1], ev[2]));

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "skfem_gb300.h"
 
@@ -160,6 +161,12 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *b, int n, int32_t 
 }  // namespace skg
 
 namespace skg {
+// Rows [lo, hi) a row-pass launch handles (groups outside are skipped); the
+// host-output paths launch the row pass in row chunks to overlap copies.
+struct RowRange {
+    int32_t lo = 0, hi = INT32_MAX;
+};
+
 constexpr int kGroupSlotsSmall = 768;
 constexpr int kGroupSlotsLarge = 2048;
 }  // namespace skg
@@ -182,6 +189,8 @@ struct skg_pattern {
     // (first row, end row).
     int32_t n_groups_small = 0, n_groups_large = 0;
     skg::DevBuf<int2> groups_small, groups_large;
+    // host copy of indptr, made on first use by the host-output paths
+    std::vector<int32_t> h_indptr;
     // Incidence records (col_local <= 12 and every row shorter than 256):
     // one int4 per incidence in `inc` order, x = e*row_local + i and the
     // bytes of y, z, w = column offset within the row of each local column.

@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <mutex>
+
 #include "skg_common.cuh"
 
 namespace skg {
@@ -428,3 +430,48 @@ extern "C" int skg_pattern_row_groups(const skg_pattern *p, int32_t *max_row_len
         *max_row_len = p->max_row_len;
     });
 }
+
+namespace skg {
+
+// Row boundaries of n_chunks row ranges with about equal slot counts (the
+// host copy of indptr is made once per pattern).
+void host_output_chunks(const skg_pattern *pat, int n_chunks, std::vector<int32_t> &rows, cudaStream_t s) {
+    skg_pattern *p = const_cast<skg_pattern *>(pat);
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if ((int64_t)p->h_indptr.size() != p->n_rows + 1) {
+            std::vector<int32_t> h((size_t)p->n_rows + 1);
+            SKG_CUDA(cudaMemcpyAsync(h.data(), p->indptr.get(), h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            SKG_CUDA(cudaStreamSynchronize(s));
+            p->h_indptr.swap(h);
+        }
+    }
+    const std::vector<int32_t> &hp = p->h_indptr;
+    const int64_t nnz = hp.back();
+    rows.assign(1, 0);
+    for (int k = 1; k <= n_chunks; ++k) {
+        int32_t r = (int32_t)p->n_rows;
+        if (k < n_chunks) {
+            const int64_t target = nnz * k / n_chunks;
+            r = (int32_t)(std::lower_bound(hp.begin(), hp.end(), (int32_t)target) - hp.begin());
+            if (r > p->n_rows) r = (int32_t)p->n_rows;
+        }
+        if (r > rows.back()) rows.push_back(r);
+    }
+    if (rows.size() == 1) rows.push_back((int32_t)p->n_rows);
+}
+
+// Non-blocking copy stream per device for the host-output paths.
+cudaStream_t copy_stream() {
+    static std::mutex mu;
+    static cudaStream_t streams[64] = {};
+    int dev = 0;
+    SKG_CUDA(cudaGetDevice(&dev));
+    require(dev >= 0 && dev < 64, "device index out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!streams[dev]) SKG_CUDA(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+    return streams[dev];
+}
+
+}  // namespace skg

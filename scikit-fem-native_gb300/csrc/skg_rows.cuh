@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
                                                            const int32_t *__restrict__ indptr,
                                                            const int32_t *__restrict__ inc_ptr,
                                                            const int4 *__restrict__ rec, const double *__restrict__ Ke,
-                                                           double *__restrict__ values) {
+                                                           double *__restrict__ values, RowRange rr) {
     static_assert(N % 2 == 0 && N <= 12, "rows are loaded as 16-byte pairs, at most 12 columns");
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
     if (gi >= n_groups) return;
     double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
     const int2 grp = groups[gi];
+    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.0;
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
 
 template <int N, int SLOTS, int P>
 inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, const double *Ke,
-                            double *values, cudaStream_t s) {
+                            double *values, cudaStream_t s, RowRange rr = RowRange()) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
@@ -96,16 +97,59 @@ inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern 
                                       (int)smem));
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_ke<N, SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
-                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values);
+                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values, rr);
     SKG_LAUNCH_CHECK("rows_ke");
 }
 
 // Sums element matrices Ke (E, N, N) into the CSR values of a pattern with
 // row groups (pat->max_row_len > 0, square N x N element blocks).
 template <int N>
-inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
-    launch_ke_class<N, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Ke, values, s);
-    launch_ke_class<N, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Ke, values, s);
+inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s,
+                             RowRange rr = RowRange()) {
+    launch_ke_class<N, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Ke, values, s, rr);
+    launch_ke_class<N, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Ke, values, s, rr);
+}
+
+// Runs a row pass fn(RowRange) over all rows, or, with a host output,
+// in row chunks of about equal slot counts: after each chunk's kernels the
+// chunk's value range is copied to the page-locked h_values on a second
+// stream while the next chunk runs.  A group that starts in one chunk and
+// ends in the next is written by the first chunk's launch, before the copy of
+// the second chunk's range, so every copied range is complete.  The caller's
+// stream waits for the copies at the end.
+void host_output_chunks(const skg_pattern *pat, int n_chunks, std::vector<int32_t> &rows, cudaStream_t s);
+cudaStream_t copy_stream();
+
+template <class F>
+void run_row_pass(const skg_pattern *pat, double *d_values, double *h_values, cudaStream_t s, F &&fn) {
+    if (!h_values) {
+        fn(RowRange());
+        return;
+    }
+    std::vector<int32_t> rows;
+    host_output_chunks(pat, 8, rows, s);
+    cudaStream_t cs = copy_stream();
+    const std::vector<int32_t> &hp = pat->h_indptr;
+    std::vector<cudaEvent_t> evs;
+    for (size_t k = 0; k + 1 < rows.size(); ++k) {
+        const int32_t r0 = rows[k], r1 = rows[k + 1];
+        fn(RowRange{r0, r1});
+        cudaEvent_t ev;
+        SKG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        evs.push_back(ev);
+        SKG_CUDA(cudaEventRecord(ev, s));
+        SKG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+        const size_t n = (size_t)(hp[r1] - hp[r0]);
+        if (n)
+            SKG_CUDA(cudaMemcpyAsync(h_values + hp[r0], d_values + hp[r0], n * sizeof(double), cudaMemcpyDeviceToHost,
+                                     cs));
+    }
+    cudaEvent_t done;
+    SKG_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    evs.push_back(done);
+    SKG_CUDA(cudaEventRecord(done, cs));
+    SKG_CUDA(cudaStreamWaitEvent(s, done, 0));
+    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once complete
 }
 
 }  // namespace skg

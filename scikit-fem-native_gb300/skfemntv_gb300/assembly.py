@@ -203,6 +203,10 @@ class _MatrixTarget:
             warnings.simplefilter("ignore", UserWarning)  # torch marks sparse CSR as beta
             return torch.sparse_csr_tensor(crow, col, self.d_values[: self.pattern.nnz], size=self.matrix.shape)
 
+    def pinned_ptr(self):
+        """Pointer to the page-locked buffer behind the host matrix (copy target)."""
+        return ctypes.c_void_p(self._pinned.data_ptr())
+
     def finish_direct(self):
         import torch
 
@@ -255,9 +259,14 @@ class NativeBilinearForm:
             if coef is None:
                 keep = dev.to_device(fast, np.float64)
                 coef = dev.ptr(keep)
-        call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-             dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
-             dev.hptr(b.W), 0, coef, prec, out, dev.stream_ptr())
+        if host:  # values to the host matrix: copies overlap the row pass
+            call("skg_h1_assemble_affine_host", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.hptr(b.W), 0, coef, prec, dev.ptr(self.target.d_values), out, dev.stream_ptr())
+        else:
+            call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.hptr(b.W), 0, coef, prec, out, dev.stream_ptr())
         return keep
 
     def assemble_device(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
@@ -293,9 +302,8 @@ class NativeBilinearForm:
         """Host CSR matrix (reused between calls, as the reference's).  On the fused
         path the kernels write the values straight into its page-locked buffer."""
         fast = self._affine_coefficient(value, gradient, symmetric_gradient, divergence)
-        out = self.target.host_out() if fast is not None else None
-        if out is not None:
-            self._affine(fast, _precision(precision), out, host=True)
+        if fast is not None:
+            self._affine(fast, _precision(precision), self.target.pinned_ptr(), host=True)
             return self.target.finish_direct()
         self.assemble_device(value=value, gradient=gradient, symmetric_gradient=symmetric_gradient,
                              divergence=divergence, precision=precision)
@@ -345,12 +353,15 @@ class NativeTensorForm:
                     keep = self._staging.upload(arr)
                     coef = dev.ptr(keep)
         if coef is not None:
-            direct = out is not None
+            if out is not None:  # values to the host matrix: copies overlap the row pass
+                call("skg_h1_assemble_affine_host", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                     dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                     dev.hptr(b.W), kind, coef, prec, dev.ptr(self.target.d_values), out, dev.stream_ptr())
+                return True
             call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
                  dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
-                 dev.hptr(b.W), kind, coef, prec, out if direct else dev.ptr(self.target.d_values),
-                 dev.stream_ptr())
-            return direct
+                 dev.hptr(b.W), kind, coef, prec, dev.ptr(self.target.d_values), dev.stream_ptr())
+            return False
         if prec != SKG_FP64:
             raise UnsupportedNativeForm("split precision is available on the affine tensor path")
         T = anisotropic_tensor(raw, E, Q)
@@ -370,7 +381,7 @@ class NativeTensorForm:
         """Host CSR matrix.  ``copy=True`` (the reference's behaviour,
         bilinear_form.py:367) returns an independent matrix; ``copy=False`` the
         reused one whose page-locked values the fused kernels write directly."""
-        direct = self._run(raw, precision, None, 2, self.target.host_out())
+        direct = self._run(raw, precision, None, 2, self.target.pinned_ptr())
         m = self.target.finish_direct() if direct else self.target.download()
         return self.target.copy_matrix() if copy else m
 
