@@ -111,39 +111,18 @@ __device__ __forceinline__ void nh_plain_row(const double *__restrict__ R, int a
     rr = PV[0] * ga[0] + PV[1] * ga[1] + PV[2] * ga[2];
 }
 
-// Row of element e from the surrogate record (FP32).
+// Row of element e from the surrogate record (FP32): precomputed tangent row
+// and residual entry.
 __device__ __forceinline__ void nh_surrogate_row(const float *__restrict__ R, int a, int i, float val[12],
                                                  float &rr) {
-    float gall[12];
-    const float4 *G4 = reinterpret_cast<const float4 *>(R + 84);
+    const int l = a * 3 + i;
+    const float4 *src = reinterpret_cast<const float4 *>(R + 12 * l);
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        const float4 v = __ldg(G4 + q);
-        gall[4 * q] = v.x; gall[4 * q + 1] = v.y; gall[4 * q + 2] = v.z; gall[4 * q + 3] = v.w;
+        const float4 v = __ldg(src + q);
+        val[4 * q] = v.x; val[4 * q + 1] = v.y; val[4 * q + 2] = v.z; val[4 * q + 3] = v.w;
     }
-    float Ai[28];
-    const float4 *A4 = reinterpret_cast<const float4 *>(R + 28 * i);
-#pragma unroll
-    for (int q = 0; q < 7; ++q) {
-        const float4 v = __ldg(A4 + q);
-        Ai[4 * q] = v.x; Ai[4 * q + 1] = v.y; Ai[4 * q + 2] = v.z; Ai[4 * q + 3] = v.w;
-    }
-    float ga[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        ga[j] = a == 0 ? gall[j] : a == 1 ? gall[3 + j] : a == 2 ? gall[6 + j] : gall[9 + j];
-    }
-    // w_kL = sum_J g_a,J (V A)_iJkL
-    float w[9];
-#pragma unroll
-    for (int kl = 0; kl < 9; ++kl) w[kl] = ga[0] * Ai[kl] + ga[1] * Ai[9 + kl] + ga[2] * Ai[18 + kl];
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-            val[b * 3 + k] = w[k * 3] * gall[b * 3] + w[k * 3 + 1] * gall[b * 3 + 1] + w[k * 3 + 2] * gall[b * 3 + 2];
-    const float *PV = R + 96 + 3 * i;
-    rr = __ldg(PV) * ga[0] + __ldg(PV + 1) * ga[1] + __ldg(PV + 2) * ga[2];
+    rr = __ldg(R + 144 + l);
 }
 
 __device__ __forceinline__ df64 df_split(double v) {

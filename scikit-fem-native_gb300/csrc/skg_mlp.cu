@@ -609,9 +609,24 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
                 }
         Ai[27] = 0.f;
         if constexpr (FUSED) {
+            // tangent rows (a, i) of the element matrix, V folded in
 #pragma unroll
-            for (int q = 0; q < 7; ++q)
-                out[7 * i + q] = make_float4(Vf * Ai[4 * q], Vf * Ai[4 * q + 1], Vf * Ai[4 * q + 2], Vf * Ai[4 * q + 3]);
+            for (int a = 0; a < 4; ++a) {
+                float w[9];
+#pragma unroll
+                for (int kL = 0; kL < 9; ++kL)
+                    w[kL] = Vf * (ga[a][0] * Ai[kL] + ga[a][1] * Ai[9 + kL] + ga[a][2] * Ai[18 + kL]);
+                float row[12];
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        row[b * 3 + k] = w[k * 3] * ga[b][0] + w[k * 3 + 1] * ga[b][1] + w[k * 3 + 2] * ga[b][2];
+                float4 *dst = out + (a * 3 + i) * 3;
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    dst[q] = make_float4(row[4 * q], row[4 * q + 1], row[4 * q + 2], row[4 * q + 3]);
+            }
         } else if (Ke) {
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
@@ -631,12 +646,15 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
     }
     if (!tail) return true;
     if constexpr (FUSED) {
-        out[21] = make_float4(ga[0][0], ga[0][1], ga[0][2], ga[1][0]);
-        out[22] = make_float4(ga[1][1], ga[1][2], ga[2][0], ga[2][1]);
-        out[23] = make_float4(ga[2][2], ga[3][0], ga[3][1], ga[3][2]);
-        out[24] = make_float4(Vf * Pm[0], Vf * Pm[1], Vf * Pm[2], Vf * Pm[3]);
-        out[25] = make_float4(Vf * Pm[4], Vf * Pm[5], Vf * Pm[6], Vf * Pm[7]);
-        out[26] = make_float4(Vf * Pm[8], 0.f, 0.f, 0.f);
+        // residual r_(a,c) = V sum_j P_cj g_a,j
+        float r[12];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                r[a * 3 + c] = Vf * (Pm[c * 3] * ga[a][0] + Pm[c * 3 + 1] * ga[a][1] + Pm[c * 3 + 2] * ga[a][2]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) out[36 + q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
     } else if (re) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)

@@ -8,10 +8,9 @@
 // so that K_(a,i),(b,k) = mu V d_ik g_a.g_b + c2 V h_b,i h_a,k + lambda V h_a,i h_b,k
 // and r_(a,i) = sum_j (V P)_ij g_a,j.
 //
-// Surrogate record (FP32, kNhRecF floats per element):
-//   [0, 84)  V A_iJkL, row i at 28 i (27 entries + pad), A the tangent tensor
-//   [84, 96) g_a                 [96, 105) V P
-// so that K_(a,i),(b,k) = sum_JL g_a,J (V A)_iJkL g_b,L.
+// Surrogate record (FP32, kNhRecF floats per element): the element tangent
+// rows [12 (3a + i) .. +12) = K_(a,i),(b,k) = sum_JL g_a,J (V A)_iJkL g_b,L,
+// then [144, 156) the residual entries r_(a,i) = sum_j (V P)_ij g_a,j.
 #pragma once
 
 #include "skg_common.cuh"
@@ -21,7 +20,7 @@
 namespace skg {
 
 constexpr int kNhRecD = 36;
-constexpr int kNhRecF = 108;
+constexpr int kNhRecF = 156;
 
 __device__ __forceinline__ void write_plain_record(const NhGeom &g, const NhLaw &L, double mu, double lmbda,
                                                    double *__restrict__ r) {
