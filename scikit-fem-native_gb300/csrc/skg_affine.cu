@@ -189,7 +189,8 @@ __host__ __device__ constexpr int tri10(int a, int b) {  // packed upper triangl
     return a * 10 - a * (a - 1) / 2 + (b - a);
 }
 
-__global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                           const double *__restrict__ p, int64_t npts,
                                                            const int32_t *__restrict__ t, int coef_kind,
                                                            const double *__restrict__ coef,
                                                            const double *__restrict__ Tg, double *__restrict__ Ke) {
@@ -197,9 +198,9 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, const dou
     __shared__ double stage[kKeBlock * kKeChunk];
     for (int i = threadIdx.x; i < 400; i += blockDim.x) Ts[i] = Tg[i];
     __syncthreads();
-    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * kKeBlock;
     const int64_t e = e0 + threadIdx.x;
-    const bool valid = e < ne;
+    const bool valid = e < e_end;
     double g[16];
     bool sym = true;
     if (valid) {
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, const dou
 #pragma unroll
             for (int bb = a; bb < 10; ++bb) U[tri10(a, bb)] = entry(a, bb);
     }
-    const int nvalid = (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock);
+    const int nvalid = (int)(e_end - e0 < kKeBlock ? e_end - e0 : kKeBlock);
     double *st = stage + threadIdx.x * kKeChunk;
 #pragma unroll
     for (int r = 0; r < 100 / kKeChunk; ++r) {
@@ -624,7 +625,7 @@ template <int N, int MODE, int SLOTS, int P, bool EXACT>
 __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
     int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
     const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec, const void *__restrict__ Gv,
-    const double *__restrict__ Tg, const int *__restrict__ s_ptr, double *__restrict__ values, RowRange rr) {
+    const double *__restrict__ Tg, const int *__restrict__ s_ptr, double *__restrict__ values) {
     using GT = typename std::conditional<MODE == MODE_FP64, double, df64>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     double *Td = reinterpret_cast<double *>(smem);
@@ -646,7 +647,6 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_group(
     double *accd = reinterpret_cast<double *>(warp_area + (size_t)warp * SLOTS * 8);
     df64 *accf = reinterpret_cast<df64 *>(accd);
     const int2 grp = groups[gi];
-    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) {
@@ -786,14 +786,13 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
                                                               const int4 *__restrict__ rec,
                                                               const float2 *__restrict__ Ke,
                                                               const int *__restrict__ s_ptr,
-                                                              double *__restrict__ values, RowRange rr) {
+                                                              double *__restrict__ values) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gi = blockIdx.x * kRowWarps + warp;
     if (gi >= n_groups) return;
     df64 *acc = reinterpret_cast<df64 *>(smem + (size_t)warp * SLOTS * 8);
     const int2 grp = groups[gi];
-    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) acc[j] = df64{0.f, 0.f};
@@ -856,14 +855,14 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
 
 template <int SLOTS, int P>
 void launch_ke_df_class(int n_groups, const int2 *groups, const skg_pattern *pat, const float2 *Ke, const int *s_ptr,
-                        double *values, cudaStream_t s, RowRange rr) {
+                        double *values, cudaStream_t s) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
         SKG_CUDA(cudaFuncSetAttribute(k_rows_ke_df<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_ke_df<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
-                                                              pat->rec.get(), Ke, s_ptr, values, rr);
+                                                              pat->rec.get(), Ke, s_ptr, values);
     SKG_LAUNCH_CHECK("rows_ke_df");
 }
 
@@ -932,7 +931,7 @@ void affine_table(int nodes, int nq, const double *X, const double *W, std::vect
 
 template <int N, int MODE, int SLOTS, int P, bool EXACT>
 void launch_group_class(int n_groups, const int2 *groups, const skg_pattern *pat, const void *G, const double *Tg,
-                        const int *s_ptr, double *values, cudaStream_t s, RowRange rr) {
+                        const int *s_ptr, double *values, cudaStream_t s) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)N * N * 4 * 8 + (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
@@ -941,17 +940,21 @@ void launch_group_class(int n_groups, const int2 *groups, const skg_pattern *pat
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_group<N, MODE, SLOTS, P, EXACT><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
                                                                       pat->inc_ptr.get(), pat->rec.get(), G, Tg, s_ptr,
-                                                                      values, rr);
+                                                                      values);
     SKG_LAUNCH_CHECK("rows_group");
 }
 
 template <int N, int MODE, bool EXACT = false>
 void launch_rows_groups(const skg_pattern *pat, const void *G, const double *Tg, const int *s_ptr, double *values,
-                        cudaStream_t s, RowRange rr = RowRange()) {
-    launch_group_class<N, MODE, kGroupSlotsSmall, 1, EXACT>(pat->n_groups_small, pat->groups_small.get(), pat, G, Tg,
-                                                            s_ptr, values, s, rr);
-    launch_group_class<N, MODE, kGroupSlotsLarge, 2, EXACT>(pat->n_groups_large, pat->groups_large.get(), pat, G, Tg,
-                                                            s_ptr, values, s, rr);
+                        cudaStream_t s, const GroupSet &gs) {
+    launch_group_class<N, MODE, kGroupSlotsSmall, 1, EXACT>(gs.n_small, gs.small, pat, G, Tg, s_ptr, values, s);
+    launch_group_class<N, MODE, kGroupSlotsLarge, 2, EXACT>(gs.n_large, gs.large, pat, G, Tg, s_ptr, values, s);
+}
+
+template <int N, int MODE, bool EXACT = false>
+void launch_rows_groups(const skg_pattern *pat, const void *G, const double *Tg, const int *s_ptr, double *values,
+                        cudaStream_t s) {
+    launch_rows_groups<N, MODE, EXACT>(pat, G, Tg, s_ptr, values, s, all_groups(pat));
 }
 
 // True when the caller's rule reproduces the exact P2 table (30 T integer).
@@ -1015,11 +1018,9 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_CUDA(cudaStreamSynchronize(s));
         if (h_misc[1] == 0 && h_misc[0] != INT_MIN) {
             if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-            run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) {
-                launch_ke_df_class<kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Kf.get(),
-                                                        misc.get(), d_values, s, rr);
-                launch_ke_df_class<kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Kf.get(),
-                                                        misc.get(), d_values, s, rr);
+            run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs) {
+                launch_ke_df_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kf.get(), misc.get(), d_values, s);
+                launch_ke_df_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kf.get(), misc.get(), d_values, s);
             });
             if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
             return;
@@ -1045,15 +1046,18 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     }
     if (mode == MODE_FP64 && nodes == 10 && blocked) {
         // FP64 P2: element matrices, then row sums
+        // (with a host output the two passes interleave, see run_passes)
         DevBuf<double> Ke((size_t)ne * 100, s);
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
-        if (ne) {
-            k_elem_ke_fp64<<<grid_for(ne, kKeBlock), kKeBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
-                                                                       Tg.get(), Ke.get());
-            SKG_LAUNCH_CHECK("elem_ke_fp64");
-        }
-        if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-        run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) { add_element_rows<10>(pat, Ke.get(), d_values, s, rr); });
+        run_passes(
+            pat, ne, d_values, h_values, s,
+            [&](int64_t e0, int64_t e1) {
+                k_elem_ke_fp64<<<grid_for(e1 - e0, kKeBlock), kKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t, coef_kind,
+                                                                             d_coef, Tg.get(), Ke.get());
+                SKG_LAUNCH_CHECK("elem_ke_fp64");
+                if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
+            },
+            [&](const GroupSet &gs) { add_element_rows<10>(pat, Ke.get(), d_values, s, gs); });
         if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
         return;
     }
@@ -1081,8 +1085,8 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
     } else {
         const int *sp_ptr = misc.get();
-        run_row_pass(pat, d_values, h_values, s, [&](RowRange rr) {
-#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, rr)
+        run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs) {
+#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, gs)
             if (nodes == 4) {
                 if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
                 else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
@@ -1090,7 +1094,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             } else {
                 if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
                 else if (mode == MODE_SPLIT) {
-                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, rr);
+                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, gs);
                     else SKG_ROWS(10, MODE_SPLIT);
                 } else {
                     SKG_ROWS(10, MODE_DF64);

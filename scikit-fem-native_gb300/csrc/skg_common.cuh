@@ -161,14 +161,19 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *b, int n, int32_t 
 }  // namespace skg
 
 namespace skg {
-// Rows [lo, hi) a row-pass launch handles (groups outside are skipped); the
-// host-output paths launch the row pass in row chunks to overlap copies.
-struct RowRange {
-    int32_t lo = 0, hi = INT32_MAX;
+// The row groups one row-pass launch handles, per class (see skg_pattern).
+struct GroupSet {
+    int n_small = 0;
+    const int2 *small = nullptr;
+    int n_large = 0;
+    const int2 *large = nullptr;
 };
 
 constexpr int kGroupSlotsSmall = 768;
 constexpr int kGroupSlotsLarge = 2048;
+// Row chunks of the host-output paths (values copied to host memory chunk by
+// chunk while later chunks are computed).
+constexpr int kHostChunks = 16;
 }  // namespace skg
 
 // Pattern handle (defined here so every translation unit sees the layout).
@@ -189,8 +194,15 @@ struct skg_pattern {
     // (first row, end row).
     int32_t n_groups_small = 0, n_groups_large = 0;
     skg::DevBuf<int2> groups_small, groups_large;
-    // host copy of indptr, made on first use by the host-output paths
-    std::vector<int32_t> h_indptr;
+    // Host-output row chunks: up to kHostChunks row ranges of about equal
+    // slot counts whose boundaries are group starts.  Chunk c covers rows
+    // [hc_row[c], hc_row[c+1]) = slots [hc_slot[c], hc_slot[c+1]); its rows
+    // reference elements below hc_ready[c] only.  The same groups as above,
+    // ordered by chunk (then by first element), are hc_small / hc_large, and
+    // chunk c's groups of a class start at hc_small_off[c] / hc_large_off[c].
+    std::vector<int32_t> hc_row, hc_slot, hc_small_off, hc_large_off;
+    std::vector<int64_t> hc_ready;
+    skg::DevBuf<int2> hc_small, hc_large;
     // Incidence records (col_local <= 12 and every row shorter than 256):
     // one int4 per incidence in `inc` order, x = e*row_local + i and the
     // bytes of y, z, w = column offset within the row of each local column.

@@ -213,12 +213,14 @@ __global__ void k_records(int64_t n_rows, const int32_t *__restrict__ indptr, co
 
 }  // namespace
 
-// First element referenced by each row (rows without incidences: INT_MAX).
-__global__ void k_first_element(int64_t n_rows, const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
-                                int32_t row_local, int32_t *__restrict__ first) {
+// First and last element referenced by each row (incidences are in ascending
+// element order; rows without incidences: INT_MAX and -1).
+__global__ void k_element_span(int64_t n_rows, const int32_t *__restrict__ inc_ptr, const int32_t *__restrict__ inc,
+                               int32_t row_local, int2 *__restrict__ span) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_rows) return;
-    first[r] = inc_ptr[r] < inc_ptr[r + 1] ? inc[inc_ptr[r]] / row_local : INT_MAX;
+    const int32_t i0 = inc_ptr[r], i1 = inc_ptr[r + 1];
+    span[r] = i0 < i1 ? make_int2(inc[i0] / row_local, inc[i1 - 1] / row_local) : make_int2(INT_MAX, -1);
 }
 
 // Incidence records for the warp-per-row assembly kernels; skipped when the
@@ -243,7 +245,7 @@ void build_records(skg_pattern *p, cudaStream_t s) {
     // fit (long rows), it is re-formed as up to 16 rows within
     // kGroupSlotsLarge / 2 slots, served by two threads per row with one
     // accumulator copy each.
-    std::vector<int2> small, large;
+    std::vector<int2> small, large, all;  // `all`: every group, in row order
     int64_t r = 0;
     while (r < p->n_rows) {
         const int64_t r0 = r;
@@ -258,44 +260,84 @@ void build_records(skg_pattern *p, cudaStream_t s) {
             if (r1 == r0) r1 = r0 + 1;  // single row above the budget (cannot happen below 256 columns)
             large.push_back(make_int2((int)r0, (int)r1));
         }
+        all.push_back(make_int2((int)r0, (int)r1));
         r = r1;
+    }
+    std::vector<int2> span(p->n_rows);
+    {
+        DevBuf<int2> d_span(p->n_rows, s);
+        k_element_span<<<grid_for(p->n_rows, 256), 256, 0, s>>>(p->n_rows, p->inc_ptr.get(), p->inc.get(),
+                                                              p->row_local, d_span.get());
+        SKG_LAUNCH_CHECK("element_span");
+        SKG_CUDA(cudaMemcpyAsync(span.data(), d_span.get(), span.size() * 8, cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
     }
     // Order the groups by the first element they reference, so that groups
     // running at the same time touch a compact band of elements (their
     // per-element data stays in L2).  Each group still owns a contiguous
     // slot range, so the output writes stay coalesced.
-    {
-        DevBuf<int32_t> first(p->n_rows, s);
-        k_first_element<<<grid_for(p->n_rows, 256), 256, 0, s>>>(p->n_rows, p->inc_ptr.get(), p->inc.get(),
-                                                               p->row_local, first.get());
-        SKG_LAUNCH_CHECK("first_element");
-        std::vector<int32_t> fe(p->n_rows);
-        SKG_CUDA(cudaMemcpyAsync(fe.data(), first.get(), fe.size() * 4, cudaMemcpyDeviceToHost, s));
-        SKG_CUDA(cudaStreamSynchronize(s));
-        auto key = [&](const int2 &g) {
-            int32_t m = INT_MAX;
-            for (int32_t rr = g.x; rr < g.y; ++rr) m = std::min(m, fe[rr]);
-            return m;
-        };
-        for (auto *vec : {&small, &large}) {
-            std::vector<std::pair<int32_t, int2>> kv;
-            kv.reserve(vec->size());
-            for (const auto &g : *vec) kv.emplace_back(key(g), g);
-            std::stable_sort(kv.begin(), kv.end(),
-                             [](const std::pair<int32_t, int2> &x, const std::pair<int32_t, int2> &y) {
-                                 return x.first < y.first;
-                             });
-            for (size_t i = 0; i < kv.size(); ++i) (*vec)[i] = kv[i].second;
-        }
+    auto first_element = [&](const int2 &g) {
+        int32_t m = INT_MAX;
+        for (int32_t q = g.x; q < g.y; ++q) m = std::min(m, span[q].x);
+        return m;
+    };
+    auto sort_by = [](std::vector<int2> &vec, const std::vector<int64_t> &key) {
+        std::vector<size_t> order(vec.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key[a] < key[b]; });
+        std::vector<int2> out(vec.size());
+        for (size_t i = 0; i < order.size(); ++i) out[i] = vec[order[i]];
+        vec.swap(out);
+    };
+    for (auto *vec : {&small, &large}) {
+        std::vector<int64_t> key(vec->size());
+        for (size_t i = 0; i < vec->size(); ++i) key[i] = first_element((*vec)[i]);
+        sort_by(*vec, key);
     }
+    // Host-output chunks: boundaries at group starts near equal slot counts.
+    const int64_t nnz = ip[p->n_rows];
+    p->hc_row.assign(1, 0);
+    for (int k = 1; k < kHostChunks; ++k) {
+        const int64_t target = nnz * k / kHostChunks;
+        const auto it = std::lower_bound(all.begin(), all.end(), target,
+                                         [&](const int2 &g, int64_t t) { return (int64_t)ip[g.x] < t; });
+        if (it != all.end() && it->x > p->hc_row.back()) p->hc_row.push_back(it->x);
+    }
+    p->hc_row.push_back((int32_t)p->n_rows);
+    const int n_chunks = (int)p->hc_row.size() - 1;
+    p->hc_slot.resize(n_chunks + 1);
+    for (int c = 0; c <= n_chunks; ++c) p->hc_slot[c] = ip[p->hc_row[c]];
+    p->hc_ready.assign(n_chunks, 0);
+    auto chunk_of = [&](int32_t row) {
+        return (int)(std::upper_bound(p->hc_row.begin(), p->hc_row.end(), row) - p->hc_row.begin()) - 1;
+    };
+    for (int c = 0; c < n_chunks; ++c)
+        for (int32_t q = p->hc_row[c]; q < p->hc_row[c + 1]; ++q)
+            p->hc_ready[c] = std::max(p->hc_ready[c], (int64_t)span[q].y + 1);
+    std::vector<int2> hc_small = small, hc_large = large;
+    for (auto *vec : {&hc_small, &hc_large}) {
+        std::vector<int64_t> key(vec->size());
+        for (size_t i = 0; i < vec->size(); ++i) key[i] = chunk_of((*vec)[i].x);
+        sort_by(*vec, key);  // stable: first-element order within a chunk
+    }
+    auto offsets = [&](const std::vector<int2> &vec, std::vector<int32_t> &off) {
+        off.assign(n_chunks + 1, 0);
+        for (const int2 &g : vec) ++off[chunk_of(g.x) + 1];
+        for (int c = 0; c < n_chunks; ++c) off[c + 1] += off[c];
+    };
+    offsets(hc_small, p->hc_small_off);
+    offsets(hc_large, p->hc_large_off);
+    auto upload = [&](const std::vector<int2> &vec, DevBuf<int2> &dst) {
+        dst = DevBuf<int2>::owned(vec.size());
+        if (!vec.empty())
+            SKG_CUDA(cudaMemcpyAsync(dst.get(), vec.data(), vec.size() * 8, cudaMemcpyHostToDevice, s));
+    };
     p->n_groups_small = (int32_t)small.size();
     p->n_groups_large = (int32_t)large.size();
-    p->groups_small = DevBuf<int2>::owned(small.size());
-    p->groups_large = DevBuf<int2>::owned(large.size());
-    if (!small.empty())
-        SKG_CUDA(cudaMemcpyAsync(p->groups_small.get(), small.data(), small.size() * 8, cudaMemcpyHostToDevice, s));
-    if (!large.empty())
-        SKG_CUDA(cudaMemcpyAsync(p->groups_large.get(), large.data(), large.size() * 8, cudaMemcpyHostToDevice, s));
+    upload(small, p->groups_small);
+    upload(large, p->groups_large);
+    upload(hc_small, p->hc_small);
+    upload(hc_large, p->hc_large);
     SKG_CUDA(cudaStreamSynchronize(s));
     p->max_row_len = longest;
 }
@@ -432,35 +474,6 @@ extern "C" int skg_pattern_row_groups(const skg_pattern *p, int32_t *max_row_len
 }
 
 namespace skg {
-
-// Row boundaries of n_chunks row ranges with about equal slot counts (the
-// host copy of indptr is made once per pattern).
-void host_output_chunks(const skg_pattern *pat, int n_chunks, std::vector<int32_t> &rows, cudaStream_t s) {
-    skg_pattern *p = const_cast<skg_pattern *>(pat);
-    static std::mutex mu;
-    {
-        std::lock_guard<std::mutex> lock(mu);
-        if ((int64_t)p->h_indptr.size() != p->n_rows + 1) {
-            std::vector<int32_t> h((size_t)p->n_rows + 1);
-            SKG_CUDA(cudaMemcpyAsync(h.data(), p->indptr.get(), h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-            SKG_CUDA(cudaStreamSynchronize(s));
-            p->h_indptr.swap(h);
-        }
-    }
-    const std::vector<int32_t> &hp = p->h_indptr;
-    const int64_t nnz = hp.back();
-    rows.assign(1, 0);
-    for (int k = 1; k <= n_chunks; ++k) {
-        int32_t r = (int32_t)p->n_rows;
-        if (k < n_chunks) {
-            const int64_t target = nnz * k / n_chunks;
-            r = (int32_t)(std::lower_bound(hp.begin(), hp.end(), (int32_t)target) - hp.begin());
-            if (r > p->n_rows) r = (int32_t)p->n_rows;
-        }
-        if (r > rows.back()) rows.push_back(r);
-    }
-    if (rows.size() == 1) rows.push_back((int32_t)p->n_rows);
-}
 
 // Non-blocking copy stream per device for the host-output paths.
 cudaStream_t copy_stream() {

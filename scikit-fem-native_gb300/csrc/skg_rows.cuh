@@ -10,6 +10,9 @@
 // coalesced stores.  No atomics: bitwise reproducible.
 #pragma once
 
+#include <algorithm>
+#include <vector>
+
 #include "skg_common.cuh"
 
 namespace skg {
@@ -21,7 +24,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
                                                            const int32_t *__restrict__ indptr,
                                                            const int32_t *__restrict__ inc_ptr,
                                                            const int4 *__restrict__ rec, const double *__restrict__ Ke,
-                                                           double *__restrict__ values, RowRange rr) {
+                                                           double *__restrict__ values) {
     static_assert(N % 2 == 0 && N <= 12, "rows are loaded as 16-byte pairs, at most 12 columns");
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -29,7 +32,6 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
     if (gi >= n_groups) return;
     double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
     const int2 grp = groups[gi];
-    if (grp.x < rr.lo || grp.x >= rr.hi) return;  // row range of this launch
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.0;
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
 
 template <int N, int SLOTS, int P>
 inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, const double *Ke,
-                            double *values, cudaStream_t s, RowRange rr = RowRange()) {
+                            double *values, cudaStream_t s) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
@@ -97,59 +99,102 @@ inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern 
                                       (int)smem));
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_ke<N, SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
-                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values, rr);
+                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values);
     SKG_LAUNCH_CHECK("rows_ke");
+}
+
+inline GroupSet all_groups(const skg_pattern *pat) {
+    return GroupSet{pat->n_groups_small, pat->groups_small.get(), pat->n_groups_large, pat->groups_large.get()};
+}
+
+// Groups of host-output chunk c.
+inline GroupSet chunk_groups(const skg_pattern *pat, int c) {
+    const int s0 = pat->hc_small_off[c], l0 = pat->hc_large_off[c];
+    return GroupSet{pat->hc_small_off[c + 1] - s0, pat->hc_small.get() + s0, pat->hc_large_off[c + 1] - l0,
+                    pat->hc_large.get() + l0};
 }
 
 // Sums element matrices Ke (E, N, N) into the CSR values of a pattern with
 // row groups (pat->max_row_len > 0, square N x N element blocks).
 template <int N>
 inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s,
-                             RowRange rr = RowRange()) {
-    launch_ke_class<N, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, Ke, values, s, rr);
-    launch_ke_class<N, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, Ke, values, s, rr);
+                             const GroupSet &gs) {
+    launch_ke_class<N, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Ke, values, s);
+    launch_ke_class<N, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Ke, values, s);
 }
 
-// Runs a row pass fn(RowRange) over all rows, or, with a host output,
-// in row chunks of about equal slot counts: after each chunk's kernels the
-// chunk's value range is copied to the page-locked h_values on a second
-// stream while the next chunk runs.  A group that starts in one chunk and
-// ends in the next is written by the first chunk's launch, before the copy of
-// the second chunk's range, so every copied range is complete.  The caller's
-// stream waits for the copies at the end.
-void host_output_chunks(const skg_pattern *pat, int n_chunks, std::vector<int32_t> &rows, cudaStream_t s);
+template <int N>
+inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
+    add_element_rows<N>(pat, Ke, values, s, all_groups(pat));
+}
+
 cudaStream_t copy_stream();
 
-template <class F>
-void run_row_pass(const skg_pattern *pat, double *d_values, double *h_values, cudaStream_t s, F &&fn) {
+// Element pass and row pass of a pattern with row groups, with the values
+// optionally copied to the page-locked host array h_values.
+//
+// Device output: elem(0, ne) then rows(all groups).
+// Host output: the row chunks are taken in the order in which their elements
+// are complete (hc_ready); before a chunk's row pass, the element pass runs
+// up to its readiness bound (in steps of at least ne / kHostChunks elements,
+// so launches stay large), and after it the chunk's slot range is copied to
+// h_values on a second stream while the following element and row launches
+// run.  Every group lies inside one chunk, so each copied range is complete.
+// The caller's stream waits for the copies at the end.
+template <class FE, class FR>
+void run_passes(const skg_pattern *pat, int64_t ne, double *d_values, double *h_values, cudaStream_t s, FE &&elem,
+                FR &&rows) {
     if (!h_values) {
-        fn(RowRange());
+        if (ne) elem((int64_t)0, ne);
+        rows(all_groups(pat));
         return;
     }
-    std::vector<int32_t> rows;
-    host_output_chunks(pat, 8, rows, s);
+    const int n_chunks = (int)pat->hc_ready.size();
+    std::vector<int> order(n_chunks);
+    for (int c = 0; c < n_chunks; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pat->hc_ready[a] < pat->hc_ready[b]; });
+    const int64_t step = std::max<int64_t>(1, ne / kHostChunks);
     cudaStream_t cs = copy_stream();
-    const std::vector<int32_t> &hp = pat->h_indptr;
     std::vector<cudaEvent_t> evs;
-    for (size_t k = 0; k + 1 < rows.size(); ++k) {
-        const int32_t r0 = rows[k], r1 = rows[k + 1];
-        fn(RowRange{r0, r1});
+    auto event = [&]() {
         cudaEvent_t ev;
         SKG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         evs.push_back(ev);
-        SKG_CUDA(cudaEventRecord(ev, s));
-        SKG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
-        const size_t n = (size_t)(hp[r1] - hp[r0]);
-        if (n)
-            SKG_CUDA(cudaMemcpyAsync(h_values + hp[r0], d_values + hp[r0], n * sizeof(double), cudaMemcpyDeviceToHost,
-                                     cs));
+        return ev;
+    };
+    try {
+        int64_t done = 0;
+        for (int c : order) {
+            const int64_t need = std::min(ne, pat->hc_ready[c]);
+            if (need > done) {
+                const int64_t to = std::min(ne, std::max(need, done + step));
+                elem(done, to);
+                done = to;
+            }
+            rows(chunk_groups(pat, c));
+            const cudaEvent_t ev = event();
+            SKG_CUDA(cudaEventRecord(ev, s));
+            SKG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+            const int64_t s0 = pat->hc_slot[c], n = pat->hc_slot[c + 1] - s0;
+            if (n)
+                SKG_CUDA(cudaMemcpyAsync(h_values + s0, d_values + s0, (size_t)n * sizeof(double),
+                                         cudaMemcpyDeviceToHost, cs));
+        }
+        if (done < ne) elem(done, ne);  // elements no row references
+        const cudaEvent_t fin = event();
+        SKG_CUDA(cudaEventRecord(fin, cs));
+        SKG_CUDA(cudaStreamWaitEvent(s, fin, 0));
+    } catch (...) {
+        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+        throw;
     }
-    cudaEvent_t done;
-    SKG_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
-    evs.push_back(done);
-    SKG_CUDA(cudaEventRecord(done, cs));
-    SKG_CUDA(cudaStreamWaitEvent(s, done, 0));
     for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once complete
+}
+
+// Row pass alone (element data already computed), as run_passes.
+template <class FR>
+void run_row_pass(const skg_pattern *pat, double *d_values, double *h_values, cudaStream_t s, FR &&rows) {
+    run_passes(pat, 0, d_values, h_values, s, [](int64_t, int64_t) {}, rows);
 }
 
 }  // namespace skg

@@ -419,3 +419,30 @@ def test_cross_basis_assembly_matches_reference():
         cf.assemble_tensor("gradient", "gradient", np.ones((2, 2)))
     with pytest.raises(ValueError, match="row divergence requires"):
         cf.assemble("row_divergence", 1.0)
+
+
+@pytest.mark.parametrize("element", ["p1", "p2"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64_emulated", "split_fp32"])
+def test_host_output_matches_device(element, precision):
+    """The host-output path (element and row passes interleaved over row chunks,
+    each chunk's values copied while later chunks run) writes exactly the
+    values of the device path, on a mesh large enough for every chunk."""
+    from skfemntv_gb300.assembly import NativeTensorForm
+
+    g = load_golden("p2_aniso")
+    axis = np.linspace(0.0, 1.0, 17)
+    m = sk.MeshTet.init_tensor(axis, axis, axis)
+    if element == "p2":
+        b = sk.Basis(sk.MeshTet2.from_mesh(m), sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(g["X"], g["W"]))
+    else:
+        b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    M = np.random.default_rng(7).standard_normal((E, 3, 3))
+    A = M @ np.swapaxes(M, 1, 2) + 3.0 * np.eye(3)
+    Apub = np.broadcast_to(np.moveaxis(A, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    form = NativeTensorForm(b)
+    K = form.assemble(Apub, precision=precision, copy=True)
+    D = form.assemble_device(Apub, precision=precision)[:K.nnz].cpu().numpy()
+    assert np.array_equal(K.data.view(np.int64), D.view(np.int64))
+    K2 = form.assemble(2.0 * Apub, precision=precision, copy=False)  # reused page-locked values
+    assert np.allclose(K2.data, 2.0 * D, rtol=1e-14, atol=0)
