@@ -271,6 +271,21 @@ int skg_n1_assemble(const skg_pattern *pattern, const double *d_p, int64_t npts,
                     int32_t include_curl, int32_t precision, double *d_values,
                     void *stream);
 
+/* skg_n1_assemble with the values also written to the page-locked host
+ * array h_values (nnz), for callers that want the host CSR matrix
+ * (TetN1Assembler.assemble_maxwell returns one, hcurl_assembler.py:160-215).
+ * d_values (nnz, device) is the staging array.  On a row-grouped pattern the
+ * element and row passes run over row chunks and each chunk's values are
+ * copied while later chunks run; the stream has the host values once it
+ * reaches the end of the call's work. */
+int skg_n1_assemble_host(const skg_pattern *pattern, const double *d_p, int64_t npts,
+                         const int32_t *d_t, const int32_t *d_elem_edges,
+                         const int8_t *d_signs, int64_t n_elements, int32_t nq,
+                         const double *h_X, const double *h_W, const double *d_mass,
+                         const double *d_curl, int32_t include_mass,
+                         int32_t include_curl, int32_t precision, double *d_values,
+                         double *h_values, void *stream);
+
 /* Per-point coefficients: d_mass / d_curl (E, Q) (not NULL); the explicit
  * quadrature loop of integrate_tet_n1 (edge_topology.cpp:156-233) on the
  * mapped basis computed in the kernel. */
@@ -335,12 +350,24 @@ int skg_p1_energy_grad(const skg_pattern *vertex_incidence,
 /* benchmarks/skfem_neo_hookean.py:8-52: NativeLinearForm residual        */
 /* (linear_form_assembler.cpp:41-154) + NativeCrossBilinearForm tensor    */
 /* tangent (cross_bilinear_assembler.cpp:207-247).  Pattern: element DOFs */
-/* (E, 12), with CSR columns when the tangent is wanted.  u (N); outputs  */
-/* d_residual (N) and d_values (nnz), either may be NULL.                 */
+/* (E, 12), with CSR columns when the tangent is wanted.  u (N), in      */
+/* device memory or in host memory the device can read (then copied to   */
+/* the device first, coalesced); outputs d_residual (N) and d_values     */
+/* (nnz), either may be NULL.                                             */
 int skg_nh_assemble(const skg_pattern *pattern, const double *d_p, int64_t npts,
                     const int32_t *d_t, int64_t n_elements, const double *d_u,
                     double mu, double lmbda, double wsum, double *d_residual,
                     double *d_values, void *stream);
+/* skg_nh_assemble with the residual and tangent values also written to the
+ * page-locked host arrays h_residual (N) and h_values (nnz); d_residual and
+ * d_values are the device staging arrays (both required).  On a row-grouped
+ * pattern the element and row passes run over row chunks and each chunk's
+ * rows are copied while later chunks run. */
+int skg_nh_assemble_host(const skg_pattern *pattern, const double *d_p, int64_t npts,
+                         const int32_t *d_t, int64_t n_elements, const double *d_u,
+                         double mu, double lmbda, double wsum, double *d_residual,
+                         double *d_values, double *h_residual, double *h_values,
+                         void *stream);
 
 /* Learned closure (no counterpart in the reference): an MLP
  * 3 -> 64 -> 64 -> 1 (tanh) with a linear input -> output skip, on the
@@ -389,6 +416,14 @@ int skg_nh_assemble_surrogate(const skg_pattern *pattern, const double *d_p,
                               double wsum, const float *d_params,
                               const float *d_box, float tol, double *d_residual,
                               double *d_values, int64_t *h_fallback, void *stream);
+/* skg_nh_assemble_surrogate with host outputs, as skg_nh_assemble_host. */
+int skg_nh_assemble_surrogate_host(const skg_pattern *pattern, const double *d_p,
+                                   int64_t npts, const int32_t *d_t,
+                                   int64_t n_elements, const double *d_u, double mu,
+                                   double lmbda, double wsum, const float *d_params,
+                                   const float *d_box, float tol, double *d_residual,
+                                   double *d_values, double *h_residual,
+                                   double *h_values, int64_t *h_fallback, void *stream);
 
 #ifdef __cplusplus
 }

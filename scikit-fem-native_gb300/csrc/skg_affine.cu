@@ -1018,9 +1018,9 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         SKG_CUDA(cudaStreamSynchronize(s));
         if (h_misc[1] == 0 && h_misc[0] != INT_MIN) {
             if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
-            run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs) {
-                launch_ke_df_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kf.get(), misc.get(), d_values, s);
-                launch_ke_df_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kf.get(), misc.get(), d_values, s);
+            run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs, cudaStream_t st) {
+                launch_ke_df_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kf.get(), misc.get(), d_values, st);
+                launch_ke_df_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kf.get(), misc.get(), d_values, st);
             });
             if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
             return;
@@ -1057,7 +1057,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
                 SKG_LAUNCH_CHECK("elem_ke_fp64");
                 if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
             },
-            [&](const GroupSet &gs) { add_element_rows<10>(pat, Ke.get(), d_values, s, gs); });
+            [&](const GroupSet &gs, cudaStream_t st) { add_element_rows<10>(pat, Ke.get(), d_values, st, gs); });
         if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
         return;
     }
@@ -1085,8 +1085,8 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
     } else {
         const int *sp_ptr = misc.get();
-        run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs) {
-#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, gs)
+        run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs, cudaStream_t st) {
+#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, st, gs)
             if (nodes == 4) {
                 if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
                 else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
@@ -1094,7 +1094,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             } else {
                 if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
                 else if (mode == MODE_SPLIT) {
-                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, s, gs);
+                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, st, gs);
                     else SKG_ROWS(10, MODE_SPLIT);
                 } else {
                     SKG_ROWS(10, MODE_DF64);

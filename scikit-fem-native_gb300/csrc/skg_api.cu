@@ -1,5 +1,6 @@
 // Library-wide C ABI entry points: version, per-thread last error, device
 // capabilities the host side needs.
+#include <algorithm>
 #include <string>
 
 #include "skg_common.cuh"
@@ -24,3 +25,25 @@ extern "C" int skg_device_pageable_access(int32_t *out) {
         *out = v;
     });
 }
+
+namespace skg {
+namespace {
+__global__ void k_stage(const double *__restrict__ src, double *__restrict__ dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+}  // namespace
+
+const double *device_resident(const double *p, int64_t n, DevBuf<double> &stage, cudaStream_t s) {
+    if (!p || n <= 0) return p;
+    cudaPointerAttributes attr{};
+    SKG_CUDA(cudaPointerGetAttributes(&attr, p));
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return p;
+    stage = DevBuf<double>((size_t)n, s);
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4 * kSmCount);
+    k_stage<<<(unsigned)blocks, 256, 0, s>>>(p, stage.get(), n);
+    SKG_LAUNCH_CHECK("stage");
+    return stage.get();
+}
+
+}  // namespace skg

@@ -135,6 +135,12 @@ struct DevBuf {
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// p (n doubles) in device memory: p itself.  In host memory the device can
+// read (page-locked, or pageable on a device with pageable access): a device
+// copy in `stage`, made by a coalesced read on the stream, so that kernels
+// gathering from it at random do not cross the host link per access.
+const double *device_resident(const double *p, int64_t n, DevBuf<double> &stage, cudaStream_t s);
+
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;

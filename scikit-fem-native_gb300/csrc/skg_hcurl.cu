@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "skg_common.cuh"
+#include "skg_rows.cuh"
 
 namespace skg {
 
@@ -162,16 +163,17 @@ constexpr int kN1Block = 128;
 // contracted in FP32 with split products (hi hi + hi lo + lo hi) and FP32
 // accumulation; FP64 keeps the geometry and the CSR slot sums.
 template <bool SPLIT>
-__global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, const double *__restrict__ p, int64_t npts,
+__global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                            const double *__restrict__ p, int64_t npts,
                                                             const int32_t *__restrict__ t,
                                                             const int8_t *__restrict__ signs, N1Table tab,
                                                             const double *__restrict__ mass,
                                                             const double *__restrict__ curl, int inc_mass,
                                                             int inc_curl, double *__restrict__ Ke) {
     __shared__ double stage[kN1Block * 37];
-    const int64_t e0 = (int64_t)blockIdx.x * kN1Block;
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * kN1Block;
     const int64_t e = e0 + threadIdx.x;
-    if (e < ne) {
+    if (e < e_end) {
         double J[9], b[4][3], det;
         n1_geometry(p, npts, t, ne, e, J, b, det);
         const double inv = 1.0 / fabs(det);
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, const dou
         }
     }
     __syncthreads();
-    const int nvalid = (int)(ne - e0 < kN1Block ? ne - e0 : kN1Block);
+    const int nvalid = (int)(e_end - e0 < kN1Block ? e_end - e0 : kN1Block);
     for (int i = threadIdx.x; i < nvalid * 36; i += kN1Block) {
         const int el = i / 36, q = i - el * 36;
         Ke[(e0 + el) * 36 + q] = stage[el * 37 + q];
@@ -442,6 +444,44 @@ static void n1_table(int nq, const double *X, const double *W, N1Table &tab) {
                 }
 }
 
+namespace skg {
+namespace {
+
+// Element matrices by the closed form, then CSR row sums.  h_values
+// (optional, page-locked host): the values are also copied there; on a
+// row-grouped pattern the element and row passes then interleave over row
+// chunks so that the copies overlap them (run_passes).
+void n1_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t, const int8_t *d_signs,
+                 int64_t ne, int32_t nq, const double *h_X, const double *h_W, const double *d_mass,
+                 const double *d_curl, int32_t include_mass, int32_t include_curl, int32_t precision,
+                 double *d_values, double *h_values, cudaStream_t s) {
+    N1Table tab;
+    n1_table(nq, h_X, h_W, tab);
+    DevBuf<double> Ke((size_t)ne * 36, s);
+    auto elem = [&](int64_t e0, int64_t e1) {
+        const unsigned grid = grid_for(e1 - e0, kN1Block);
+        if (precision == SKG_SPLIT_FP32)
+            k_n1_elem_fast<true><<<grid, kN1Block, 0, s>>>(ne, e0, e1, d_p, npts, d_t, d_signs, tab, d_mass, d_curl,
+                                                           include_mass, include_curl, Ke.get());
+        else
+            k_n1_elem_fast<false><<<grid, kN1Block, 0, s>>>(ne, e0, e1, d_p, npts, d_t, d_signs, tab, d_mass, d_curl,
+                                                            include_mass, include_curl, Ke.get());
+        SKG_LAUNCH_CHECK("n1_element");
+    };
+    if (h_values && pat->max_row_len > 0) {
+        run_passes(pat, ne, d_values, h_values, s, elem,
+                   [&](const GroupSet &gs, cudaStream_t st) { add_element_rows<6>(pat, Ke.get(), d_values, st, gs); });
+        return;
+    }
+    if (ne) elem(0, ne);
+    gather_element_matrices(pat, Ke.get(), d_values, s);
+    if (h_values && pat->nnz)
+        SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+
+}  // namespace
+}  // namespace skg
+
 extern "C" int skg_n1_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
                                const int32_t *d_elem_edges, const int8_t *d_signs, int64_t ne, int32_t nq,
                                const double *h_X, const double *h_W, const double *d_mass, const double *d_curl,
@@ -453,20 +493,25 @@ extern "C" int skg_n1_assemble(const skg_pattern *pat, const double *d_p, int64_
         require(nq > 0 && h_X && h_W, "quadrature rule is empty");
         require(d_p && d_t && d_signs, "mesh arrays are NULL");
         (void)d_elem_edges;
-        cudaStream_t s = as_stream(stream);
-        N1Table tab;
-        n1_table(nq, h_X, h_W, tab);
-        DevBuf<double> Ke((size_t)ne * 36, s);
-        if (ne) {
-            if (precision == SKG_SPLIT_FP32)
-                k_n1_elem_fast<true><<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(
-                    ne, d_p, npts, d_t, d_signs, tab, d_mass, d_curl, include_mass, include_curl, Ke.get());
-            else
-                k_n1_elem_fast<false><<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(
-                    ne, d_p, npts, d_t, d_signs, tab, d_mass, d_curl, include_mass, include_curl, Ke.get());
-            SKG_LAUNCH_CHECK("n1_element");
-        }
-        gather_element_matrices(pat, Ke.get(), d_values, s);
+        n1_assemble(pat, d_p, npts, d_t, d_signs, ne, nq, h_X, h_W, d_mass, d_curl, include_mass, include_curl,
+                    precision, d_values, nullptr, as_stream(stream));
+    });
+}
+
+extern "C" int skg_n1_assemble_host(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
+                                    const int32_t *d_elem_edges, const int8_t *d_signs, int64_t ne, int32_t nq,
+                                    const double *h_X, const double *h_W, const double *d_mass, const double *d_curl,
+                                    int32_t include_mass, int32_t include_curl, int32_t precision, double *d_values,
+                                    double *h_values, void *stream) {
+    return guarded([&] {
+        require(pat != nullptr, "pattern is NULL");
+        require(ne == pat->n_elements && pat->row_local == 6 && pat->col_local == 6, "mesh does not match the pattern");
+        require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+        require(d_p && d_t && d_signs, "mesh arrays are NULL");
+        require(d_values && h_values, "device staging or host output is NULL");
+        (void)d_elem_edges;
+        n1_assemble(pat, d_p, npts, d_t, d_signs, ne, nq, h_X, h_W, d_mass, d_curl, include_mass, include_curl,
+                    precision, d_values, h_values, as_stream(stream));
     });
 }
 

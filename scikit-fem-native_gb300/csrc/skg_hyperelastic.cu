@@ -51,12 +51,12 @@ __global__ void k_nh_element(int64_t ne, const double *__restrict__ p, int64_t n
 }
 
 // Plain records for the fused row pass.
-__global__ void k_nh_plain_record(int64_t ne, const double *__restrict__ p, int64_t npts,
-                                  const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
+__global__ void k_nh_plain_record(int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p,
+                                  int64_t npts, const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
                                   const double *__restrict__ u, double mu, double lmbda, double wsum,
                                   double *__restrict__ rec) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+    const int64_t e = e_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= e_end) return;
     NhGeom g;
     nh_geometry(p, npts, t, ne, e, wsum, g);
     double Gu[9];
@@ -268,19 +268,29 @@ __global__ void k_vector_gather(int64_t n_rows, const int32_t *__restrict__ inc_
 
 }  // namespace
 
-void nh_rows(const skg_pattern *pat, const double *recd, const float *recf, const unsigned char *flags,
-             double *d_residual, double *d_values, cudaStream_t s) {
+void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, const float *recf,
+             const unsigned char *flags, double *d_residual, double *d_values, cudaStream_t s) {
     if (recf) {
-        launch_nh_rows<true, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, recd, recf, flags,
-                                                  d_residual, d_values, s);
-        launch_nh_rows<true, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, recd, recf, flags,
-                                                  d_residual, d_values, s);
+        launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, d_residual, d_values,
+                                                  s);
+        launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, d_residual, d_values,
+                                                  s);
     } else {
-        launch_nh_rows<false, kGroupSlotsSmall, 1>(pat->n_groups_small, pat->groups_small.get(), pat, recd, nullptr,
-                                                   nullptr, d_residual, d_values, s);
-        launch_nh_rows<false, kGroupSlotsLarge, 2>(pat->n_groups_large, pat->groups_large.get(), pat, recd, nullptr,
-                                                   nullptr, d_residual, d_values, s);
+        launch_nh_rows<false, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, nullptr, nullptr, d_residual,
+                                                   d_values, s);
+        launch_nh_rows<false, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, nullptr, nullptr, d_residual,
+                                                   d_values, s);
     }
+}
+
+// Whole-array copies of the results to the host (paths without row chunks).
+void nh_download(const skg_pattern *pat, const double *d_residual, const double *d_values, double *h_residual,
+                 double *h_values, cudaStream_t s) {
+    if (h_values && d_values && pat->nnz)
+        SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (h_residual && d_residual && pat->n_rows)
+        SKG_CUDA(cudaMemcpyAsync(h_residual, d_residual, (size_t)pat->n_rows * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
 }
 
 void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, double *d_residual, double *d_values,
@@ -297,31 +307,65 @@ void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, doubl
 
 using namespace skg;
 
+namespace skg {
+namespace {
+
+// Plain-law residual and tangent; with h_values / h_residual (page-locked
+// host) the results also go there, chunk by chunk on the fused path.
+void nh_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t, int64_t ne,
+                 const double *d_u, double mu, double lmbda, double wsum, double *d_residual, double *d_values,
+                 double *h_residual, double *h_values, cudaStream_t s) {
+    require(pat != nullptr, "pattern is NULL");
+    require(pat->row_local == 12 && pat->n_elements == ne, "neo-Hookean assembly needs the vector P1 pattern");
+    require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
+    require(d_p && d_t && d_u, "mesh or displacement arrays are NULL");
+    DevBuf<double> u_stage;
+    d_u = device_resident(d_u, pat->n_rows, u_stage, s);
+    if (d_values && pat->max_row_len > 0) {  // fused path
+        DevBuf<double> rec((size_t)ne * kNhRecD, s);
+        run_passes(
+            pat, ne, d_values, h_values, s,
+            [&](int64_t e0, int64_t e1) {
+                k_nh_plain_record<<<grid_for(e1 - e0, 128), 128, 0, s>>>(ne, e0, e1, d_p, npts, d_t,
+                                                                        pat->row_dofs.get(), d_u, mu, lmbda, wsum,
+                                                                        rec.get());
+                SKG_LAUNCH_CHECK("nh_plain_record");
+            },
+            [&](const GroupSet &gs, cudaStream_t st) {
+                nh_rows(pat, gs, rec.get(), nullptr, nullptr, d_residual, d_values, st);
+            },
+            d_residual, h_residual);
+        return;
+    }
+    DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
+    if (ne) {
+        k_nh_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum,
+                                                      Ke.get(), re.get());
+        SKG_LAUNCH_CHECK("nh_element");
+    }
+    nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
+    nh_download(pat, d_residual, d_values, h_residual, h_values, s);
+}
+
+}  // namespace
+}  // namespace skg
+
 extern "C" int skg_nh_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
                                int64_t ne, const double *d_u, double mu, double lmbda, double wsum,
                                double *d_residual, double *d_values, void *stream) {
     return guarded([&] {
-        require(pat != nullptr, "pattern is NULL");
-        require(pat->row_local == 12 && pat->n_elements == ne, "neo-Hookean assembly needs the vector P1 pattern");
-        require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
-        require(d_p && d_t && d_u, "mesh or displacement arrays are NULL");
-        cudaStream_t s = as_stream(stream);
-        if (d_values && pat->max_row_len > 0) {  // fused path
-            DevBuf<double> rec((size_t)ne * kNhRecD, s);
-            if (ne) {
-                k_nh_plain_record<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
-                                                                   lmbda, wsum, rec.get());
-                SKG_LAUNCH_CHECK("nh_plain_record");
-            }
-            nh_rows(pat, rec.get(), nullptr, nullptr, d_residual, d_values, s);
-            return;
-        }
-        DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
-        if (ne) {
-            k_nh_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda,
-                                                          wsum, Ke.get(), re.get());
-            SKG_LAUNCH_CHECK("nh_element");
-        }
-        nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
+        nh_assemble(pat, d_p, npts, d_t, ne, d_u, mu, lmbda, wsum, d_residual, d_values, nullptr, nullptr,
+                    as_stream(stream));
+    });
+}
+
+extern "C" int skg_nh_assemble_host(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
+                                    int64_t ne, const double *d_u, double mu, double lmbda, double wsum,
+                                    double *d_residual, double *d_values, double *h_residual, double *h_values,
+                                    void *stream) {
+    return guarded([&] {
+        require(d_residual && d_values && h_residual && h_values, "device staging or host output is NULL");
+        nh_assemble(pat, d_p, npts, d_t, ne, d_u, mu, lmbda, wsum, d_residual, d_values, h_residual, h_values,
+                    as_stream(stream));
     });
 }

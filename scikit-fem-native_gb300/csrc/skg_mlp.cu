@@ -37,10 +37,6 @@
 #include "skg_tc.cuh"
 
 namespace skg {
-
-void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, double *d_residual, double *d_values,
-               cudaStream_t s);
-
 namespace {
 
 constexpr int H = 64;
@@ -858,7 +854,7 @@ __device__ __forceinline__ bool geometry_fp32(const double *__restrict__ p, int6
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
-    int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+    int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
     const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda, double wsum,
     const float *__restrict__ params, const float *__restrict__ box, float tol, float *__restrict__ recf,
     double *__restrict__ recd, unsigned char *__restrict__ flags, unsigned long long *__restrict__ counters) {
@@ -900,9 +896,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
     const float *Nrm = Q + QNORM;
     uint32_t phase = 0;
     bool tc_ok = true;
-    for (int64_t tile = blockIdx.x; tile * kTcRows < ne; tile += gridDim.x) {
-        const int64_t e = tile * kTcRows + row;
-        const bool valid = e < ne;
+    for (int64_t tile = blockIdx.x; e_begin + tile * kTcRows < e_end; tile += gridDim.x) {
+        const int64_t e = e_begin + tile * kTcRows + row;
+        const bool valid = e < e_end;
         float ga[4][3], Vf = 0.f, F[9];
         bool geo = false;
         if (valid) geo = geometry_fp32(p, npts, t, ne, e, dofs, u, wsum, ga, Vf, F);
@@ -1252,51 +1248,86 @@ extern "C" int skg_mlp_eval(const float *d_params, const float *d_x, int64_t n, 
     });
 }
 
+namespace skg {
+namespace {
+
+// Learned-closure residual and tangent (see k_nh_surrogate_tc); with
+// h_values / h_residual (page-locked host) the results also go there, chunk
+// by chunk on the fused path.  Returns the fallback count when h_fallback.
+void nh_assemble_surrogate(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t, int64_t ne,
+                           const double *d_u, double mu, double lmbda, double wsum, const float *d_params,
+                           const float *d_box, float tol, double *d_residual, double *d_values, double *h_residual,
+                           double *h_values, int64_t *h_fallback, cudaStream_t s) {
+    require(pat != nullptr, "pattern is NULL");
+    require(pat->row_local == 12 && pat->n_elements == ne, "neo-Hookean assembly needs the vector P1 pattern");
+    require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
+    require(d_p && d_t && d_u && d_params && d_box, "invalid surrogate arguments");
+    DevBuf<double> u_stage;
+    d_u = device_resident(d_u, pat->n_rows, u_stage, s);
+    DevBuf<unsigned long long> fb(2, s);  // [0] fallback elements, [1] tensor-core waits given up
+    SKG_CUDA(cudaMemsetAsync(fb.get(), 0, 16, s));
+    if (d_values && pat->max_row_len > 0) {  // fused path, network on the tensor cores
+        DevBuf<float> recf((size_t)ne * kNhRecF, s);
+        DevBuf<double> recd((size_t)ne * kNhRecD, s);
+        DevBuf<unsigned char> flags((size_t)ne, s);
+        SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+        run_passes(
+            pat, ne, d_values, h_values, s,
+            [&](int64_t e0, int64_t e1) {
+                const int64_t tiles = (e1 - e0 + kTcRows - 1) / kTcRows;
+                const unsigned grid = (unsigned)(tiles < kSmCount ? tiles : kSmCount);
+                k_nh_surrogate_tc<<<grid, kTcThreads, kTcSmem, s>>>(ne, e0, e1, d_p, npts, d_t, pat->row_dofs.get(),
+                                                                 d_u, mu, lmbda, wsum, d_params, d_box, tol,
+                                                                 recf.get(), recd.get(), flags.get(), fb.get());
+                SKG_LAUNCH_CHECK("nh_surrogate_tc");
+            },
+            [&](const GroupSet &gs, cudaStream_t st) {
+                nh_rows(pat, gs, recd.get(), recf.get(), flags.get(), d_residual, d_values, st);
+            },
+            d_residual, h_residual);
+    } else {
+        DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
+        if (ne) {
+            SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_element<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kEvalSmem));
+            k_nh_surrogate_element<false><<<grid_for(ne, kEvalBlock), kEvalBlock, kEvalSmem, s>>>(
+                ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum, d_params, d_box, tol, Ke.get(),
+                re.get(), nullptr, nullptr, nullptr, fb.get());
+            SKG_LAUNCH_CHECK("nh_surrogate_element");
+        }
+        nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
+        nh_download(pat, d_residual, d_values, h_residual, h_values, s);
+    }
+    if (h_fallback) {
+        unsigned long long h[2] = {0, 0};
+        SKG_CUDA(cudaMemcpyAsync(h, fb.get(), 16, cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        *h_fallback = (int64_t)h[0];
+        require(h[1] == 0, "tensor-core MMA wait timed out (elements fell back to the plain law)", SKG_ECUDA);
+    }
+}
+
+}  // namespace
+}  // namespace skg
+
 extern "C" int skg_nh_assemble_surrogate(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
                                          int64_t ne, const double *d_u, double mu, double lmbda, double wsum,
                                          const float *d_params, const float *d_box, float tol, double *d_residual,
                                          double *d_values, int64_t *h_fallback, void *stream) {
     return guarded([&] {
-        require(pat != nullptr, "pattern is NULL");
-        require(pat->row_local == 12 && pat->n_elements == ne, "neo-Hookean assembly needs the vector P1 pattern");
-        require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
-        require(d_p && d_t && d_u && d_params && d_box, "invalid surrogate arguments");
-        cudaStream_t s = as_stream(stream);
-        DevBuf<unsigned long long> fb(2, s);  // [0] fallback elements, [1] tensor-core waits given up
-        SKG_CUDA(cudaMemsetAsync(fb.get(), 0, 16, s));
-        if (d_values && pat->max_row_len > 0) {  // fused path, network on the tensor cores
-            DevBuf<float> recf((size_t)ne * kNhRecF, s);
-            DevBuf<double> recd((size_t)ne * kNhRecD, s);
-            DevBuf<unsigned char> flags((size_t)ne, s);
-            if (ne) {
-                SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)kTcSmem));
-                const int64_t tiles = (ne + kTcRows - 1) / kTcRows;
-                const unsigned grid = (unsigned)(tiles < kSmCount ? tiles : kSmCount);
-                k_nh_surrogate_tc<<<grid, kTcThreads, kTcSmem, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu,
-                                                                 lmbda, wsum, d_params, d_box, tol, recf.get(),
-                                                                 recd.get(), flags.get(), fb.get());
-                SKG_LAUNCH_CHECK("nh_surrogate_tc");
-            }
-            nh_rows(pat, recd.get(), recf.get(), flags.get(), d_residual, d_values, s);
-        } else {
-            DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
-            if (ne) {
-                SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_element<false>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem));
-                k_nh_surrogate_element<false><<<grid_for(ne, kEvalBlock), kEvalBlock, kEvalSmem, s>>>(
-                    ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum, d_params, d_box, tol, Ke.get(),
-                    re.get(), nullptr, nullptr, nullptr, fb.get());
-                SKG_LAUNCH_CHECK("nh_surrogate_element");
-            }
-            nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
-        }
-        if (h_fallback) {
-            unsigned long long h[2] = {0, 0};
-            SKG_CUDA(cudaMemcpyAsync(h, fb.get(), 16, cudaMemcpyDeviceToHost, s));
-            SKG_CUDA(cudaStreamSynchronize(s));
-            *h_fallback = (int64_t)h[0];
-            require(h[1] == 0, "tensor-core MMA wait timed out (elements fell back to the plain law)", SKG_ECUDA);
-        }
+        nh_assemble_surrogate(pat, d_p, npts, d_t, ne, d_u, mu, lmbda, wsum, d_params, d_box, tol, d_residual,
+                              d_values, nullptr, nullptr, h_fallback, as_stream(stream));
+    });
+}
+
+extern "C" int skg_nh_assemble_surrogate_host(const skg_pattern *pat, const double *d_p, int64_t npts,
+                                              const int32_t *d_t, int64_t ne, const double *d_u, double mu,
+                                              double lmbda, double wsum, const float *d_params, const float *d_box,
+                                              float tol, double *d_residual, double *d_values, double *h_residual,
+                                              double *h_values, int64_t *h_fallback, void *stream) {
+    return guarded([&] {
+        require(d_residual && d_values && h_residual && h_values, "device staging or host output is NULL");
+        nh_assemble_surrogate(pat, d_p, npts, d_t, ne, d_u, mu, lmbda, wsum, d_params, d_box, tol, d_residual,
+                              d_values, h_residual, h_values, h_fallback, as_stream(stream));
     });
 }

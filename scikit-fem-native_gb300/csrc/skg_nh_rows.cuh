@@ -16,6 +16,7 @@
 #include "skg_common.cuh"
 #include "skg_df64.cuh"
 #include "skg_nh.cuh"
+#include "skg_rows.cuh"
 
 namespace skg {
 
@@ -38,7 +39,15 @@ __device__ __forceinline__ void write_plain_record(const NhGeom &g, const NhLaw 
     r[35] = lmbda * g.V;
 }
 
-void nh_rows(const skg_pattern *pat, const double *recd, const float *recf, const unsigned char *flags,
-             double *d_residual, double *d_values, cudaStream_t s);
+void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, const float *recf,
+             const unsigned char *flags, double *d_residual, double *d_values, cudaStream_t s);
+
+// Residual and tangent from per-element arrays (patterns without row groups).
+void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, double *d_residual, double *d_values,
+               cudaStream_t s);
+
+// Whole-array copies of the results to the host (paths without row chunks).
+void nh_download(const skg_pattern *pat, const double *d_residual, const double *d_values, double *h_residual,
+                 double *h_values, cudaStream_t s);
 
 }  // namespace skg

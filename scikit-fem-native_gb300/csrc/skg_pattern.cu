@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "skg_common.cuh"
+#include "skg_rows.cuh"
 
 namespace skg {
 
@@ -475,16 +476,24 @@ extern "C" int skg_pattern_row_groups(const skg_pattern *p, int32_t *max_row_len
 
 namespace skg {
 
-// Non-blocking copy stream per device for the host-output paths.
-cudaStream_t copy_stream() {
+// Non-blocking side streams per device (copy, rows, minor class).  The row
+// streams have the highest priority: their blocks are scheduled ahead of the
+// element pass running beside them, so each chunk's values are ready for its
+// copy as early as possible.
+cudaStream_t side_stream(Side which) {
     static std::mutex mu;
-    static cudaStream_t streams[64] = {};
+    static cudaStream_t streams[64][3] = {};
     int dev = 0;
     SKG_CUDA(cudaGetDevice(&dev));
     require(dev >= 0 && dev < 64, "device index out of range");
+    const int k = (int)which;
     std::lock_guard<std::mutex> lock(mu);
-    if (!streams[dev]) SKG_CUDA(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
-    return streams[dev];
+    if (!streams[dev][k]) {
+        int least = 0, greatest = 0;
+        SKG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        const int priority = which == Side::copy ? least : greatest;
+        SKG_CUDA(cudaStreamCreateWithPriority(&streams[dev][k], cudaStreamNonBlocking, priority));
+    }
+    return streams[dev][k];
 }
-
 }  // namespace skg

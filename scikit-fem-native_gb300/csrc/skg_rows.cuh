@@ -123,30 +123,78 @@ inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *v
     launch_ke_class<N, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Ke, values, s);
 }
 
-template <int N>
-inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
-    add_element_rows<N>(pat, Ke, values, s, all_groups(pat));
+// Per-device non-blocking side streams of the assembly passes.
+enum class Side { copy = 0, rows = 1, minor = 2 };
+cudaStream_t side_stream(Side which);
+
+// Events of one assembly call, released at the end (an event destroyed
+// while its work is pending is released once that work completes).
+struct EventSet {
+    std::vector<cudaEvent_t> evs;
+    cudaEvent_t record(cudaStream_t s) {
+        cudaEvent_t ev;
+        SKG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        evs.push_back(ev);
+        SKG_CUDA(cudaEventRecord(ev, s));
+        return ev;
+    }
+    void order(cudaStream_t from, cudaStream_t to) {  // `to` waits for the work queued on `from`
+        SKG_CUDA(cudaStreamWaitEvent(to, record(from), 0));
+    }
+    ~EventSet() {
+        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+    }
+};
+
+// Row pass of a group set on stream st.  When both classes are present the
+// class with fewer groups runs on the minor side stream at the same time: a
+// class of a few groups is bound by the latency of one group's incidence
+// walk and would otherwise leave the GPU idle behind the other class.
+template <class FR>
+void rows_on(const GroupSet &gs, cudaStream_t st, EventSet &ev, FR &&rows) {
+    if (gs.n_small == 0 || gs.n_large == 0) {
+        rows(gs, st);
+        return;
+    }
+    const GroupSet small{gs.n_small, gs.small, 0, nullptr}, large{0, nullptr, gs.n_large, gs.large};
+    const bool small_major = gs.n_small >= gs.n_large;
+    cudaStream_t xs = side_stream(Side::minor);
+    ev.order(st, xs);
+    rows(small_major ? large : small, xs);
+    rows(small_major ? small : large, st);
+    ev.order(xs, st);
 }
 
-cudaStream_t copy_stream();
+// All groups (both classes at once, see rows_on).
+template <int N>
+inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s) {
+    EventSet ev;
+    rows_on(all_groups(pat), s, ev,
+            [&](const GroupSet &gs, cudaStream_t st) { add_element_rows<N>(pat, Ke, values, st, gs); });
+}
 
-// Element pass and row pass of a pattern with row groups, with the values
-// optionally copied to the page-locked host array h_values.
+// Element pass and row pass of a pattern with row groups; elem(e0, e1)
+// launches the element pass over elements [e0, e1) on s, rows(groups, st)
+// the row pass of a group set on stream st.  The values optionally go to
+// the page-locked host array h_values as well.
 //
-// Device output: elem(0, ne) then rows(all groups).
+// Device output: elem(0, ne), then the row pass of all groups on s.
 // Host output: the row chunks are taken in the order in which their elements
-// are complete (hc_ready); before a chunk's row pass, the element pass runs
-// up to its readiness bound (in steps of at least ne / kHostChunks elements,
-// so launches stay large), and after it the chunk's slot range is copied to
-// h_values on a second stream while the following element and row launches
-// run.  Every group lies inside one chunk, so each copied range is complete.
-// The caller's stream waits for the copies at the end.
+// are complete (hc_ready).  The element pass runs on s in steps of at least
+// ne / kHostChunks elements, so launches stay large; each chunk's row pass
+// runs on the rows side stream once the element steps it needs are done,
+// overlapping the following element steps, and its slot range is then copied
+// to h_values on the copy stream.  Every group lies inside one chunk, so each
+// copied range is complete.  d_rowvec / h_rowvec (optional): a per-row vector
+// the row pass also writes (a residual), copied with each chunk's rows.  At
+// the end s waits for the copies, which waited for every row pass.
 template <class FE, class FR>
 void run_passes(const skg_pattern *pat, int64_t ne, double *d_values, double *h_values, cudaStream_t s, FE &&elem,
-                FR &&rows) {
+                FR &&rows, const double *d_rowvec = nullptr, double *h_rowvec = nullptr) {
+    EventSet ev;
     if (!h_values) {
         if (ne) elem((int64_t)0, ne);
-        rows(all_groups(pat));
+        rows_on(all_groups(pat), s, ev, rows);
         return;
     }
     const int n_chunks = (int)pat->hc_ready.size();
@@ -154,15 +202,9 @@ void run_passes(const skg_pattern *pat, int64_t ne, double *d_values, double *h_
     for (int c = 0; c < n_chunks; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pat->hc_ready[a] < pat->hc_ready[b]; });
     const int64_t step = std::max<int64_t>(1, ne / kHostChunks);
-    cudaStream_t cs = copy_stream();
-    std::vector<cudaEvent_t> evs;
-    auto event = [&]() {
-        cudaEvent_t ev;
-        SKG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        evs.push_back(ev);
-        return ev;
-    };
+    cudaStream_t rs = side_stream(Side::rows), cs = side_stream(Side::copy);
     try {
+        ev.order(s, rs);  // inputs written earlier on s
         int64_t done = 0;
         for (int c : order) {
             const int64_t need = std::min(ne, pat->hc_ready[c]);
@@ -170,25 +212,33 @@ void run_passes(const skg_pattern *pat, int64_t ne, double *d_values, double *h_
                 const int64_t to = std::min(ne, std::max(need, done + step));
                 elem(done, to);
                 done = to;
+                ev.order(s, rs);
             }
-            rows(chunk_groups(pat, c));
-            const cudaEvent_t ev = event();
-            SKG_CUDA(cudaEventRecord(ev, s));
-            SKG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+            rows_on(chunk_groups(pat, c), rs, ev, rows);
+            ev.order(rs, cs);
             const int64_t s0 = pat->hc_slot[c], n = pat->hc_slot[c + 1] - s0;
             if (n)
                 SKG_CUDA(cudaMemcpyAsync(h_values + s0, d_values + s0, (size_t)n * sizeof(double),
                                          cudaMemcpyDeviceToHost, cs));
+            const int64_t r0 = pat->hc_row[c], nr = pat->hc_row[c + 1] - r0;
+            if (d_rowvec && h_rowvec && nr)
+                SKG_CUDA(cudaMemcpyAsync(h_rowvec + r0, d_rowvec + r0, (size_t)nr * sizeof(double),
+                                         cudaMemcpyDeviceToHost, cs));
         }
         if (done < ne) elem(done, ne);  // elements no row references
-        const cudaEvent_t fin = event();
-        SKG_CUDA(cudaEventRecord(fin, cs));
-        SKG_CUDA(cudaStreamWaitEvent(s, fin, 0));
+        ev.order(rs, cs);
+        ev.order(cs, s);
     } catch (...) {
-        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+        // scratch freed on s after this call must outlive the queued work
+        cudaEvent_t e;
+        for (cudaStream_t st : {rs, cs, side_stream(Side::minor)})
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+                cudaEventRecord(e, st);
+                cudaStreamWaitEvent(s, e, 0);
+                cudaEventDestroy(e);
+            }
         throw;
     }
-    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once complete
 }
 
 // Row pass alone (element data already computed), as run_passes.

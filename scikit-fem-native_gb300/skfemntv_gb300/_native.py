@@ -51,6 +51,8 @@ SIGNATURES = {
     "skg_edge_topology": [_vp, _i64, _vp, _vp, _vp, _i64p, _i64p, _vp],
     "skg_n1_assemble": [_vp, _vp, _i64, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _i32,
                         _i32, _vp, _vp],
+    "skg_n1_assemble_host": [_vp, _vp, _i64, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _i32,
+                             _i32, _vp, _vp, _vp],
     "skg_n1_assemble_pointwise": [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32,
                                   _i32, _vp, _vp],
     "skg_p1_energy": [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp],
@@ -58,6 +60,8 @@ SIGNATURES = {
                            ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
     "skg_nh_assemble": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                         _vp, _vp, _vp],
+    "skg_nh_assemble_host": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
+                             ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
     "skg_mlp_param_count": [],
     "skg_mlp_dataset": [_i64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
     "skg_mlp_loss_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _i32, ctypes.c_float, _vp, _vp, _vp],
@@ -75,6 +79,9 @@ SIGNATURES = {
     "skg_pattern_row_groups": [_vp, ctypes.POINTER(ctypes.c_int32)],
     "skg_nh_assemble_surrogate": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _vp, _vp, ctypes.c_float, _vp, _vp, _i64p, _vp],
+    "skg_nh_assemble_surrogate_host": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _i64p,
+                                       _vp],
     "skg_linear_assemble_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp],
 }

@@ -176,20 +176,16 @@ class _MatrixTarget:
         self._pinned, host = dev.pinned_empty(max(1, pattern.nnz))
         self.matrix = csr_matrix((host[: pattern.nnz], indices, indptr), shape=shape, copy=False)
 
+    def enqueue_download(self):
+        """Queue the copy of the device values into the host matrix's page-locked values."""
+        self._pinned[: self.pattern.nnz].copy_(self.d_values[: self.pattern.nnz], non_blocking=True)
+
     def download(self):
         import torch
 
-        self._pinned[: self.pattern.nnz].copy_(self.d_values[: self.pattern.nnz], non_blocking=True)
+        self.enqueue_download()
         torch.cuda.current_stream().synchronize()
         return self.matrix
-
-    def host_out(self):
-        """Pointer kernels can write the host matrix's values through (page-locked
-        memory), when the device can write host memory and the pattern's row pass
-        writes every value once; else None."""
-        if not (self.pattern.blocked and dev.pageable_access()):
-            return None
-        return ctypes.c_void_p(self._pinned.data_ptr())
 
     def torch_csr(self):
         """The device values as a CUDA ``torch.sparse_csr_tensor`` (no host copy;

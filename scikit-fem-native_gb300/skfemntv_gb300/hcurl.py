@@ -162,32 +162,57 @@ class TetN1Assembler:
         self._dofs = basis._ee_dev.t().contiguous()  # (E, 6)
         self.pattern = Pattern(self._dofs, self._dofs, E, 6, 6, basis.N, basis.N)
         self.target = _MatrixTarget(self.pattern, (basis.N, basis.N))
+        self._keep = None
 
     def _coef(self, name, value):
+        """(per-element values (host array) or None, per-point device array or
+        None); per-element values of 1 are dropped (the kernels' default)."""
         E, Q = self.basis.dx.shape
         if value is None:
             return None, None
         pe = per_element(value, E, Q, name)
         if pe is not None:
-            return (None if np.all(pe == 1.0) else dev.to_device(pe, np.float64)), None
+            return (None if np.all(pe == 1.0) else np.ascontiguousarray(pe, dtype=np.float64)), None
         return None, dev.to_device(per_point(value, E, Q, name), np.float64)
+
+    def _element_pointer(self, pe, host, keep):
+        """Kernel pointer of per-element values: read in place from host memory
+        on the host-output path when the device can, else uploaded."""
+        if pe is None:
+            return None
+        if host:
+            ptr = dev.host_readable(pe)
+            if ptr is not None:
+                keep.append(pe)
+                return ptr
+        d = dev.to_device(pe, np.float64)
+        keep.append(d)
+        return dev.ptr(d)
 
     def assemble_device(self, *, mass_coefficient=None, curl_coefficient=None, include_mass=True,
                         include_curl=True, precision="fp64", _out=None):
-        """Assemble into the device values (or, with ``_out``, into the host
-        matrix's page-locked buffer); returns the device values tensor."""
+        """Assemble into the device values (with ``_out``, the host matrix's
+        page-locked values, also into those); returns the device values tensor.
+        The caller synchronises before host arrays passed in go away."""
         b = self.basis
-        out = _out if _out is not None else dev.ptr(self.target.d_values)
+        d_values = dev.ptr(self.target.d_values)
         E = b.mesh.nelements
         Q = len(b.W)
         prec = _precision(precision)
         m_el, m_pt = self._coef("mass", mass_coefficient)
         c_el, c_pt = self._coef("curl", curl_coefficient)
+        keep = []
         if m_pt is None and c_pt is None:
-            call("skg_n1_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b._t4), dev.ptr(b._ee_dev), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W),
-                 dev.ptr(m_el), dev.ptr(c_el), int(include_mass), int(include_curl), prec,
-                 out, dev.stream_ptr())
+            args = (self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1], dev.ptr(b._t4),
+                    dev.ptr(b._ee_dev), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W),
+                    self._element_pointer(m_el, _out is not None, keep),
+                    self._element_pointer(c_el, _out is not None, keep), int(include_mass), int(include_curl),
+                    prec, d_values)
+            if _out is not None:
+                call("skg_n1_assemble_host", *args, _out, dev.stream_ptr())
+            else:
+                call("skg_n1_assemble", *args, dev.stream_ptr())
+            self._keep = keep
         else:
             if prec != SKG_FP64:
                 from .errors import UnsupportedNativeForm
@@ -195,21 +220,23 @@ class TetN1Assembler:
                 raise UnsupportedNativeForm("split precision needs per-element coefficients")
             ones = dev.to_device(np.ones((E, Q)), np.float64)
             mp = m_pt if m_pt is not None else (
-                ones if m_el is None else dev.to_device(np.repeat(m_el.cpu().numpy()[:, None], Q, 1), np.float64))
+                ones if m_el is None else dev.to_device(np.repeat(m_el[:, None], Q, 1), np.float64))
             cp = c_pt if c_pt is not None else (
-                ones if c_el is None else dev.to_device(np.repeat(c_el.cpu().numpy()[:, None], Q, 1), np.float64))
+                ones if c_el is None else dev.to_device(np.repeat(c_el[:, None], Q, 1), np.float64))
             call("skg_n1_assemble_pointwise", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
                  dev.ptr(b._t4), dev.ptr(b._signs_dev), E, Q, dev.hptr(b.X), dev.hptr(b.W), dev.ptr(mp),
-                 dev.ptr(cp), int(include_mass), int(include_curl), out,
-                 dev.stream_ptr())
+                 dev.ptr(cp), int(include_mass), int(include_curl), d_values, dev.stream_ptr())
+            if _out is not None:
+                self.target.enqueue_download()
         return self.target.d_values
 
     def _host(self, **kw):
-        """Host matrix: values written straight into its page-locked buffer when
-        the device can write host memory (row-grouped pattern), else copied."""
-        out = self.target.host_out()
-        self.assemble_device(_out=out, **kw)
-        return self.target.finish_direct() if out is not None else self.target.download()
+        """Host matrix: the values are copied chunk by chunk into its
+        page-locked buffer while the later chunks are computed."""
+        self.assemble_device(_out=self.target.pinned_ptr(), **kw)
+        out = self.target.finish_direct()
+        self._keep = None
+        return out
 
     def assemble_maxwell_torch(self, *, mass_coefficient=None, curl_coefficient=None, precision="fp64"):
         """Device-resident Maxwell matrix: a CUDA sparse CSR tensor (values reused)."""

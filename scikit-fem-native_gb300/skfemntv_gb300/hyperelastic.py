@@ -140,19 +140,26 @@ class NeoHookean:
         self.last_fallback = 0
         self._res_pinned = self._res_host = None
 
-    def _launch(self, u_ptr, surrogate, tol, res_ptr, val_ptr, count_fallback):
+    def _launch(self, u_ptr, surrogate, tol, res_ptr, val_ptr, count_fallback, host=None):
+        """host: (residual, values) page-locked host pointers that also receive
+        the results (copied chunk by chunk while later chunks run)."""
         b = self.basis
+        mesh = (self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1], dev.ptr(b.mesh._dev("t")),
+                b.mesh.nelements, u_ptr, self.mu, self.lmbda, self.wsum)
         if surrogate is None:
             self.last_fallback = 0
-            call("skg_nh_assemble", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, u_ptr, self.mu, self.lmbda, self.wsum, res_ptr,
-                 val_ptr, dev.stream_ptr())
+            if host is None:
+                call("skg_nh_assemble", *mesh, res_ptr, val_ptr, dev.stream_ptr())
+            else:
+                call("skg_nh_assemble_host", *mesh, res_ptr, val_ptr, *host, dev.stream_ptr())
         else:
             fb = ctypes.c_int64(-1)
-            call("skg_nh_assemble_surrogate", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b.mesh.nelements, u_ptr, self.mu, self.lmbda, self.wsum,
-                 dev.ptr(surrogate.params), dev.ptr(surrogate.box), ctypes.c_float(tol), res_ptr, val_ptr,
-                 ctypes.byref(fb) if count_fallback else None, dev.stream_ptr())
+            net = (dev.ptr(surrogate.params), dev.ptr(surrogate.box), ctypes.c_float(tol), res_ptr, val_ptr)
+            count = ctypes.byref(fb) if count_fallback else None
+            if host is None:
+                call("skg_nh_assemble_surrogate", *mesh, *net, count, dev.stream_ptr())
+            else:
+                call("skg_nh_assemble_surrogate_host", *mesh, *net, *host, count, dev.stream_ptr())
             self.last_fallback = int(fb.value)
 
     def assemble_device(self, u, surrogate=None, tol=1e-3, residual=True, tangent=True, count_fallback=True):
@@ -166,11 +173,11 @@ class NeoHookean:
 
     def assemble(self, u, surrogate=None, tol=1e-3):
         """(residual vector, tangent csr_matrix) at displacement u (N,).  The
-        tangent matrix is reused between calls; on the fused path the kernels read
-        u from host memory and write the residual and the CSR values straight
-        into page-locked host buffers."""
-        out = self.target.host_out()
-        if out is None or hasattr(u, "data_ptr"):
+        tangent matrix is reused between calls.  A host u is read by the device in
+        place when it can (the library copies it to the device first); on a
+        row-grouped pattern the row pass writes the residual and the CSR values
+        straight into page-locked host buffers, else they are copied there."""
+        if hasattr(u, "data_ptr"):
             self.assemble_device(u, surrogate=surrogate, tol=tol)
             K = self.target.download()
             return self.d_res[: self.basis.N].cpu().numpy(), K
@@ -182,6 +189,14 @@ class NeoHookean:
             u_ptr = dev.ptr(keep)
         if self._res_pinned is None:
             self._res_pinned, self._res_host = dev.pinned_empty(max(1, self.basis.N))
-        self._launch(u_ptr, surrogate, tol, ctypes.c_void_p(self._res_pinned.data_ptr()), out, True)
+        res_host = ctypes.c_void_p(self._res_pinned.data_ptr())
+        if self.pattern.blocked:
+            # the row pass writes every residual entry and CSR value once, and
+            # is long enough to carry the writes over the host link itself
+            self._launch(u_ptr, surrogate, tol, res_host, self.target.pinned_ptr(), True)
+        else:
+            self._launch(u_ptr, surrogate, tol, dev.ptr(self.d_res), dev.ptr(self.target.d_values), True,
+                         host=(res_host, self.target.pinned_ptr()))
         K = self.target.finish_direct()
-        return self._res_host[: self.basis.N].copy(), K
+        del keep
+        return dev.host_copy(self._res_host[: self.basis.N]), K

@@ -164,3 +164,37 @@ def test_surrogate_is_faster_than_plain_law(surrogate):
     print(f"48^3 plain {t_plain:.3f} ms, surrogate {t_sur:.3f} ms, fallback {nh.last_fallback}")
     assert nh.last_fallback == 0
     assert t_sur < t_plain
+
+
+def test_host_output_matches_device(surrogate):
+    """The host-output path (element and row passes over row chunks, results
+    copied chunk by chunk, u read from host memory) returns exactly the device
+    path's residual and tangent, for the plain law, the surrogate and the
+    all-fallback surrogate."""
+    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 17),) * 3)
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
+    nh = sk.NeoHookean(b, 1.0, 10.0)
+    u = sine_displacement(b)
+    du = torch.as_tensor(u, dtype=torch.float64, device="cuda")
+    import ctypes
+    from skfemntv_gb300 import _device as dev
+
+    res_pinned, res_view = dev.pinned_empty(b.N)
+    val_pinned, val_view = dev.pinned_empty(nh.pattern.nnz)
+    for kw in ({}, {"surrogate": surrogate, "tol": 1e-2}, {"surrogate": surrogate, "tol": -1.0}):
+        r_host, K_host = nh.assemble(u, **kw)
+        fb_host = nh.last_fallback
+        r_host, d_host = r_host.copy(), K_host.data.copy()
+        r_dev, k_dev = nh.assemble_device(du, **kw)
+        assert nh.last_fallback == fb_host
+        r_dev, k_dev = r_dev[: b.N].cpu().numpy(), k_dev[: nh.pattern.nnz].cpu().numpy()
+        assert np.array_equal(r_host.view(np.int64), r_dev.view(np.int64))
+        assert np.array_equal(d_host.view(np.int64), k_dev.view(np.int64))
+        # the chunked host-output entry points (device staging, copies per row chunk)
+        nh._launch(dev.ptr(du), kw.get("surrogate"), kw.get("tol", 1e-3), dev.ptr(nh.d_res),
+                   dev.ptr(nh.target.d_values), True,
+                   host=(ctypes.c_void_p(res_pinned.data_ptr()), ctypes.c_void_p(val_pinned.data_ptr())))
+        torch.cuda.synchronize()
+        assert nh.last_fallback == fb_host
+        assert np.array_equal(res_view.view(np.int64), r_dev.view(np.int64))
+        assert np.array_equal(val_view.view(np.int64), k_dev.view(np.int64))
