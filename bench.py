@@ -234,6 +234,29 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+# FP64 instructions per element of the FP64 passes (DFMA + DMUL + DADD thread
+# instructions counted by ncu on the 32^3 case, profiles/fp64_ops_p2_aniso_32.md).
+FP64_OPS_PER_ELEMENT = {"k_elem_ke_fp64": 293.1, "k_rows_ke": 111.1}
+
+
+def fp64_roof(call, passes, elements):
+    """FP64 pipe roof of the FP64 passes: the device's FMA rate measured now
+    (skg_fp64_fma_rate) against each pass's FP64 instructions per second."""
+    import ctypes
+
+    rate = ctypes.c_double()
+    call("skg_fp64_fma_rate", ctypes.byref(rate), None)
+    out = {"peak_gops": rate.value, "peak_source": "skg_fp64_fma_rate: independent FMA chains, measured in this run",
+           "passes": {}}
+    for name, _, _, ms in passes:
+        ops = FP64_OPS_PER_ELEMENT.get(name)
+        if ops is None:
+            continue
+        achieved = ops * elements / (ms * 1e-3) / 1e9
+        out["passes"][name] = {"ops_per_element": ops, "achieved_gops": achieved, "frac": achieved / rate.value}
+    return out
+
+
 def profiled_traffic(key):
     """DRAM bytes of one FP64 pass at 64^3 (element or row pass) from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_affine_fp64_p2_aniso_48.md")
@@ -364,7 +387,8 @@ def run_gpu(args, rank, world):
                                  if head_mode == "fp64" else "CUDA-core issue / shared-memory latency"),
                      "passes": {q[0]: {"ms": q[3], "algorithmic_bytes": q[2],
                                        "achieved_gbs": q[2] / (q[3] * 1e-3) / 1e9} for q in passes},
-                     "whole_assembly_hbm_frac": (bytes_elem + bytes_rows) / ((t_el + t_rows) * 1e-3) / 1e9 / peak},
+                     "whole_assembly_hbm_frac": (bytes_elem + bytes_rows) / ((t_el + t_rows) * 1e-3) / 1e9 / peak,
+                     "fp64_pipe": fp64_roof(call, passes, E) if head_mode == "fp64" else None},
         "precision_variants": results,
         "gpu_launches": 3 * args.steps,  # element pass + one row pass per group class
         "clocks": head["clocks"],

@@ -54,6 +54,12 @@ int skg_version(void);
 /* Message of the last failure on the calling thread ("" when none). */
 const char *skg_last_error(void);
 
+/* Measured FP64 FMA throughput of the current device (FMAs per second /
+ * 1e9), from one full-grid launch of independent FMA chains timed with CUDA
+ * events on the stream; the FP64 roof for reporting the FP64 passes.
+ * Synchronous. */
+int skg_fp64_fma_rate(double *h_gfma, void *stream);
+
 /* 1 when kernels on the current device may read and write pageable host
  * memory directly (Grace-Blackwell: address translation over NVLink-C2C).
  * The host side then lets kernels read coefficients from, and write CSR

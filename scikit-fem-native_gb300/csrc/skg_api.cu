@@ -47,3 +47,62 @@ const double *device_resident(const double *p, int64_t n, DevBuf<double> &stage,
 }
 
 }  // namespace skg
+
+// ---------------------------------------------------------------- FP64 rate
+// Measured FP64 FMA throughput of this device: every thread of a full grid
+// runs eight independent FMA chains; the time of one launch (CUDA events on
+// the stream) gives FMAs per second.  The FP64 roof against which the FP64
+// assembly passes are reported.
+namespace skg {
+namespace {
+constexpr int kRateBlocksPerSm = 8, kRateThreads = 256, kRateIters = 4096;
+
+__global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double *out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x + k;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+}  // namespace skg
+
+extern "C" int skg_fp64_fma_rate(double *h_gfma, void *stream) {
+    return skg::guarded([&] {
+        using namespace skg;
+        require(h_gfma != nullptr, "output pointer is NULL");
+        cudaStream_t s = as_stream(stream);
+        int dev = 0, sms = 0;
+        SKG_CUDA(cudaGetDevice(&dev));
+        SKG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int blocks = sms * kRateBlocksPerSm;
+        DevBuf<double> out((size_t)blocks * kRateThreads, s);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float ms = 0.f;
+        try {
+            SKG_CUDA(cudaEventCreate(&e0));
+            SKG_CUDA(cudaEventCreate(&e1));
+            k_fp64_rate<<<blocks, kRateThreads, 0, s>>>(out.get(), 64, 1.0000001, 1e-9);  // warm-up
+            SKG_LAUNCH_CHECK("fp64_rate");
+            SKG_CUDA(cudaEventRecord(e0, s));
+            k_fp64_rate<<<blocks, kRateThreads, 0, s>>>(out.get(), kRateIters, 1.0000001, 1e-9);
+            SKG_LAUNCH_CHECK("fp64_rate");
+            SKG_CUDA(cudaEventRecord(e1, s));
+            SKG_CUDA(cudaEventSynchronize(e1));
+            SKG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        } catch (...) {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const double fmas = 8.0 * kRateIters * (double)blocks * kRateThreads;
+        *h_gfma = fmas / ((double)ms * 1e-3) / 1e9;
+    });
+}

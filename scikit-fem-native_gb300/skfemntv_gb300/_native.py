@@ -70,6 +70,7 @@ SIGNATURES = {
     "skg_mlp_refine": [_vp, _vp, _vp, _i64, _vp, _i64, _i32, _i32, _i32, ctypes.c_float,
                        ctypes.POINTER(ctypes.c_double), _vp],
     "skg_mlp_eval": [_vp, _vp, _i64, _vp, _vp],
+    "skg_fp64_fma_rate": [_vp, _vp],
     "skg_device_pageable_access": [ctypes.POINTER(ctypes.c_int32)],
     "skg_h1_assemble_affine_host": [_vp, _vp, _i64, _vp, _i32, _i64, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp,
                                     _vp],

@@ -460,3 +460,14 @@ def test_n1_host_output_matches_device(precision):
     D = asmb.assemble_maxwell_torch(mass_coefficient=1.0, curl_coefficient=nu, precision=precision)
     d = D.values().cpu().numpy()
     assert np.array_equal(K.data.view(np.int64), d.view(np.int64))
+
+
+def test_fp64_rate_probe():
+    """The FP64 roof the bench reports against: a positive FMA rate of the
+    order of GB300's FP64 pipe (hundreds of GFMA/s)."""
+    import ctypes
+    from skfemntv_gb300._native import call
+
+    rate = ctypes.c_double()
+    call("skg_fp64_fma_rate", ctypes.byref(rate), None)
+    assert 50.0 < rate.value < 50000.0
