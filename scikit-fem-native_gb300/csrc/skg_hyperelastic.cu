@@ -36,38 +36,109 @@ void gather_element_matrices(const skg_pattern *pat, const double *Ke, double *v
 
 namespace {
 
-__global__ void k_nh_element(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
-                             const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda,
-                             double wsum, double *__restrict__ Ke, double *__restrict__ re) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    NhGeom g;
-    nh_geometry(p, npts, t, ne, e, wsum, g);
-    double Gu[9];
-    displacement_gradient(g, dofs + e * 12, u, Gu);
-    NhLaw law;
-    nh_plain_law(Gu, mu, lmbda, law);
-    write_nh_element(g, law, mu, lmbda, Ke ? Ke + e * 144 : nullptr, re ? re + e * 12 : nullptr);
-}
+constexpr int kNhKeBlock = 128;
+constexpr int kNhKeRound = 36;  // the three tangent rows of one vertex per staging round
 
-// Plain records for the fused row pass.
-__global__ void k_nh_plain_record(int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p,
-                                  int64_t npts, const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
-                                  const double *__restrict__ u, double mu, double lmbda, double wsum,
-                                  double *__restrict__ rec) {
-    const int64_t e = e_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= e_end) return;
-    NhGeom g;
-    nh_geometry(p, npts, t, ne, e, wsum, g);
-    double Gu[9];
-    displacement_gradient(g, dofs + e * 12, u, Gu);
-    NhLaw law;
-    nh_plain_law(Gu, mu, lmbda, law);
-    double r[kNhRecD];
-    write_plain_record(g, law, mu, lmbda, r);
-    double2 *out = reinterpret_cast<double2 *>(rec + e * kNhRecD);
+// Element tangent (E, 12, 12; row (a,i), column (b,k)) and residual (E, 12)
+// of the plain law for elements [e_begin, e_end), thread per element.  With
+// h_a = F^-T g_a, p_a = (mu - lambda ln J) V h_a, q_a = lambda V h_a and
+// G_ab = mu V g_a . g_b every entry is p_a,k h_b,i + q_a,i h_b,k (+ G_ab when
+// i = k): two FP64 operations.  The matrix is symmetric (block (b,a) is block
+// (a,b) transposed), so only the upper blocks and the upper halves of the
+// diagonal blocks are evaluated; upper blocks are kept in registers until the
+// rows of their lower twins are written.  The three rows of one vertex at a
+// time go through a shared-memory stage, so that the block writes whole
+// contiguous row triples.  Ke or re may be NULL (that output is skipped).
+__global__ void __launch_bounds__(kNhKeBlock) k_nh_ke(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                     const double *__restrict__ p, int64_t npts,
+                                                     const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
+                                                     const double *__restrict__ u, double mu, double lmbda,
+                                                     double wsum, double *__restrict__ Ke, double *__restrict__ re) {
+    __shared__ double stage[kNhKeBlock * (kNhKeRound + 1)];
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * kNhKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    double h[4][3], pp[4][3], qq[4][3], G[4][4], r[12];
+    if (e < e_end) {
+        NhGeom g;
+        nh_geometry(p, npts, t, ne, e, wsum, g);
+        double Gu[9];
+        displacement_gradient(g, dofs + e * 12, u, Gu);
+        NhLaw law;
+        nh_plain_law(Gu, mu, lmbda, law);
+        const double c2V = (mu - lmbda * law.lnJ) * g.V, lamV = lmbda * g.V, muV = mu * g.V;
 #pragma unroll
-    for (int k = 0; k < kNhRecD / 2; ++k) out[k] = make_double2(r[2 * k], r[2 * k + 1]);
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                h[a][i] = law.FiT[i * 3] * g.g[a][0] + law.FiT[i * 3 + 1] * g.g[a][1] + law.FiT[i * 3 + 2] * g.g[a][2];
+                pp[a][i] = c2V * h[a][i];
+                qq[a][i] = lamV * h[a][i];
+                r[a * 3 + i] =
+                    g.V * (law.P[i * 3] * g.g[a][0] + law.P[i * 3 + 1] * g.g[a][1] + law.P[i * 3 + 2] * g.g[a][2]);
+            }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = a; b < 4; ++b) {
+                G[a][b] = muV * (g.g[a][0] * g.g[b][0] + g.g[a][1] * g.g[b][1] + g.g[a][2] * g.g[b][2]);
+                G[b][a] = G[a][b];
+            }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) h[a][i] = pp[a][i] = qq[a][i] = r[a * 3 + i] = 0.0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) G[a][b] = 0.0;
+        }
+    }
+    const int nvalid = (int)(e_end - e0 < kNhKeBlock ? e_end - e0 : kNhKeBlock);
+    double *st = stage + threadIdx.x * (kNhKeRound + 1);
+    double up[4][4][9];  // upper blocks (a < b), entry i * 3 + k; only those indices are used
+#pragma unroll
+    for (int rnd = 0; rnd < (Ke ? 4 : 0); ++rnd) {
+        const int a = rnd;
+        double dg[9];
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    double v;
+                    if (b > a) {
+                        v = pp[a][k] * h[b][i] + qq[a][i] * h[b][k];
+                        if (i == k) v += G[a][b];
+                        up[a][b][i * 3 + k] = v;
+                    } else if (b == a) {
+                        if (k >= i) {
+                            v = pp[a][k] * h[a][i] + qq[a][i] * h[a][k];
+                            if (i == k) v += G[a][a];
+                            dg[i * 3 + k] = v;
+                        } else {
+                            v = dg[k * 3 + i];
+                        }
+                    } else {
+                        v = up[b][a][k * 3 + i];
+                    }
+                    st[i * 12 + b * 3 + k] = v;
+                }
+        __syncthreads();
+        for (int x = threadIdx.x; x < nvalid * kNhKeRound; x += kNhKeBlock) {
+            const int el = x / kNhKeRound, q = x - el * kNhKeRound;
+            Ke[(e0 + el) * 144 + rnd * kNhKeRound + q] = stage[el * (kNhKeRound + 1) + q];
+        }
+        __syncthreads();
+    }
+    if (re) {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) st[q] = r[q];
+        __syncthreads();
+        for (int x = threadIdx.x; x < nvalid * 12; x += kNhKeBlock) {
+            const int el = x / 12, q = x - el * 12;
+            re[(e0 + el) * 12 + q] = stage[el * (kNhKeRound + 1) + q];
+        }
+    }
 }
 
 // ------------------------------------------------------------------ row pass
@@ -270,17 +341,8 @@ __global__ void k_vector_gather(int64_t n_rows, const int32_t *__restrict__ inc_
 
 void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, const float *recf,
              const unsigned char *flags, double *d_residual, double *d_values, cudaStream_t s) {
-    if (recf) {
-        launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, d_residual, d_values,
-                                                  s);
-        launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, d_residual, d_values,
-                                                  s);
-    } else {
-        launch_nh_rows<false, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, nullptr, nullptr, d_residual,
-                                                   d_values, s);
-        launch_nh_rows<false, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, nullptr, nullptr, d_residual,
-                                                   d_values, s);
-    }
+    launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, d_residual, d_values, s);
+    launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, d_residual, d_values, s);
 }
 
 // Whole-array copies of the results to the host (paths without row chunks).
@@ -321,28 +383,22 @@ void nh_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const 
     require(d_p && d_t && d_u, "mesh or displacement arrays are NULL");
     DevBuf<double> u_stage;
     d_u = device_resident(d_u, pat->n_rows, u_stage, s);
-    if (d_values && pat->max_row_len > 0) {  // fused path
-        DevBuf<double> rec((size_t)ne * kNhRecD, s);
+    DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
+    auto elem = [&](int64_t e0, int64_t e1) {
+        k_nh_ke<<<grid_for(e1 - e0, kNhKeBlock), kNhKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t, pat->row_dofs.get(),
+                                                                    d_u, mu, lmbda, wsum, Ke.get(), re.get());
+        SKG_LAUNCH_CHECK("nh_ke");
+    };
+    if (d_values && pat->max_row_len > 0) {  // element matrices, then fixed-order row sums
         run_passes(
-            pat, ne, d_values, h_values, s,
-            [&](int64_t e0, int64_t e1) {
-                k_nh_plain_record<<<grid_for(e1 - e0, 128), 128, 0, s>>>(ne, e0, e1, d_p, npts, d_t,
-                                                                        pat->row_dofs.get(), d_u, mu, lmbda, wsum,
-                                                                        rec.get());
-                SKG_LAUNCH_CHECK("nh_plain_record");
-            },
+            pat, ne, d_values, h_values, s, elem,
             [&](const GroupSet &gs, cudaStream_t st) {
-                nh_rows(pat, gs, rec.get(), nullptr, nullptr, d_residual, d_values, st);
+                add_element_rows<12>(pat, Ke.get(), d_values, st, gs, re.get(), d_residual);
             },
             d_residual, h_residual);
         return;
     }
-    DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);
-    if (ne) {
-        k_nh_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum,
-                                                      Ke.get(), re.get());
-        SKG_LAUNCH_CHECK("nh_element");
-    }
+    if (ne) elem(0, ne);
     nh_gather(pat, Ke.get(), re.get(), d_residual, d_values, s);
     nh_download(pat, d_residual, d_values, h_residual, h_values, s);
 }

@@ -7,7 +7,9 @@
 // loads row a of K_e (N doubles, the next record's row one step ahead) and
 // adds it into its accumulator copy at the record's column offsets; the
 // warp sums the copies in copy order and writes the group's slot range with
-// coalesced stores.  No atomics: bitwise reproducible.
+// coalesced stores.  No atomics: bitwise reproducible.  Optionally the same
+// walk sums a per-incidence vector re (E * row_local, e.g. element residual
+// entries) into residual[row], the P parts combined in part order.
 #pragma once
 
 #include <algorithm>
@@ -24,8 +26,10 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
                                                            const int32_t *__restrict__ indptr,
                                                            const int32_t *__restrict__ inc_ptr,
                                                            const int4 *__restrict__ rec, const double *__restrict__ Ke,
-                                                           double *__restrict__ values) {
+                                                           double *__restrict__ values, const double *__restrict__ re,
+                                                           double *__restrict__ residual) {
     static_assert(N % 2 == 0 && N <= 12, "rows are loaded as 16-byte pairs, at most 12 columns");
+    static_assert(P == 1 || P == 2, "one or two accumulator copies");
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gi = blockIdx.x * kRowWarps + warp;
@@ -38,7 +42,9 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
     __syncwarp();
     const int ridx = lane / P, part = lane - (lane / P) * P;
     const int32_t r = grp.x + ridx;
-    if (ridx < 32 / P && r < grp.y) {
+    const bool live = ridx < 32 / P && r < grp.y;
+    double rsum = 0.0;
+    if (live) {
         const int base = indptr[r] - s0 + part * nslots;
         const int32_t it1 = inc_ptr[r + 1];
         int32_t it = inc_ptr[r] + part;
@@ -60,6 +66,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
 #pragma unroll
                     for (int q = 0; q < N / 2; ++q) nxt[q] = __ldg(src + q);
                 }
+                if (re) rsum += __ldg(re + rc.x);
                 const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
                 int off[N];
 #pragma unroll
@@ -80,6 +87,10 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
             }
         }
     }
+    if (re) {  // uniform across the warp: every lane takes part in the shuffle
+        if constexpr (P == 2) rsum += __shfl_down_sync(0xffffffffu, rsum, 1);
+        if (live && part == 0) residual[r] = rsum;
+    }
     __syncwarp();
     for (int j = lane; j < nslots; j += 32) {
         double v = acc[j];
@@ -91,7 +102,8 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
 
 template <int N, int SLOTS, int P>
 inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern *pat, const double *Ke,
-                            double *values, cudaStream_t s) {
+                            double *values, cudaStream_t s, const double *re = nullptr,
+                            double *residual = nullptr) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kRowWarps * SLOTS * 8;
     if (smem > 48 * 1024)
@@ -99,7 +111,8 @@ inline void launch_ke_class(int n_groups, const int2 *groups, const skg_pattern 
                                       (int)smem));
     const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
     k_rows_ke<N, SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
-                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values);
+                                                              pat->inc_ptr.get(), pat->rec.get(), Ke, values, re,
+                                                              residual);
     SKG_LAUNCH_CHECK("rows_ke");
 }
 
@@ -118,9 +131,9 @@ inline GroupSet chunk_groups(const skg_pattern *pat, int c) {
 // row groups (pat->max_row_len > 0, square N x N element blocks).
 template <int N>
 inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *values, cudaStream_t s,
-                             const GroupSet &gs) {
-    launch_ke_class<N, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Ke, values, s);
-    launch_ke_class<N, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Ke, values, s);
+                             const GroupSet &gs, const double *re = nullptr, double *residual = nullptr) {
+    launch_ke_class<N, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Ke, values, s, re, residual);
+    launch_ke_class<N, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Ke, values, s, re, residual);
 }
 
 // Per-device non-blocking side streams of the assembly passes.

@@ -174,9 +174,9 @@ class NeoHookean:
     def assemble(self, u, surrogate=None, tol=1e-3):
         """(residual vector, tangent csr_matrix) at displacement u (N,).  The
         tangent matrix is reused between calls.  A host u is read by the device in
-        place when it can (the library copies it to the device first); on a
-        row-grouped pattern the row pass writes the residual and the CSR values
-        straight into page-locked host buffers, else they are copied there."""
+        place when it can (the library copies it to the device first); the
+        residual and the CSR values reach page-locked host buffers row chunk by
+        row chunk while the later chunks are computed."""
         if hasattr(u, "data_ptr"):
             self.assemble_device(u, surrogate=surrogate, tol=tol)
             K = self.target.download()
@@ -189,14 +189,8 @@ class NeoHookean:
             u_ptr = dev.ptr(keep)
         if self._res_pinned is None:
             self._res_pinned, self._res_host = dev.pinned_empty(max(1, self.basis.N))
-        res_host = ctypes.c_void_p(self._res_pinned.data_ptr())
-        if self.pattern.blocked:
-            # the row pass writes every residual entry and CSR value once, and
-            # is long enough to carry the writes over the host link itself
-            self._launch(u_ptr, surrogate, tol, res_host, self.target.pinned_ptr(), True)
-        else:
-            self._launch(u_ptr, surrogate, tol, dev.ptr(self.d_res), dev.ptr(self.target.d_values), True,
-                         host=(res_host, self.target.pinned_ptr()))
+        self._launch(u_ptr, surrogate, tol, dev.ptr(self.d_res), dev.ptr(self.target.d_values), True,
+                     host=(ctypes.c_void_p(self._res_pinned.data_ptr()), self.target.pinned_ptr()))
         K = self.target.finish_direct()
         del keep
         return dev.host_copy(self._res_host[: self.basis.N]), K
