@@ -237,6 +237,9 @@ def measured_peak():
 # FP64 instructions per element of the FP64 passes (DFMA + DMUL + DADD thread
 # instructions counted by ncu on the 32^3 case, profiles/fp64_ops_p2_aniso_32.md).
 FP64_OPS_PER_ELEMENT = {"k_elem_ke_fp64": 293.1, "k_rows_ke": 111.1}
+# The same for the plain neo-Hookean call (profiles/fp64_ops_nh_32.md):
+# element matrices k_nh_ke + row pass k_rows_ke<12>.
+NH_FP64_OPS_PER_ELEMENT = 535.1 + 180.0
 
 
 def fp64_roof(call, passes, elements):
@@ -628,6 +631,23 @@ def wl_p1_adjoint(args, world, timed, wall):
         roofline=_roofline(alg, ms), gpu_launches=5 * args.steps)
 
 
+def _nh_fp64(elements, ms):
+    peak = _fp64_rate()
+    achieved = NH_FP64_OPS_PER_ELEMENT * elements / (ms * 1e-3) / 1e9
+    return {"ops_per_element": NH_FP64_OPS_PER_ELEMENT, "achieved_gops": achieved, "peak_gops": peak,
+            "frac": achieved / peak, "peak_source": "skg_fp64_fma_rate, measured in this run"}
+
+
+def _fp64_rate():
+    import ctypes
+
+    from skfemntv_gb300._native import call
+
+    rate = ctypes.c_double()
+    call("skg_fp64_fma_rate", ctypes.byref(rate), None)
+    return rate.value
+
+
 def wl_nh(args, world, timed, wall):
     """Vector P1 neo-Hookean residual + tangent, 64^3 x 6 cube, mu = 1, lambda = 10:
     plain FP64 law against the GPU-trained MLP energy surrogate."""
@@ -674,7 +694,7 @@ def wl_nh(args, world, timed, wall):
                 "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
         e2e={"value": world * E / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": 8 * b.N,
              "d2h_bytes_per_step": 8 * (b.N + nnz), "ms_per_step": 1e3 * e2e_s},
-        roofline=_roofline(alg, ms_plain),
+        roofline=dict(_roofline(alg, ms_plain), fp64_pipe=_nh_fp64(E, ms_plain)),
         learned_closure={"value": world * E / (ms_sur * 1e-3), "ms_per_step": ms_sur,
                          "speedup_vs_plain": ms_plain / ms_sur, "max_rel_err_residual": err_r,
                          "max_rel_err_tangent": err_k, "fallback_elements": fallback,
