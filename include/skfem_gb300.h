@@ -340,7 +340,9 @@ int skg_p1_energy(const double *d_p, int64_t npts, const int32_t *d_t,
 /* Gradients of grad_out * J: d_gkappa (E), d_gp (3, npts) (needs the
  * incidence-only handle of the vertex connectivity, d_t^T with npts rows),
  * d_gu / d_gv (N) (needs the incidence-only handle of the DOF map); any
- * output may be NULL.  Geometry is recomputed, nothing is kept from the
+ * output may be NULL.  When the DOFs are the vertices (scalar P1, every
+ * vertex a DOF) the same handle may be passed twice: all gradients are then
+ * gathered in one walk.  Geometry is recomputed, nothing is kept from the
  * forward call. */
 int skg_p1_energy_grad(const skg_pattern *vertex_incidence,
                        const skg_pattern *dof_incidence, const double *d_p,

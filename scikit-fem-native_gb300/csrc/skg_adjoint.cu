@@ -100,13 +100,15 @@ __global__ void __launch_bounds__(kRed) k_energy(int64_t ne, const double *__res
     if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
 }
 
+// One warp, fixed order: lane l sums the block sums l, l + 32, ... in turn,
+// then the lanes are combined by a fixed shuffle tree.
 __global__ void k_sum_blocks(const double *__restrict__ in, int64_t n, double *__restrict__ out) {
-    // one thread, fixed order (n is the number of forward blocks)
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int64_t i = 0; i < n; ++i) s += in[i];
-        *out = s;
-    }
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    for (int64_t i = lane; i < n; i += 32) s += in[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) *out = s;
 }
 
 // Backward, element pass: dJ/dkappa and the per-element vertex / DOF
@@ -165,36 +167,36 @@ __global__ void k_energy_grad_elem(int64_t ne, const double *__restrict__ p, int
 
 // Backward, gather pass: one thread per row of an incidence list (vertex or
 // DOF), summing the element contributions in element order.
-//   mode 0: coordinates -> out (3, n_rows) (component-major like mesh.p)
-//   mode 1: u / v DOFs  -> out_u (n_rows), out_v (n_rows)
+//   coordinates (out_x, (3, n_rows), component-major like mesh.p) and / or
+//   u / v DOFs (out_u, out_v (n_rows)); both in one walk when the vertex and
+//   DOF incidence lists coincide (scalar P1 with every vertex a DOF).
 __global__ void k_energy_grad_gather(int64_t n_rows, const int32_t *__restrict__ inc_ptr,
-                                     const int32_t *__restrict__ inc, const double *__restrict__ contrib, int mode,
-                                     double *__restrict__ out0, double *__restrict__ out1) {
+                                     const int32_t *__restrict__ inc, const double *__restrict__ contrib,
+                                     double *__restrict__ out_x, double *__restrict__ out_u,
+                                     double *__restrict__ out_v) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_rows) return;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, su = 0.0, sv = 0.0;
     for (int32_t it = inc_ptr[r]; it < inc_ptr[r + 1]; ++it) {
         const int32_t item = inc[it];
         const int64_t e = item >> 2;
         const int k = item & 3;
         const double *c = contrib + e * 20;
-        if (mode == 0) {
+        if (out_x) {
             s0 += c[k * 3];
             s1 += c[k * 3 + 1];
             s2 += c[k * 3 + 2];
-        } else {
-            s0 += c[12 + k];
-            s1 += c[16 + k];
         }
+        if (out_u) su += c[12 + k];
+        if (out_v) sv += c[16 + k];
     }
-    if (mode == 0) {
-        out0[r] = s0;
-        out0[n_rows + r] = s1;
-        out0[2 * n_rows + r] = s2;
-    } else {
-        if (out0) out0[r] = s0;
-        if (out1) out1[r] = s1;
+    if (out_x) {
+        out_x[r] = s0;
+        out_x[n_rows + r] = s1;
+        out_x[2 * n_rows + r] = s2;
     }
+    if (out_u) out_u[r] = su;
+    if (out_v) out_v[r] = sv;
 }
 
 }  // namespace
@@ -240,15 +242,23 @@ extern "C" int skg_p1_energy_grad(const skg_pattern *vertex_inc, const skg_patte
                                                                  grad_out, d_gkappa, contrib.get());
             SKG_LAUNCH_CHECK("energy_grad_elem");
         }
+        const bool shared = vertex_inc == dof_inc;  // one incidence structure for both
+        if (d_gp && shared) {
+            k_energy_grad_gather<<<grid_for(npts, 128), 128, 0, s>>>(npts, vertex_inc->inc_ptr.get(),
+                                                                     vertex_inc->inc.get(), contrib.get(), d_gp, d_gu,
+                                                                     d_gv);
+            SKG_LAUNCH_CHECK("energy_grad_xuv");
+            return;
+        }
         if (d_gp) {
             k_energy_grad_gather<<<grid_for(npts, 128), 128, 0, s>>>(npts, vertex_inc->inc_ptr.get(),
-                                                                     vertex_inc->inc.get(), contrib.get(), 0, d_gp,
-                                                                     nullptr);
+                                                                     vertex_inc->inc.get(), contrib.get(), d_gp,
+                                                                     nullptr, nullptr);
             SKG_LAUNCH_CHECK("energy_grad_x");
         }
         if (d_gu || d_gv) {
             k_energy_grad_gather<<<grid_for(dof_inc->n_rows, 128), 128, 0, s>>>(
-                dof_inc->n_rows, dof_inc->inc_ptr.get(), dof_inc->inc.get(), contrib.get(), 1, d_gu, d_gv);
+                dof_inc->n_rows, dof_inc->inc_ptr.get(), dof_inc->inc.get(), contrib.get(), nullptr, d_gu, d_gv);
             SKG_LAUNCH_CHECK("energy_grad_uv");
         }
     });

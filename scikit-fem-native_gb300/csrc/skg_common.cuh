@@ -180,6 +180,7 @@ constexpr int kGroupSlotsLarge = 2048;
 // Row chunks of the host-output paths (values copied to host memory chunk by
 // chunk while later chunks are computed).
 constexpr int kHostChunks = 16;
+constexpr int64_t kHostChunkMinNnz = int64_t(1) << 22;  // 32 MiB of values
 }  // namespace skg
 
 // Pattern handle (defined here so every translation unit sees the layout).

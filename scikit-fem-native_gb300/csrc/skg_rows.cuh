@@ -191,7 +191,9 @@ inline void add_element_rows(const skg_pattern *pat, const double *Ke, double *v
 // the row pass of a group set on stream st.  The values optionally go to
 // the page-locked host array h_values as well.
 //
-// Device output: elem(0, ne), then the row pass of all groups on s.
+// Device output, or a host output of fewer than kHostChunkMinNnz values
+// (where the chunks' launches and events would cost more than the overlap
+// gains): elem(0, ne), the row pass of all groups on s, then one copy.
 // Host output: the row chunks are taken in the order in which their elements
 // are complete (hc_ready).  The element pass runs on s in steps of at least
 // ne / kHostChunks elements, so launches stay large; each chunk's row pass
@@ -205,9 +207,14 @@ template <class FE, class FR>
 void run_passes(const skg_pattern *pat, int64_t ne, double *d_values, double *h_values, cudaStream_t s, FE &&elem,
                 FR &&rows, const double *d_rowvec = nullptr, double *h_rowvec = nullptr) {
     EventSet ev;
-    if (!h_values) {
+    if (!h_values || pat->nnz < kHostChunkMinNnz) {
         if (ne) elem((int64_t)0, ne);
         rows_on(all_groups(pat), s, ev, rows);
+        if (h_values && pat->nnz)
+            SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (h_values && d_rowvec && h_rowvec && pat->n_rows)
+            SKG_CUDA(cudaMemcpyAsync(h_rowvec, d_rowvec, (size_t)pat->n_rows * sizeof(double), cudaMemcpyDeviceToHost,
+                                     s));
         return;
     }
     const int n_chunks = (int)pat->hc_ready.size();

@@ -35,7 +35,10 @@ class P1Energy:
         self.dofs = basis._dev_dofs()                  # (E, 4)
         vt = self.t.t().contiguous()                   # (E, 4) vertex ids
         self.vertex_inc = Pattern(vt, None, self.E, 4, 0, self.npts, 0)
-        self.dof_inc = Pattern(self.dofs, None, self.E, 4, 0, basis.N, 0)
+        if basis.N == self.npts and np.array_equal(basis.element_dofs, mesh.t):
+            self.dof_inc = self.vertex_inc             # DOFs are the vertices: one gather walk
+        else:
+            self.dof_inc = Pattern(self.dofs, None, self.E, 4, 0, basis.N, 0)
         self.wsum = float(np.sum(basis.W))
 
     def __call__(self, kappa, coords, u, v):

@@ -87,3 +87,20 @@ def test_gradient_matches_own_fd_and_is_deterministic():
     fd = (op.energy(kt + h * d, pt, ut, vt) - op.energy(kt - h * d, pt, ut, vt)).item() / (2 * h)
     an = float((g1[0] * d).sum())
     assert abs(an - fd) <= 1e-7 * max(1.0, abs(an))
+
+
+def test_shared_and_separate_incidence_walks_agree():
+    """Scalar P1 (DOFs = vertices) gathers all gradients in one walk over the
+    vertex incidences; the two-walk path over separate handles gives the same
+    bits."""
+    from skfemntv_gb300.assembly import Pattern
+
+    mesh, basis, kappa, u, v = problem(n=3, seed=5)
+    kt, pt, ut, vt = (cuda(a) for a in (kappa, mesh.p, u, v))
+    op = sk.P1Energy(basis)
+    assert op.dof_inc is op.vertex_inc
+    g1 = op.gradients(kt, pt, ut, vt)
+    op.dof_inc = Pattern(op.dofs, None, op.E, 4, 0, basis.N, 0)
+    g2 = op.gradients(kt, pt, ut, vt)
+    for a, b in zip(g1, g2):
+        assert torch.equal(a, b)

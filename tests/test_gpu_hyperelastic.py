@@ -167,12 +167,13 @@ def test_surrogate_speed_against_plain_law(surrogate):
     assert t_sur < 1.15 * t_plain
 
 
-def test_host_output_matches_device(surrogate):
-    """The host-output path (element and row passes over row chunks, results
-    copied chunk by chunk, u read from host memory) returns exactly the device
-    path's residual and tangent, for the plain law, the surrogate and the
-    all-fallback surrogate."""
-    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 17),) * 3)
+@pytest.mark.parametrize("cells", [16, 34])
+def test_host_output_matches_device(surrogate, cells):
+    """The host-output path (u read from host memory; at 34^3, 5.4 M values,
+    element and row passes over row chunks with the results copied chunk by
+    chunk) returns exactly the device path's residual and tangent, for the
+    plain law, the surrogate and the all-fallback surrogate."""
+    m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, cells + 1),) * 3)
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
     nh = sk.NeoHookean(b, 1.0, 10.0)
     u = sine_displacement(b)

@@ -421,16 +421,17 @@ def test_cross_basis_assembly_matches_reference():
         cf.assemble("row_divergence", 1.0)
 
 
-@pytest.mark.parametrize("element", ["p1", "p2"])
+@pytest.mark.parametrize("element,cells", [("p1", 16), ("p2", 16), ("p2", 28)])
 @pytest.mark.parametrize("precision", ["fp64", "fp64_emulated", "split_fp32"])
-def test_host_output_matches_device(element, precision):
-    """The host-output path (element and row passes interleaved over row chunks,
-    each chunk's values copied while later chunks run) writes exactly the
-    values of the device path, on a mesh large enough for every chunk."""
+def test_host_output_matches_device(element, cells, precision):
+    """The host-output path writes exactly the values of the device path: one
+    copy after the passes for small outputs (16^3), and at 28^3 (5.1 M values,
+    above the chunking threshold) the element and row passes interleaved over
+    16 row chunks, each chunk's values copied while later chunks run."""
     from skfemntv_gb300.assembly import NativeTensorForm
 
     g = load_golden("p2_aniso")
-    axis = np.linspace(0.0, 1.0, 17)
+    axis = np.linspace(0.0, 1.0, cells + 1)
     m = sk.MeshTet.init_tensor(axis, axis, axis)
     if element == "p2":
         b = sk.Basis(sk.MeshTet2.from_mesh(m), sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(g["X"], g["W"]))
@@ -448,11 +449,13 @@ def test_host_output_matches_device(element, precision):
     assert np.allclose(K2.data, 2.0 * D, rtol=1e-14, atol=0)
 
 
+@pytest.mark.parametrize("cells", [12, 34])
 @pytest.mark.parametrize("precision", ["fp64", "split_fp32"])
-def test_n1_host_output_matches_device(precision):
-    """N1 Maxwell through the host-output path (chunked copies, per-element
-    curl coefficient read from host memory) equals the device path bit for bit."""
-    axis = np.linspace(0.0, 1.0, 13)
+def test_n1_host_output_matches_device(precision, cells):
+    """N1 Maxwell through the host-output path (per-element curl coefficient
+    read from host memory; at 34^3, 4.6 M values, copies per row chunk) equals
+    the device path bit for bit."""
+    axis = np.linspace(0.0, 1.0, cells + 1)
     mesh = sk.MeshTet.init_tensor(axis, axis, axis)
     asmb = sk.TetN1Assembler(sk.AffineTetN1Basis(mesh))
     nu = np.exp(np.random.default_rng(3).normal(0.0, 0.3, mesh.nelements))[:, None]
