@@ -111,6 +111,12 @@ class ClockSampler:
     def __exit__(self, *exc):
         self.lines = []
         if self.proc is not None:
+            # a timed region shorter than the sampling period: keep the sampler
+            # until one sample from after its start is in (at most 0.5 s)
+            t_end = time.perf_counter() + 0.5
+            while (not any(t >= self.t_start for t, _ in self.samples) and time.perf_counter() < t_end
+                   and self.proc.poll() is None):
+                time.sleep(0.005)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
