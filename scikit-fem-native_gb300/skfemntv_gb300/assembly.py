@@ -49,8 +49,9 @@ class Pattern:
         self.n_rows, self.n_cols = n_rows, n_cols
         mrl = ctypes.c_int32(0)
         call("skg_pattern_row_groups", h, ctypes.byref(mrl))
-        # fused row passes write every CSR value once, so they may write host memory directly
-        self.blocked = mrl.value > 0
+        # the fixed-order row-group passes (and their chunked host outputs) serve
+        # this pattern; otherwise assemblies gather per row from global memory
+        self.row_groups = mrl.value > 0
 
     def device_csr(self):
         """(crow_indices, col_indices) int64 CUDA tensors of the pattern (cached)."""

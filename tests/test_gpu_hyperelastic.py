@@ -176,6 +176,7 @@ def test_host_output_matches_device(surrogate, cells):
     m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, cells + 1),) * 3)
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
     nh = sk.NeoHookean(b, 1.0, 10.0)
+    assert nh.pattern.row_groups
     u = sine_displacement(b)
     du = torch.as_tensor(u, dtype=torch.float64, device="cuda")
     import ctypes

@@ -442,6 +442,7 @@ def test_host_output_matches_device(element, cells, precision):
     A = M @ np.swapaxes(M, 1, 2) + 3.0 * np.eye(3)
     Apub = np.broadcast_to(np.moveaxis(A, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
     form = NativeTensorForm(b)
+    assert form.pattern.row_groups  # the fixed-order row-group passes serve this pattern
     K = form.assemble(Apub, precision=precision, copy=True)
     D = form.assemble_device(Apub, precision=precision)[:K.nnz].cpu().numpy()
     assert np.array_equal(K.data.view(np.int64), D.view(np.int64))
@@ -458,6 +459,7 @@ def test_n1_host_output_matches_device(precision, cells):
     axis = np.linspace(0.0, 1.0, cells + 1)
     mesh = sk.MeshTet.init_tensor(axis, axis, axis)
     asmb = sk.TetN1Assembler(sk.AffineTetN1Basis(mesh))
+    assert asmb.pattern.row_groups
     nu = np.exp(np.random.default_rng(3).normal(0.0, 0.3, mesh.nelements))[:, None]
     K = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=nu, precision=precision)
     D = asmb.assemble_maxwell_torch(mass_coefficient=1.0, curl_coefficient=nu, precision=precision)
