@@ -208,7 +208,7 @@ extern "C" int skg_p1_energy(const double *d_p, int64_t npts, const int32_t *d_t
                              const double *d_kappa, const double *d_u, const double *d_v, double wsum, double *d_out,
                              void *stream) {
     return guarded([&] {
-        require(ne >= 0 && d_p && d_t && d_dofs && d_u && d_v && d_out, "invalid energy arguments");
+        require(ne >= 0 && d_out && (ne == 0 || (d_p && d_t && d_dofs && d_u && d_v)), "invalid energy arguments");
         cudaStream_t s = as_stream(stream);
         const int64_t nb = ne ? (ne + kRed - 1) / kRed : 1;
         DevBuf<double> partial(nb, s);
@@ -229,7 +229,7 @@ extern "C" int skg_p1_energy_grad(const skg_pattern *vertex_inc, const skg_patte
                                   double grad_out, double *d_gkappa, double *d_gp, double *d_gu, double *d_gv,
                                   void *stream) {
     return guarded([&] {
-        require(ne >= 0 && d_p && d_t && d_dofs && d_u && d_v, "invalid energy arguments");
+        require(ne >= 0 && (ne == 0 || (d_p && d_t && d_dofs && d_u && d_v)), "invalid energy arguments");
         require(!d_gp || (vertex_inc && vertex_inc->row_local == 4 && vertex_inc->n_elements == ne &&
                           vertex_inc->n_rows == npts),
                 "coordinate gradients need the vertex incidence handle of this mesh");

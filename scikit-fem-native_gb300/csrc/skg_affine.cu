@@ -983,11 +983,11 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     require(nodes == 4 || nodes == 10, "affine assembly supports P1 (4) and P2 (10) tetrahedra");
     require(ne == pat->n_elements && pat->row_local == nodes && pat->col_local == nodes,
             "mesh does not match the pattern");
-    require(coef_kind == 0 || ((coef_kind == 1 || coef_kind == 2) && d_coef), "invalid coefficient kind");
+    require(coef_kind == 0 || ((coef_kind == 1 || coef_kind == 2) && (d_coef || ne == 0)), "invalid coefficient kind");
     require(precision == SKG_FP64 || precision == SKG_SPLIT_FP32 || precision == SKG_FP64_EMULATED,
             "invalid precision");
     require(nq > 0 && h_X && h_W, "quadrature rule is empty");
-    require(d_p && d_t, "mesh arrays are NULL");
+    require(ne == 0 || (d_p && d_t), "mesh arrays are NULL");
     std::vector<double> T;
     Support sp{};
     affine_table(nodes, nq, h_X, h_W, T, sp);
@@ -1256,11 +1256,11 @@ extern "C" int skg_h1_assemble_affine_noalloc(const skg_pattern *pat, const doub
                 "allocation-free assembly supports at most " + std::to_string(kNoAllocMaxElements) +
                     " elements (its scratch array is fixed); got " + std::to_string(ne) +
                     ": use skg_h1_assemble_affine");
-        require(coef_kind == 0 || ((coef_kind == 1 || coef_kind == 2) && d_coef), "invalid coefficient kind");
+        require(coef_kind == 0 || ((coef_kind == 1 || coef_kind == 2) && (d_coef || ne == 0)), "invalid coefficient kind");
         require(precision == SKG_FP64 || precision == SKG_SPLIT_FP32 || precision == SKG_FP64_EMULATED,
                 "invalid precision");
         require(nq > 0 && h_X && h_W, "quadrature rule is empty");
-        require(d_p && d_t, "mesh arrays are NULL");
+        require(ne == 0 || (d_p && d_t), "mesh arrays are NULL");
         cudaStream_t s = as_stream(stream);
         unsigned char *base = noalloc_base();
         double *G = reinterpret_cast<double *>(base);

@@ -112,7 +112,7 @@ extern "C" int skg_tabulate_geometry(const double *d_p, int64_t npts, const int3
     return guarded([&] {
         require(nq > 0 && nodes > 0 && gnodes > 0 && ne >= 0, "invalid basis geometry sizes");
         require(h_shape && h_refgrad && h_gshape && h_grefgrad && h_w, "reference tables are NULL");
-        require(d_p && d_t, "mesh arrays are NULL");
+        require(ne == 0 || (d_p && d_t), "mesh arrays are NULL");
         if (h_bad) { h_bad[0] = -1; h_bad[1] = -1; h_bad[2] = 0; }
         cudaStream_t s = as_stream(stream);
         const int total = nq * nodes * 4 + nq * gnodes * 4 + nq;

@@ -200,11 +200,12 @@ extern "C" int skg_h1_assemble_tabulated(const skg_pattern *pat, const int32_t *
                                          void *stream) {
     return guarded([&] {
         require(pat != nullptr, "pattern is NULL");
-        require(d_value || d_gradient || d_symgrad || d_div, "at least one coefficient is required");
         const int L = nodes * comp;
         require(nodes > 0 && comp > 0 && nq > 0 && ne == pat->n_elements && L == pat->row_local &&
                     L == pat->col_local,
                 "tabulated arrays do not match the pattern");
+        if (ne == 0) return;  // no elements: no CSR entries
+        require(d_value || d_gradient || d_symgrad || d_div, "at least one coefficient is required");
         require(d_grad && d_w && (!d_value || d_shape), "tabulated geometry arrays are NULL");
         (void)d_dofs;
         cudaStream_t s = as_stream(stream);
@@ -229,11 +230,12 @@ extern "C" int skg_h1_assemble_tensor_tabulated(const skg_pattern *pat, const in
                                                 double *d_scratch, void *stream) {
     return guarded([&] {
         require(pat != nullptr, "pattern is NULL");
-        require(d_coef && d_grad && d_w, "tensor coefficient or geometry is NULL");
         const int L = nodes * comp;
         require(nodes > 0 && comp > 0 && nq > 0 && ne == pat->n_elements && L == pat->row_local &&
                     L == pat->col_local,
                 "tabulated arrays do not match the pattern");
+        if (ne == 0) return;  // no elements: no CSR entries
+        require(d_coef && d_grad && d_w, "tensor coefficient or geometry is NULL");
         (void)d_dofs;
         cudaStream_t s = as_stream(stream);
         DevBuf<double> tmp;
@@ -263,6 +265,7 @@ extern "C" int skg_cross_assemble_tabulated(const skg_pattern *pat, int64_t ne, 
                 "tabulated arrays do not match the pattern");
         require((row_kind == 0 || row_kind == 1) && (col_kind == 0 || col_kind == 1),
                 "tensor kind must be value or gradient");
+        if (ne == 0) return;  // no elements: no CSR entries
         require((row_kind == 0 ? d_t_shape : d_t_grad) && (col_kind == 0 ? d_c_shape : d_c_grad) && d_dx && d_coef,
                 "tabulated geometry or coefficient arrays are NULL");
         cudaStream_t s = as_stream(stream);

@@ -491,7 +491,7 @@ extern "C" int skg_n1_assemble(const skg_pattern *pat, const double *d_p, int64_
         require(pat != nullptr, "pattern is NULL");
         require(ne == pat->n_elements && pat->row_local == 6 && pat->col_local == 6, "mesh does not match the pattern");
         require(nq > 0 && h_X && h_W, "quadrature rule is empty");
-        require(d_p && d_t && d_signs, "mesh arrays are NULL");
+        require(ne == 0 || (d_p && d_t && d_signs), "mesh arrays are NULL");
         (void)d_elem_edges;
         n1_assemble(pat, d_p, npts, d_t, d_signs, ne, nq, h_X, h_W, d_mass, d_curl, include_mass, include_curl,
                     precision, d_values, nullptr, as_stream(stream));
@@ -507,7 +507,7 @@ extern "C" int skg_n1_assemble_host(const skg_pattern *pat, const double *d_p, i
         require(pat != nullptr, "pattern is NULL");
         require(ne == pat->n_elements && pat->row_local == 6 && pat->col_local == 6, "mesh does not match the pattern");
         require(nq > 0 && h_X && h_W, "quadrature rule is empty");
-        require(d_p && d_t && d_signs, "mesh arrays are NULL");
+        require(ne == 0 || (d_p && d_t && d_signs), "mesh arrays are NULL");
         require(d_values && h_values, "device staging or host output is NULL");
         (void)d_elem_edges;
         n1_assemble(pat, d_p, npts, d_t, d_signs, ne, nq, h_X, h_W, d_mass, d_curl, include_mass, include_curl,

@@ -380,7 +380,7 @@ void nh_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const 
     require(pat != nullptr, "pattern is NULL");
     require(pat->row_local == 12 && pat->n_elements == ne, "neo-Hookean assembly needs the vector P1 pattern");
     require(!d_values || pat->col_local == 12, "tangent output needs a pattern with CSR columns");
-    require(d_p && d_t && d_u, "mesh or displacement arrays are NULL");
+    require(ne == 0 || (d_p && d_t && d_u), "mesh or displacement arrays are NULL");
     DevBuf<double> u_stage;
     d_u = device_resident(d_u, pat->n_rows, u_stage, s);
     DevBuf<double> Ke(d_values ? (size_t)ne * 144 : 0, s), re(d_residual ? (size_t)ne * 12 : 0, s);

@@ -50,12 +50,17 @@ extern "C" int skg_linear_assemble_tabulated(const skg_pattern *pat, const int32
                                              const double *d_gradient, double *d_out, void *stream) {
     return guarded([&] {
         require(pat != nullptr, "pattern is NULL");
-        require(d_value || d_gradient, "at least one coefficient is required");
         require(ne == pat->n_elements && pat->row_local == nodes * comp, "tabulated arrays do not match the pattern");
-        require(d_w && (!d_value || d_shape) && (!d_gradient || d_grad), "tabulated geometry arrays are NULL");
         (void)d_dofs;
         cudaStream_t s = as_stream(stream);
         if (!pat->n_rows) return;
+        if (ne == 0) {  // no elements: a zero vector
+            require(d_out != nullptr, "output is NULL");
+            SKG_CUDA(cudaMemsetAsync(d_out, 0, (size_t)pat->n_rows * sizeof(double), s));
+            return;
+        }
+        require(d_value || d_gradient, "at least one coefficient is required");
+        require(d_w && (!d_value || d_shape) && (!d_gradient || d_grad), "tabulated geometry arrays are NULL");
         k_linear_rows<<<grid_for(pat->n_rows, 128), 128, 0, s>>>(pat->n_rows, pat->inc_ptr.get(), pat->inc.get(), nodes,
                                                                  comp, nq, d_shape, d_grad, d_w, d_value, d_gradient,
                                                                  d_out);

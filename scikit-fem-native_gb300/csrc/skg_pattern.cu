@@ -353,7 +353,9 @@ extern "C" int skg_pattern_create(const int32_t *d_row_dofs, const int32_t *d_co
     return guarded([&] {
         require(out != nullptr, "output handle pointer is NULL");
         *out = nullptr;
-        const bool with_csr = d_col_dofs != nullptr;
+        // CSR columns when column DOFs are given (for an empty mesh, whose arrays
+        // may be NULL, when the column width is)
+        const bool with_csr = d_col_dofs != nullptr || (n_elements == 0 && col_local > 0);
         if (!with_csr) col_local = 0;
         require(n_elements >= 0 && row_local > 0 && (col_local > 0 || !with_csr), "invalid pattern sizes");
         require(n_rows >= 0 && n_cols >= 0, "invalid matrix shape");
