@@ -540,6 +540,14 @@ def wl_p1_laplace(args, world, timed, wall):
         variants[mode] = {"value": world * nnz / (ms * 1e-3), "ms_per_step": ms,
                           "max_rel_err_vs_fp64": _relerr(vals, ref), "clocks": clk}
 
+    # the same FP64 assembly replayed from a CUDA graph (per-element kappa on the device)
+    import torch
+
+    kappa = torch.ones(E, dtype=torch.float64, device="cuda")
+    graph = form.capture_gradient(kappa)
+    ms_g, clk_g = timed(graph.replay, flush_l2=True)
+    graph_err = _relerr(form.target.d_values[:nnz], ref)
+
     @sk.BilinearForm
     def lap(u, v, w):
         return sk.ddot(sk.grad(u), sk.grad(v))
@@ -555,6 +563,8 @@ def wl_p1_laplace(args, world, timed, wall):
         e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 0,
              "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
         roofline=_roofline(alg, head["ms_per_step"]), precision_variants=variants,
+        cuda_graph={"value": world * nnz / (ms_g * 1e-3), "ms_per_step": ms_g, "max_rel_err_vs_fp64": graph_err,
+                    "clocks": clk_g, "note": "NativeBilinearForm.capture_gradient, replay() per step"},
         gpu_launches=3 * args.steps)
 
 

@@ -991,8 +991,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     std::vector<double> T;
     Support sp{};
     affine_table(nodes, nq, h_X, h_W, T, sp);
-    DevBuf<double> Tg(T.size(), s);
-    SKG_CUDA(cudaMemcpyAsync(Tg.get(), T.data(), T.size() * 8, cudaMemcpyHostToDevice, s));
+    const double *Tg = device_table(T.data(), T.size(), s);
     DevBuf<double> G((size_t)ne * 16, s);  // 16 doubles or 16 df64 pairs per element
     const bool blocked = pat->max_row_len > 0;
     const bool exact = nodes == 10 && blocked && precision != SKG_FP64 && p2_rule_is_exact(T);
@@ -1053,7 +1052,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             pat, ne, d_values, h_values, s,
             [&](int64_t e0, int64_t e1) {
                 k_elem_ke_fp64<<<grid_for(e1 - e0, kKeBlock), kKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t, coef_kind,
-                                                                             d_coef, Tg.get(), Ke.get());
+                                                                             d_coef, Tg, Ke.get());
                 SKG_LAUNCH_CHECK("elem_ke_fp64");
                 if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
             },
@@ -1075,18 +1074,18 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         if (nodes == 4)
             k_rows_global<4><<<grid, 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
                                                   pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(), G.get(),
-                                                  Tg.get(), sp, d_values);
+                                                  Tg, sp, d_values);
         else
             k_rows_global<10><<<grid, 128, 0, s>>>(pat->n_rows, pat->indptr.get(), pat->indices.get(),
                                                    pat->inc_ptr.get(), pat->inc.get(), pat->col_dofs.get(), G.get(),
-                                                   Tg.get(), sp, d_values);
+                                                   Tg, sp, d_values);
         SKG_LAUNCH_CHECK("rows_global");
         if (h_values && pat->nnz)
             SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
     } else {
         const int *sp_ptr = misc.get();
         run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs, cudaStream_t st) {
-#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg.get(), sp_ptr, d_values, st, gs)
+#define SKG_ROWS(NN, MM) launch_rows_groups<NN, MM>(pat, G.get(), Tg, sp_ptr, d_values, st, gs)
             if (nodes == 4) {
                 if (mode == MODE_FP64) SKG_ROWS(4, MODE_FP64);
                 else if (mode == MODE_SPLIT) SKG_ROWS(4, MODE_SPLIT);
@@ -1094,7 +1093,7 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
             } else {
                 if (mode == MODE_FP64) SKG_ROWS(10, MODE_FP64);
                 else if (mode == MODE_SPLIT) {
-                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg.get(), sp_ptr, d_values, st, gs);
+                    if (exact) launch_rows_groups<10, MODE_SPLIT, true>(pat, G.get(), Tg, sp_ptr, d_values, st, gs);
                     else SKG_ROWS(10, MODE_SPLIT);
                 } else {
                     SKG_ROWS(10, MODE_DF64);

@@ -1,7 +1,11 @@
 // Library-wide C ABI entry points: version, per-thread last error, device
 // capabilities the host side needs.
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "skg_common.cuh"
 
@@ -106,3 +110,27 @@ extern "C" int skg_fp64_fma_rate(double *h_gfma, void *stream) {
         *h_gfma = fmas / ((double)ms * 1e-3) / 1e9;
     });
 }
+
+namespace skg {
+
+const double *device_table(const double *h, size_t n, cudaStream_t s) {
+    static std::mutex mu;
+    static std::map<std::pair<int, std::vector<double>>, double *> cache;
+    int dev = 0;
+    SKG_CUDA(cudaGetDevice(&dev));
+    std::pair<int, std::vector<double>> key(dev, std::vector<double>(h, h + n));
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SKG_CUDA(cudaStreamIsCapturing(s, &cap));
+    require(cap == cudaStreamCaptureStatusNone,
+            "assembly tables are built on the first call: run the assembly once before capturing it");
+    double *d = nullptr;
+    SKG_CUDA(cudaMalloc((void **)&d, std::max<size_t>(n, 1) * sizeof(double)));
+    if (n) SKG_CUDA(cudaMemcpy(d, h, n * sizeof(double), cudaMemcpyHostToDevice));
+    cache.emplace(std::move(key), d);
+    return d;
+}
+
+}  // namespace skg

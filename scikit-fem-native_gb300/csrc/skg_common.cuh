@@ -141,6 +141,13 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // gathering from it at random do not cross the host link per access.
 const double *device_resident(const double *p, int64_t n, DevBuf<double> &stage, cudaStream_t s);
 
+// Device copy of a small host table (quadrature / basis tables of a few KB),
+// made on first use per content and device and kept for the process, so
+// that repeated assemblies need no host-to-device copy; in particular an
+// assembly captured into a CUDA graph after one warm-up call replays without
+// reading host memory.  Fails if the first use happens while s is capturing.
+const double *device_table(const double *h, size_t n, cudaStream_t s);
+
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;

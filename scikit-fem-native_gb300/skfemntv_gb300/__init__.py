@@ -10,7 +10,7 @@ CUDA kernels for sm_103a reached through the C ABI in
 ``include/skfem_gb300.h``.
 """
 from .adjoint import P1Energy
-from .assembly import NativeBilinearForm, NativeCrossBilinearForm, NativeLinearForm
+from .assembly import AssemblyGraph, NativeBilinearForm, NativeCrossBilinearForm, NativeLinearForm
 from .basis import Basis, GeometryDiagnostics
 from .element import ElementTetP1, ElementTetP2, ElementVector
 from .errors import UnsupportedNativeForm
@@ -27,7 +27,7 @@ from .runtime import (BACKEND, CAPABILITIES, available_num_threads, get_num_thre
 __version__ = "0.1.0"
 
 __all__ = [
-    "NativeBilinearForm", "NativeCrossBilinearForm", "NativeLinearForm",
+    "AssemblyGraph", "NativeBilinearForm", "NativeCrossBilinearForm", "NativeLinearForm",
     "AffineTetN1Basis", "AssemblyMemoryBudgetError", "AssemblyMemoryEstimate", "BACKEND", "Basis",
     "BilinearForm", "CAPABILITIES", "ElementTetP1", "ElementTetP2", "ElementVector", "GeometryDiagnostics",
     "HcurlTetGeometryDiagnostics", "LinearForm", "EnergySurrogate", "MeshTet", "MeshTet2", "NeoHookean", "P1Energy", "TetN1Assembler", "TetN1LinearAssembler",

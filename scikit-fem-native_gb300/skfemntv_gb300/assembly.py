@@ -217,6 +217,41 @@ class _MatrixTarget:
                           copy=False)
 
 
+class AssemblyGraph:
+    """An assembly captured into a CUDA graph, for repeated assemblies whose
+    inputs change in place (a time loop updating a coefficient between steps):
+    ``replay()`` recomputes the matrix values from the current contents of the
+    device tensors the capture read, as one graph launch instead of the
+    per-call host work (argument checks, tables, a dozen launches).  Capture
+    covers the FP64 fused affine path; one plain call runs first (it builds the
+    device tables and sets kernel attributes, which a capture may not do)."""
+
+    def __init__(self, launch, target):
+        import torch
+
+        launch()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            launch()
+        self.target = target
+
+    def replay(self):
+        """Re-run the captured assembly on the current stream; returns the device values."""
+        self.graph.replay()
+        return self.target.d_values
+
+
+def _device_tensor(t, shape, name):
+    import torch
+
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous float64 CUDA tensor")
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} must have shape {tuple(shape)}")
+    return t
+
+
 class NativeBilinearForm:
     """value / gradient / symmetric-gradient / divergence assembly on one basis."""
 
@@ -265,6 +300,23 @@ class NativeBilinearForm:
                  dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
                  dev.hptr(b.W), 0, coef, prec, out, dev.stream_ptr())
         return keep
+
+    def capture_gradient(self, kappa):
+        """CUDA-graph capture of ``gradient=kappa`` (per-element FP64 CUDA tensor,
+        shape (E,)) on an affine scalar basis: returns an ``AssemblyGraph`` whose
+        ``replay()`` reassembles the device values for the current ``kappa``."""
+        b = self.basis
+        if b._comp != 1 or not b.is_affine:
+            raise UnsupportedNativeForm("graph capture covers the affine scalar gradient path")
+        E, Q = b._coefficient_shape
+        kappa = _device_tensor(kappa, (E,), "kappa")
+
+        def launch():
+            call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.hptr(b.W), 0, dev.ptr(kappa), SKG_FP64, dev.ptr(self.target.d_values), dev.stream_ptr())
+
+        return AssemblyGraph(launch, self.target)
 
     def assemble_device(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
                         precision="fp64"):
@@ -373,6 +425,18 @@ class NativeTensorForm:
         """Device-resident result for GPU consumers: a CUDA sparse CSR tensor."""
         self.assemble_device(raw, precision)
         return self.target.torch_csr()
+
+    def capture(self, tensor_device, tensor_kind=2):
+        """CUDA-graph capture of the FP64 assembly with a per-element tensor
+        already on the device ((3, 3, E) for tensor_kind 2, (E, 3, 3) for 1):
+        returns an ``AssemblyGraph`` whose ``replay()`` reassembles the device
+        values for the tensor's current contents."""
+        b = self.basis
+        if not b.is_affine:
+            raise UnsupportedNativeForm("graph capture covers affine bases")
+        E = b.mesh.nelements
+        _device_tensor(tensor_device, (3, 3, E) if tensor_kind == 2 else (E, 3, 3), "tensor_device")
+        return AssemblyGraph(lambda: self._run(None, "fp64", tensor_device, tensor_kind, None), self.target)
 
     def assemble(self, raw, precision="fp64", copy=True):
         """Host CSR matrix.  ``copy=True`` (the reference's behaviour,
