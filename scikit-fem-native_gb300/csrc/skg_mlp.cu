@@ -761,6 +761,9 @@ constexpr int kPart = 9;  // gx (3) + H (6)
 constexpr int SM_PART = SM_Q + QSIZE * 4;
 constexpr size_t kTcSmem = SM_PART + sizeof(float) * 2 * kTcRows * kPart;
 constexpr uint32_t kTcWaitLimit = 1u << 24;
+constexpr int kNetOut = 10;
+constexpr int kFinishBlock = 128;
+constexpr int kGeoRec = 24;  // floats per element: F (9), grad lambda (12), V, padding  // per element: d psi / dx (3), d2 psi / dx2 (6 upper entries), usable flag
 
 // tanh(a) = 1 - 2 / (exp(2a) + 1) with the fast exponential and division;
 // absolute error ~1e-7, which is what the layer sums see.
@@ -853,11 +856,11 @@ __device__ __forceinline__ bool geometry_fp32(const double *__restrict__ p, int6
     return ok;
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
-    int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
-    const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu, double lmbda, double wsum,
-    const float *__restrict__ params, const float *__restrict__ box, float tol, float *__restrict__ recf,
-    double *__restrict__ recd, unsigned char *__restrict__ flags, unsigned long long *__restrict__ counters) {
+__global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(int64_t e_begin, int64_t e_end,
+                                                                   const float *__restrict__ params,
+                                                                   const float4 *__restrict__ xin,
+                                                                   float *__restrict__ net,
+                                                                   unsigned long long *__restrict__ counters) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
@@ -893,24 +896,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
     sync_for_mma();
     const uint32_t tmem = tslot;
     const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lane quarter
-    const float *Nrm = Q + QNORM;
     uint32_t phase = 0;
     bool tc_ok = true;
     for (int64_t tile = blockIdx.x; e_begin + tile * kTcRows < e_end; tile += gridDim.x) {
         const int64_t e = e_begin + tile * kTcRows + row;
         const bool valid = e < e_end;
-        float ga[4][3], Vf = 0.f, F[9];
-        bool geo = false;
-        if (valid) geo = geometry_fp32(p, npts, t, ne, e, dofs, u, wsum, ga, Vf, F);
-        if (!geo) {
-#pragma unroll
-            for (int k = 0; k < 9; ++k) F[k] = (k % 4) == 0 ? 1.f : 0.f;
-        }
-        SurState st;
-        surrogate_state(F, st);
-        bool use = valid && geo && st.ok && in_box(st, box);
-        float x[3] = {0.f, 0.f, 0.f};
-        if (use) normalised_input(st, Nrm, x);
+        const float4 xe = valid ? xin[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+        bool use = xe.w != 0.f;
+        const float x[3] = {xe.x, xe.y, xe.z};
         float z1[kHalf];  // hidden units jb .. jb + 31
         if (tc_ok) {
             // ---- layer 1; A operands Z1 and Q0 (own half of the columns)
@@ -1030,16 +1023,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
 #pragma unroll
         for (int k = 0; k < kPart; ++k)
             tot[k] = part[(0 * kPart + k) * kTcRows + row] + part[(1 * kPart + k) * kTcRows + row];
-        const float gx[3] = {Q[QC] + tot[0], Q[QC + 1] + tot[1], Q[QC + 2] + tot[2]};
-        const float Hx[9] = {tot[3], tot[4], tot[5], tot[4], tot[6], tot[7], tot[5], tot[7], tot[8]};
-        if (use)
-            use = surrogate_finish<true>(st, Nrm, gx, Hx, mu, lmbda, tol, Vf, ga,
-                                         reinterpret_cast<float4 *>(recf + e * kNhRecF), nullptr, nullptr, 0.0,
-                                         half == 0 ? 0 : 2, half == 0 ? 2 : 3, half == 1);
-        if (valid && half == 1) {
-            if (!use) surrogate_fallback<true>(e, p, npts, t, ne, dofs, u, mu, lmbda, wsum, nullptr, nullptr, recd,
-                                               flags, counters);
-            else flags[e] = 0;
+        // network result of the element: feature gradient (3), Hessian (6), usable flag
+        if (valid && half == 0) {
+            float *o = net + e * kNetOut;
+            o[0] = Q[QC] + tot[0]; o[1] = Q[QC + 1] + tot[1]; o[2] = Q[QC + 2] + tot[2];
+#pragma unroll
+            for (int k = 3; k < 9; ++k) o[k] = tot[k];
+            o[9] = use ? 1.f : 0.f;
         }
         // tensor-memory reads, operand buffers and partial sums are free for the next tile
         tc::fence_before_sync();
@@ -1050,6 +1040,77 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(
     __syncthreads();
     tc::fence_after_sync();
     if (warp == 0) tc::tmem_dealloc(tmem, kTcCols);
+}
+
+// The surrogate element pass runs in three kernels: k_nh_surrogate_prep
+// (thread per element: FP32 geometry, deformation gradient, invariants, the
+// network input and whether the network may serve the element), the
+// tensor-core network k_nh_surrogate_tc (feature gradient and Hessian), and
+// k_nh_surrogate_finish (three threads per element, one per tangent row
+// block i: stress from the invariant derivatives, the check against the plain
+// law, tangent rows and, for the last block, the residual entries; elements
+// the network may not serve, or whose check fails, get the FP64 plain record).
+// The two CUDA-core kernels have no tensor-memory or shared-memory budget and
+// run at full occupancy, which hides the gathers' latency.
+__global__ void __launch_bounds__(kFinishBlock) k_nh_surrogate_prep(
+    int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p, int64_t npts,
+    const int32_t *__restrict__ t, const int32_t *__restrict__ dofs, const double *__restrict__ u, double wsum,
+    const float *__restrict__ params, const float *__restrict__ box, float4 *__restrict__ xin,
+    float4 *__restrict__ geo_out) {
+    const int64_t e = e_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= e_end) return;
+    float ga[4][3], Vf = 0.f, F[9];
+    const bool geo = geometry_fp32(p, npts, t, ne, e, dofs, u, wsum, ga, Vf, F);
+    if (!geo) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) F[k] = (k % 4) == 0 ? 1.f : 0.f;
+    }
+    SurState st;
+    surrogate_state(F, st);
+    const bool use = geo && st.ok && in_box(st, box);
+    float x[3] = {0.f, 0.f, 0.f};
+    if (use) normalised_input(st, params + ONORM, x);
+    xin[e] = make_float4(x[0], x[1], x[2], use ? 1.f : 0.f);
+    // geometry record: F (9), grad lambda (12), V, padding (2)
+    float4 *g = geo_out + e * (kGeoRec / 4);
+    g[0] = make_float4(F[0], F[1], F[2], F[3]);
+    g[1] = make_float4(F[4], F[5], F[6], F[7]);
+    g[2] = make_float4(F[8], ga[0][0], ga[0][1], ga[0][2]);
+    g[3] = make_float4(ga[1][0], ga[1][1], ga[1][2], ga[2][0]);
+    g[4] = make_float4(ga[2][1], ga[2][2], ga[3][0], ga[3][1]);
+    g[5] = make_float4(ga[3][2], Vf, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(kFinishBlock, 4) k_nh_surrogate_finish(
+    int64_t ne, int64_t e_begin, int64_t e_end, const double *__restrict__ p, int64_t npts,
+    const int32_t *__restrict__ t, const int32_t *__restrict__ dofs, const double *__restrict__ u, double mu,
+    double lmbda, double wsum, const float *__restrict__ params, const float *__restrict__ net,
+    const float4 *__restrict__ geo_in, float tol, float *__restrict__ recf, double *__restrict__ recd,
+    unsigned char *__restrict__ flags, unsigned long long *__restrict__ counters) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t e = e_begin + k / 3;
+    const int i = (int)(k % 3);  // tangent row block of this thread; block 2 also does the tail
+    if (e >= e_end) return;
+    const float *o = net + e * kNetOut;
+    bool use = o[9] != 0.f;
+    if (use) {
+        const float4 *g = geo_in + e * (kGeoRec / 4);
+        const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
+        const float F[9] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x};
+        const float ga[4][3] = {{g2.y, g2.z, g2.w}, {g3.x, g3.y, g3.z}, {g3.w, g4.x, g4.y}, {g4.z, g4.w, g5.x}};
+        const float Vf = g5.y;
+        SurState st;
+        surrogate_state(F, st);
+        const float gx[3] = {o[0], o[1], o[2]};
+        const float Hx[9] = {o[3], o[4], o[5], o[4], o[6], o[7], o[5], o[7], o[8]};
+        use = surrogate_finish<true>(st, params + ONORM, gx, Hx, mu, lmbda, tol, Vf, ga,
+                                     reinterpret_cast<float4 *>(recf + e * kNhRecF), nullptr, nullptr, 0.0, i, i + 1,
+                                     i == 2);
+    }
+    if (i != 2) return;
+    if (!use) surrogate_fallback<true>(e, p, npts, t, ne, dofs, u, mu, lmbda, wsum, nullptr, nullptr, recd, flags,
+                                       counters);
+    else flags[e] = 0;
 }
 
 }  // namespace
@@ -1267,19 +1328,26 @@ void nh_assemble_surrogate(const skg_pattern *pat, const double *d_p, int64_t np
     DevBuf<unsigned long long> fb(2, s);  // [0] fallback elements, [1] tensor-core waits given up
     SKG_CUDA(cudaMemsetAsync(fb.get(), 0, 16, s));
     if (d_values && pat->max_row_len > 0) {  // fused path, network on the tensor cores
-        DevBuf<float> recf((size_t)ne * kNhRecF, s);
+        DevBuf<float> recf((size_t)ne * kNhRecF, s), net((size_t)ne * kNetOut, s), geo((size_t)ne * kGeoRec, s);
+        DevBuf<float4> xin((size_t)ne, s);
         DevBuf<double> recd((size_t)ne * kNhRecD, s);
         DevBuf<unsigned char> flags((size_t)ne, s);
         SKG_CUDA(cudaFuncSetAttribute(k_nh_surrogate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
         run_passes(
             pat, ne, d_values, h_values, s,
             [&](int64_t e0, int64_t e1) {
+                k_nh_surrogate_prep<<<grid_for(e1 - e0, kFinishBlock), kFinishBlock, 0, s>>>(
+                    ne, e0, e1, d_p, npts, d_t, pat->row_dofs.get(), d_u, wsum, d_params, d_box, xin.get(),
+                    reinterpret_cast<float4 *>(geo.get()));
+                SKG_LAUNCH_CHECK("nh_surrogate_prep");
                 const int64_t tiles = (e1 - e0 + kTcRows - 1) / kTcRows;
                 const unsigned grid = (unsigned)(tiles < kSmCount ? tiles : kSmCount);
-                k_nh_surrogate_tc<<<grid, kTcThreads, kTcSmem, s>>>(ne, e0, e1, d_p, npts, d_t, pat->row_dofs.get(),
-                                                                 d_u, mu, lmbda, wsum, d_params, d_box, tol,
-                                                                 recf.get(), recd.get(), flags.get(), fb.get());
+                k_nh_surrogate_tc<<<grid, kTcThreads, kTcSmem, s>>>(e0, e1, d_params, xin.get(), net.get(), fb.get());
                 SKG_LAUNCH_CHECK("nh_surrogate_tc");
+                k_nh_surrogate_finish<<<grid_for(3 * (e1 - e0), kFinishBlock), kFinishBlock, 0, s>>>(
+                    ne, e0, e1, d_p, npts, d_t, pat->row_dofs.get(), d_u, mu, lmbda, wsum, d_params, net.get(),
+                    reinterpret_cast<const float4 *>(geo.get()), tol, recf.get(), recd.get(), flags.get(), fb.get());
+                SKG_LAUNCH_CHECK("nh_surrogate_finish");
             },
             [&](const GroupSet &gs, cudaStream_t st) {
                 nh_rows(pat, gs, recd.get(), recf.get(), flags.get(), d_residual, d_values, st);
