@@ -136,11 +136,11 @@ def test_surrogate_assembly_accuracy_and_fallback(surrogate):
     assert relerr(r4, r3) < 3e-2 and relerr(K4.data, d3) < 5e-2
 
 
-def test_surrogate_speed_against_plain_law(surrogate):
-    """On a 48^3 x 6 mesh the surrogate residual + tangent assembly
-    (tensor-core network, FP32 rows) stays within 15 % of the FP64 plain law's
-    time (both paths FP64-pipe or latency bound; measured at 64^3: 2.25 ms
-    surrogate, 2.27 ms plain), at the accuracy asserted above."""
+def test_surrogate_is_faster_than_plain_law(surrogate):
+    """What the trained network gains: on a 48^3 x 6 mesh the surrogate
+    residual + tangent assembly (tensor-core network, FP32 rows) takes less
+    time than the FP64 plain law (itself FP64-pipe bound), at the accuracy
+    asserted above."""
     m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 49),) * 3)
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
     nh = sk.NeoHookean(b, 1.0, 10.0)
@@ -164,7 +164,7 @@ def test_surrogate_speed_against_plain_law(surrogate):
     nh.assemble_device(du, surrogate=surrogate, tol=1e-2)
     print(f"48^3 plain {t_plain:.3f} ms, surrogate {t_sur:.3f} ms, fallback {nh.last_fallback}")
     assert nh.last_fallback == 0
-    assert t_sur < 1.15 * t_plain
+    assert t_sur < t_plain
 
 
 @pytest.mark.parametrize("cells", [16, 34])
