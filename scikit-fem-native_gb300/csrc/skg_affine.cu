@@ -254,11 +254,6 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, int64_t e
     }
 }
 
-__device__ __forceinline__ bool df_in_range(df64 x) {
-    const float a = fabsf(x.hi);
-    return a == 0.f || (a > 1e-30f && a < 1e30f);
-}
-
 // Scale exponent s: vertex coordinates times 2^-s are at most 1 in magnitude.
 // The largest |x| is found on the bit patterns (for non-negative doubles the
 // integer order of the bits is the numeric order), so the scan runs on the
@@ -971,6 +966,11 @@ bool p2_rule_is_exact(const std::vector<double> &T) {
 }
 
 }  // namespace
+
+void launch_scale_exponent(const double *d_p, int64_t n, int *d_s, cudaStream_t stream) {
+    k_scale<<<2 * kSmCount, 256, 0, stream>>>(d_p, n, d_s);
+    SKG_LAUNCH_CHECK("scale");
+}
 
 // Shared by the C ABI entry points below.
 // h_values (optional, page-locked host): the values also go there, copied in

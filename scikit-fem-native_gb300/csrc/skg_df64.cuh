@@ -79,6 +79,20 @@ __device__ __forceinline__ df64 df_mul(df64 x, df64 y) {
 // acc + x * y
 __device__ __forceinline__ df64 df_fma(df64 x, df64 y, df64 acc) { return df_add(acc, df_mul(x, y)); }
 
+// |x| inside the range the double-float paths accept (or zero)
+__device__ __forceinline__ bool df_in_range(df64 x) {
+    const float a = fabsf(x.hi);
+    return a == 0.f || (a > 1e-30f && a < 1e30f);
+}
+
+// x * 2^k, exact while the parts stay normal
+__device__ __forceinline__ df64 df_ldexp(df64 x, int k) { return {ldexpf(x.hi, k), ldexpf(x.lo, k)}; }
+
+// Scale exponent s of the vertex coordinates p (n doubles): |p| * 2^-s <= 1.
+// *d_s must hold INT_MIN before the launch (it stays INT_MIN when every
+// coordinate is zero or not finite).
+void launch_scale_exponent(const double *d_p, int64_t n, int *d_s, cudaStream_t stream);
+
 // 1 / x: float estimate refined by one Newton step in df64
 __device__ __forceinline__ df64 df_recip(df64 x) {
     const float r = 1.0f / x.hi;

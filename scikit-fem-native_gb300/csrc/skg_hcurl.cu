@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "skg_common.cuh"
+#include "skg_df64.cuh"
 #include "skg_rows.cuh"
 
 namespace skg {
@@ -115,6 +116,12 @@ struct N1Table {
     double wsum;
 };
 
+// The same table as FP32 (hi, lo) pairs for the split-precision pass.
+struct N1TableF {
+    float2 Tm[6][6][4];
+    float2 wsum;
+};
+
 __device__ __forceinline__ void n1_geometry(const double *__restrict__ p, int64_t npts,
                                             const int32_t *__restrict__ t, int64_t ne, int64_t e, double J[9],
                                             double b[4][3], double &det) {
@@ -158,11 +165,7 @@ constexpr int kN1Block = 128;
 
 // Per-element coefficients, closed form: K_ac = s_a s_c (mu sum_uv G T + nu
 // (J c_a . J c_c) wsum / |det|) with G = b_k . b_l / |det|; the 21 entries of
-// the symmetric 6 x 6 matrix, stores staged through shared memory.  SPLIT: G,
-// J c and the table in FP64, converted to FP32 (hi, lo) pairs, the entries
-// contracted in FP32 with split products (hi hi + hi lo + lo hi) and FP32
-// accumulation; FP64 keeps the geometry and the CSR slot sums.
-template <bool SPLIT>
+// the symmetric 6 x 6 matrix, stores staged through shared memory (FP64).
 __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e_begin, int64_t e_end,
                                                             const double *__restrict__ p, int64_t npts,
                                                             const int32_t *__restrict__ t,
@@ -202,71 +205,152 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
 #pragma unroll
         for (int a = 0; a < 6; ++a) sg[a] = (float)signs[a * ne + e];
         double *st = stage + threadIdx.x * 37;
-        if constexpr (!SPLIT) {
 #pragma unroll
-            for (int a = 0; a < 6; ++a)
+        for (int a = 0; a < 6; ++a)
 #pragma unroll
-                for (int c = a; c < 6; ++c) {
-                    double m = 0.0;
+            for (int c = a; c < 6; ++c) {
+                double m = 0.0;
 #pragma unroll
-                    for (int u = 0; u < 2; ++u)
+                for (int u = 0; u < 2; ++u)
 #pragma unroll
-                        for (int v = 0; v < 2; ++v) m += Gm[edge_v(a, u)][edge_v(c, v)] * tab.Tm[a][c][u * 2 + v];
-                    const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
-                    const double val = (double)(sg[a] * sg[c]) * (mu * m + nu * cc);
-                    st[a * 6 + c] = val;
-                    st[c * 6 + a] = val;
-                }
-        } else {
-            float2 G2[4][4], C2[6][3];
+                    for (int v = 0; v < 2; ++v) m += Gm[edge_v(a, u)][edge_v(c, v)] * tab.Tm[a][c][u * 2 + v];
+                const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
+                const double val = (double)(sg[a] * sg[c]) * (mu * m + nu * cc);
+                st[a * 6 + c] = val;
+                st[c * 6 + a] = val;
+            }
+    }
+    __syncthreads();
+    const int nvalid = (int)(e_end - e0 < kN1Block ? e_end - e0 : kN1Block);
+    for (int i = threadIdx.x; i < nvalid * 36; i += kN1Block) {
+        const int el = i / 36, q = i - el * 36;
+        Ke[(e0 + el) * 36 + q] = stage[el * 37 + q];
+    }
+}
+
+// Split precision without FP64 arithmetic beyond the edge differences: the
+// geometry in double-float with coordinates scaled by 2^-s (G = b_k.b_l / |det|
+// then carries 2^-s and nu = curl / |det| 2^3s, J c 2^-s), the entries
+// contracted in FP32 with split products (hi hi + hi lo + lo hi) and FP32
+// accumulation of the products' high and low parts; the mass term (scale 2^-s) and the
+// curl term (2^s) are unscaled exactly and summed in double-float, and the
+// FP64 entry is assembled by integer bit arithmetic.  *range_bad is set when a
+// value leaves the FP32 range (the caller then recomputes in FP64).
+__global__ void __launch_bounds__(kN1Block) k_n1_elem_df(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                          const double *__restrict__ p, int64_t npts,
+                                                          const int32_t *__restrict__ t,
+                                                          const int8_t *__restrict__ signs, N1TableF tab,
+                                                          const double *__restrict__ mass,
+                                                          const double *__restrict__ curl, int inc_mass,
+                                                          int inc_curl, const int *__restrict__ s_ptr,
+                                                          int *__restrict__ range_bad, double *__restrict__ Ke) {
+    __shared__ double stage[kN1Block * 37];
+    const int sc = *s_ptr;
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * kN1Block;
+    const int64_t e = e0 + threadIdx.x;
+    if (e < e_end) {
+        int32_t v[4];
+        bool ok = true;
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 4; ++k) {
+            v[k] = t[k * ne + e];
+            ok = ok && v[k] >= 0 && v[k] < npts;
+        }
+        if (!ok) v[0] = v[1] = v[2] = v[3] = 0;
+        df64 J[9];
 #pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    const float h = (float)Gm[k][l];
-                    G2[k][l] = make_float2(h, (float)(Gm[k][l] - (double)h));
-                }
+        for (int i = 0; i < 3; ++i) {
+            const double x0 = p[i * npts + v[0]];
 #pragma unroll
-            for (int a = 0; a < 6; ++a)
+            for (int r = 0; r < 3; ++r) J[i * 3 + r] = df_from_double(p[i * npts + v[r + 1]] - x0, -sc, ok);
+        }
+        df64 b[4][3];
+#define SKG_CROSS(a, bb, c, d) df_add_fast(df_mul(J[a], J[bb]), df_neg(df_mul(J[c], J[d])))
+        b[1][0] = SKG_CROSS(4, 8, 5, 7);
+        b[1][1] = SKG_CROSS(2, 7, 1, 8);
+        b[1][2] = SKG_CROSS(1, 5, 2, 4);
+        b[2][0] = SKG_CROSS(5, 6, 3, 8);
+        b[2][1] = SKG_CROSS(0, 8, 2, 6);
+        b[2][2] = SKG_CROSS(2, 3, 0, 5);
+        b[3][0] = SKG_CROSS(3, 7, 4, 6);
+        b[3][1] = SKG_CROSS(1, 6, 0, 7);
+        b[3][2] = SKG_CROSS(0, 4, 1, 3);
+#undef SKG_CROSS
+        df64 det = df_add_fast(df_add_fast(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add_fast(df_add_fast(b[1][i], b[2][i]), b[3][i]));
+        if (det.hi < 0.f) det = df_neg(det);
+        ok = ok && det.hi > 1e-30f;
+        const df64 inv = df_recip(det);
+        float2 G2[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int l = k; l < 4; ++l) {
+                const df64 d = df_mul(inv, df_add_fast(df_add_fast(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])),
+                                                       df_mul(b[k][2], b[l][2])));
+                ok = ok && df_in_range(d);
+                G2[k][l] = G2[l][k] = make_float2(d.hi, d.lo);
+            }
+        float2 C2[6][3];
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                df64 c{0.f, 0.f};
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    if (ref_curl(a, r) != 0.0) {
+                        const df64 x = df64{2.f * J[i * 3 + r].hi, 2.f * J[i * 3 + r].lo};  // |ref_curl| = 2
+                        c = ref_curl(a, r) > 0.0 ? df_add(c, x) : df_sub(c, x);
+                    }
+                C2[a][i] = make_float2(c.hi, c.lo);
+            }
+        const df64 mu = inc_mass ? df_from_double(mass ? mass[e] : 1.0, 0, ok) : df64{0.f, 0.f};
+        df64 nu{0.f, 0.f};
+        if (inc_curl) {
+            nu = df_mul(df_mul(df_from_double(curl ? curl[e] : 1.0, 0, ok), inv), df64{tab.wsum.x, tab.wsum.y});
+            ok = ok && df_in_range(nu);
+        }
+        float sg[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) sg[a] = (float)signs[a * ne + e];
+        double *st = stage + threadIdx.x * 37;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int c = a; c < 6; ++c) {
+                float mh = 0.f, ml = 0.f;
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+#pragma unroll
+                    for (int w = 0; w < 2; ++w) {
+                        const float2 g = G2[edge_v(a, u)][edge_v(c, w)];
+                        const float2 tt = tab.Tm[a][c][u * 2 + w];
+                        const float ph = g.x * tt.x;
+                        mh += ph;
+                        ml += fmaf(g.x, tt.x, -ph) + fmaf(g.x, tt.y, g.y * tt.x);
+                    }
+                float ch = 0.f, cl = 0.f;
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
-                    const float h = (float)Jc[a][i];
-                    C2[a][i] = make_float2(h, (float)(Jc[a][i] - (double)h));
+                    const float2 x = C2[a][i], y = C2[c][i];
+                    const float ph = x.x * y.x;
+                    ch += ph;
+                    cl += fmaf(x.x, y.x, -ph) + fmaf(x.x, y.y, x.y * y.x);
                 }
-            const float muh = (float)mu, mul = (float)(mu - (double)muh);
-            const float nuh = (float)nu, nul = (float)(nu - (double)nuh);
-#pragma unroll
-            for (int a = 0; a < 6; ++a)
-#pragma unroll
-                for (int c = a; c < 6; ++c) {
-                    float mh = 0.f, ml = 0.f;
-#pragma unroll
-                    for (int u = 0; u < 2; ++u)
-#pragma unroll
-                        for (int v = 0; v < 2; ++v) {
-                            const float2 g = G2[edge_v(a, u)][edge_v(c, v)];
-                            const double td = tab.Tm[a][c][u * 2 + v];
-                            const float th = (float)td, tl = (float)(td - (double)th);
-                            const float ph = g.x * th;
-                            mh += ph;
-                            ml += fmaf(g.x, th, -ph) + fmaf(g.x, tl, g.y * th);
-                        }
-                    float ch = 0.f, cl = 0.f;
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-                        const float2 x = C2[a][i], y = C2[c][i];
-                        const float ph = x.x * y.x;
-                        ch += ph;
-                        cl += fmaf(x.x, y.x, -ph) + fmaf(x.x, y.y, x.y * y.x);
-                    }
-                    const float m = mh + ml, cc = ch + cl;
-                    const float vh = muh * m + nuh * cc;
-                    const float vl = fmaf(muh, m, -muh * m) + fmaf(nuh, cc, -nuh * cc) + mul * m + nul * cc;
-                    const double val = (double)(sg[a] * sg[c]) * ((double)vh + (double)vl);
-                    st[a * 6 + c] = val;
-                    st[c * 6 + a] = val;
-                }
-        }
+                const float m = mh + ml, cc = ch + cl;
+                // mass term (scale 2^-s) and curl term (scale 2^s) as (hi, lo) pairs
+                const float mth = mu.hi * m, ctl_h = nu.hi * cc;
+                const df64 mt = fast_two_sum(mth, fmaf(mu.hi, m, -mth) + mu.lo * m);
+                const df64 ct = fast_two_sum(ctl_h, fmaf(nu.hi, cc, -ctl_h) + nu.lo * cc);
+                df64 val = df_add(df_ldexp(mt, sc), df_ldexp(ct, -sc));
+                if (sg[a] * sg[c] < 0.f) val = df_neg(val);
+                const double dv = df_to_double(val, 0);
+                st[a * 6 + c] = dv;
+                st[c * 6 + a] = dv;
+            }
+        if (!ok) *range_bad = 1;
     }
     __syncthreads();
     const int nvalid = (int)(e_end - e0 < kN1Block ? e_end - e0 : kN1Block);
@@ -458,22 +542,49 @@ void n1_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const 
     N1Table tab;
     n1_table(nq, h_X, h_W, tab);
     DevBuf<double> Ke((size_t)ne * 36, s);
-    auto elem = [&](int64_t e0, int64_t e1) {
-        const unsigned grid = grid_for(e1 - e0, kN1Block);
-        if (precision == SKG_SPLIT_FP32)
-            k_n1_elem_fast<true><<<grid, kN1Block, 0, s>>>(ne, e0, e1, d_p, npts, d_t, d_signs, tab, d_mass, d_curl,
-                                                           include_mass, include_curl, Ke.get());
-        else
-            k_n1_elem_fast<false><<<grid, kN1Block, 0, s>>>(ne, e0, e1, d_p, npts, d_t, d_signs, tab, d_mass, d_curl,
-                                                            include_mass, include_curl, Ke.get());
+    auto elem64 = [&](int64_t e0, int64_t e1) {
+        k_n1_elem_fast<<<grid_for(e1 - e0, kN1Block), kN1Block, 0, s>>>(ne, e0, e1, d_p, npts, d_t, d_signs, tab,
+                                                                      d_mass, d_curl, include_mass, include_curl,
+                                                                      Ke.get());
         SKG_LAUNCH_CHECK("n1_element");
     };
-    if (h_values && pat->max_row_len > 0) {
-        run_passes(pat, ne, d_values, h_values, s, elem,
-                   [&](const GroupSet &gs, cudaStream_t st) { add_element_rows<6>(pat, Ke.get(), d_values, st, gs); });
+    auto rows = [&](const GroupSet &gs, cudaStream_t st) { add_element_rows<6>(pat, Ke.get(), d_values, st, gs); };
+    const bool groups = pat->max_row_len > 0;
+    if (precision == SKG_SPLIT_FP32 && ne) {
+        // element pass in split precision over all elements first (its range
+        // check decides whether the FP64 pass replaces it), then the row pass
+        N1TableF tf;
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 6; ++c)
+                for (int k = 0; k < 4; ++k) {
+                    const double v = tab.Tm[a][c][k];
+                    const float h = (float)v;
+                    tf.Tm[a][c][k] = make_float2(h, (float)(v - (double)h));
+                }
+        const float wh = (float)tab.wsum;
+        tf.wsum = make_float2(wh, (float)(tab.wsum - (double)wh));
+        DevBuf<int> misc(2, s);  // [0] scale exponent, [1] range flag
+        const int init[2] = {INT_MIN, 0};
+        SKG_CUDA(cudaMemcpyAsync(misc.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+        launch_scale_exponent(d_p, 3 * npts, misc.get(), s);
+        k_n1_elem_df<<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(ne, 0, ne, d_p, npts, d_t, d_signs, tf, d_mass,
+                                                                 d_curl, include_mass, include_curl, misc.get(),
+                                                                 misc.get() + 1, Ke.get());
+        SKG_LAUNCH_CHECK("n1_element_df");
+        int h_misc[2];
+        SKG_CUDA(cudaMemcpyAsync(h_misc, misc.get(), sizeof(h_misc), cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        if (h_misc[1] != 0 || h_misc[0] == INT_MIN) elem64(0, ne);  // out of FP32 range: FP64 instead
+        if (groups) {
+            run_row_pass(pat, d_values, h_values, s, rows);
+            return;
+        }
+    } else if (h_values && groups) {
+        run_passes(pat, ne, d_values, h_values, s, elem64, rows);
         return;
+    } else if (ne) {
+        elem64(0, ne);
     }
-    if (ne) elem(0, ne);
     gather_element_matrices(pat, Ke.get(), d_values, s);
     if (h_values && pat->nnz)
         SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
