@@ -761,9 +761,9 @@ constexpr int kPart = 9;  // gx (3) + H (6)
 constexpr int SM_PART = SM_Q + QSIZE * 4;
 constexpr size_t kTcSmem = SM_PART + sizeof(float) * 2 * kTcRows * kPart;
 constexpr uint32_t kTcWaitLimit = 1u << 24;
-constexpr int kNetOut = 10;
+constexpr int kNetOut = 10;  // per element: d psi / dx (3), d2 psi / dx2 (6 upper entries), usable flag
 constexpr int kFinishBlock = 128;
-constexpr int kGeoRec = 24;  // floats per element: F (9), grad lambda (12), V, padding  // per element: d psi / dx (3), d2 psi / dx2 (6 upper entries), usable flag
+constexpr int kGeoRec = 24;  // floats per element: F (9), grad lambda (12), V, padding
 
 // tanh(a) = 1 - 2 / (exp(2a) + 1) with the fast exponential and division;
 // absolute error ~1e-7, which is what the layer sums see.
