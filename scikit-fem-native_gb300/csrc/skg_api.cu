@@ -59,7 +59,7 @@ const double *device_resident(const double *p, int64_t n, DevBuf<double> &stage,
 // assembly passes are reported.
 namespace skg {
 namespace {
-constexpr int kRateBlocksPerSm = 8, kRateThreads = 256, kRateIters = 4096;
+constexpr int kRateBlocksPerSm = 4, kRateThreads = 256, kRateIters = 1024;
 
 __global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double *out, int iters, double a, double b) {
     double x[8];
