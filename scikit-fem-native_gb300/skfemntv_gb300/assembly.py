@@ -82,10 +82,11 @@ class Pattern:
 
 def per_element(c, E, Q, name):
     """(E,) values when ``c`` (broadcastable to (E, Q)) is constant over the
-    points of every element, else None."""
+    points of every element, else None; a scalar stays a 0-d array (callers
+    pass no array at all for the scalar 1, the kernels' default)."""
     c = np.asarray(c, dtype=np.float64)
     if c.ndim == 0:
-        return np.full(E, float(c))
+        return c
     try:
         b = np.broadcast_to(c, (E, Q))
     except ValueError as error:
@@ -286,7 +287,9 @@ class NativeBilinearForm:
         b = self.basis
         E, Q = b._coefficient_shape
         coef = keep = None
-        if not np.all(fast == 1.0):
+        if np.ndim(fast) == 0:
+            fast = None if float(fast) == 1.0 else np.full(E, float(fast))
+        if fast is not None:
             coef = dev.host_readable(fast) if host else None
             if coef is None:
                 keep = dev.to_device(fast, np.float64)

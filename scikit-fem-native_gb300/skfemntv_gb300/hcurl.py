@@ -172,7 +172,9 @@ class TetN1Assembler:
             return None, None
         pe = per_element(value, E, Q, name)
         if pe is not None:
-            return (None if np.all(pe == 1.0) else np.ascontiguousarray(pe, dtype=np.float64)), None
+            if np.ndim(pe) == 0:  # scalar: none for 1 (the kernels' default)
+                return (None if float(pe) == 1.0 else np.full(E, float(pe))), None
+            return np.ascontiguousarray(pe, dtype=np.float64), None
         return None, dev.to_device(per_point(value, E, Q, name), np.float64)
 
     def _element_pointer(self, pe, host, keep):
