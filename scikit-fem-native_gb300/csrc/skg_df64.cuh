@@ -85,9 +85,6 @@ __device__ __forceinline__ bool df_in_range(df64 x) {
     return a == 0.f || (a > 1e-30f && a < 1e30f);
 }
 
-// x * 2^k, exact while the parts stay normal
-__device__ __forceinline__ df64 df_ldexp(df64 x, int k) { return {ldexpf(x.hi, k), ldexpf(x.lo, k)}; }
-
 // Scale exponent s of the vertex coordinates p (n doubles): |p| * 2^-s <= 1.
 // *d_s must hold INT_MIN before the launch (it stays INT_MIN when every
 // coordinate is zero or not finite).

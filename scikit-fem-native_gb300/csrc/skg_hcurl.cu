@@ -232,10 +232,10 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
 // geometry in double-float with coordinates scaled by 2^-s (G = b_k.b_l / |det|
 // then carries 2^-s and nu = curl / |det| 2^3s, J c 2^-s), the entries
 // contracted in FP32 with split products (hi hi + hi lo + lo hi) and FP32
-// accumulation of the products' high and low parts; the mass term (scale 2^-s) and the
-// curl term (2^s) are unscaled exactly and summed in double-float, and the
-// FP64 entry is assembled by integer bit arithmetic.  *range_bad is set when a
-// value leaves the FP32 range (the caller then recomputes in FP64).
+// accumulation of the products' high and low parts; the mass term (scale 2^-s)
+// and the curl term (2^s) are converted to FP64 by integer bit arithmetic with
+// the scale applied to the exponent (exact), then added.  *range_bad is set
+// when a value leaves the FP32 range (the caller then recomputes in FP64).
 __global__ void __launch_bounds__(kN1Block) k_n1_elem_df(int64_t ne, int64_t e_begin, int64_t e_end,
                                                           const double *__restrict__ p, int64_t npts,
                                                           const int32_t *__restrict__ t,
@@ -344,9 +344,9 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_df(int64_t ne, int64_t e_b
                 const float mth = mu.hi * m, ctl_h = nu.hi * cc;
                 const df64 mt = fast_two_sum(mth, fmaf(mu.hi, m, -mth) + mu.lo * m);
                 const df64 ct = fast_two_sum(ctl_h, fmaf(nu.hi, cc, -ctl_h) + nu.lo * cc);
-                df64 val = df_add(df_ldexp(mt, sc), df_ldexp(ct, -sc));
-                if (sg[a] * sg[c] < 0.f) val = df_neg(val);
-                const double dv = df_to_double(val, 0);
+                // unscaled in the FP64 exponent (exact), then one FP64 add
+                double dv = df_to_double(mt, sc) + df_to_double(ct, -sc);
+                if (sg[a] * sg[c] < 0.f) dv = -dv;
                 st[a * 6 + c] = dv;
                 st[c * 6 + a] = dv;
             }

@@ -476,3 +476,21 @@ def test_fp64_rate_probe():
     rate = ctypes.c_double()
     call("skg_fp64_fma_rate", ctypes.byref(rate), None)
     assert 50.0 < rate.value < 50000.0
+
+
+@pytest.mark.parametrize("scale", [1e40, 1e12, 1.0])
+def test_n1_split_precision_extreme_scales(scale):
+    """N1 split precision works in coordinates scaled by 2^-s and unscales in
+    the FP64 exponent, so meshes far outside the FP32 range (coordinates up to
+    1e40) stay within 1e-7 of the FP64 pass like a unit mesh.  (Tiny meshes are
+    rejected as singular by the basis, as the reference's isclose(detJ, 0)
+    check does, hcurl_basis.py:321-322.)"""
+    axis = np.linspace(0.0, 1.0, 5)
+    m = sk.MeshTet.init_tensor(axis, axis, axis)
+    mesh = sk.MeshTet(m.p * scale, m.t)
+    asmb = sk.TetN1Assembler(sk.AffineTetN1Basis(mesh))
+    nu = np.exp(np.random.default_rng(4).normal(0.0, 0.3, mesh.nelements))[:, None]
+    K64 = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=nu).copy()
+    Ks = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=nu, precision="split_fp32")
+    assert np.all(np.isfinite(Ks.data))
+    assert relerr(Ks.data, K64.data) < 1e-7
