@@ -428,6 +428,7 @@ AUX_METRIC = {
     "n1_maxwell": "assembled CSR nnz/s (FP64 Nedelec N1 Maxwell)",
     "p1_adjoint": "adjoint elements/s (J = u^T K(kappa) v with dJ/dkappa, dJ/dx, dJ/du, dJ/dv, P1)",
     "nh": "neo-Hookean residual+tangent elements/s (FP64 plain law)",
+    "vp1_elasticity": "assembled CSR nnz/s (FP64 vector P1 elasticity, tabulated path)",
 }
 
 
@@ -739,8 +740,40 @@ def wl_nh(args, world, timed, wall):
         gpu_launches=3 * args.steps)
 
 
+def wl_vp1_elasticity(args, world, timed, wall):
+    """Vector P1 linear elasticity 2 mu eps(u):eps(v) + lambda div u div v + rho u.v (mu = 1, lambda = 10,
+    rho = 0.5) on a 48^3 x 6 cube with the reference's default 4-point rule: the general tabulated path
+    (value, symmetric-gradient and divergence kinds, bilinear_form_assembler.cpp:79-105)."""
+    import skfemntv_gb300 as sk
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    n = args.cells or 48
+    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3))
+    form = NativeBilinearForm(b)
+    nnz, E = form.pattern.nnz, m.nelements
+    ms, clk = timed(lambda: form.assemble_device(value=0.5, symmetric_gradient=2.0, divergence=10.0))
+
+    @sk.BilinearForm
+    def elast(u, v, w):
+        return 2.0 * sk.ddot(sk.sym_grad(u), sk.sym_grad(v)) + 10.0 * sk.div(u) * sk.div(v) + 0.5 * sk.dot(u, v)
+
+    e2e_s = wall(lambda: sk.asm(elast, b))
+    Q = len(b.W)
+    alg = 24 * m.p.shape[1] + 48 * E + 8 * nnz
+    return dict(
+        metric=AUX_METRIC["vp1_elasticity"], unit="nnz/s", value=world * nnz / (ms * 1e-3), ms_per_step=ms,
+        dtype="f64", clocks=clk,
+        config={"workload": f"vector P1 elasticity, {n}^3x6 cube ({E} tets), {Q}-point rule, "
+                            "mu=1, lambda=10, rho=0.5",
+                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
+        e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 0,
+             "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
+        roofline=_roofline(alg, ms), gpu_launches=2 * args.steps)
+
+
 AUX_WORKLOADS = {"p1_laplace": wl_p1_laplace, "n1_maxwell": wl_n1_maxwell, "p1_adjoint": wl_p1_adjoint,
-                 "nh": wl_nh}
+                 "nh": wl_nh, "vp1_elasticity": wl_vp1_elasticity}
 
 
 def run_aux(args, rank, world):
@@ -808,6 +841,16 @@ def aux_cpu_baseline(workload, threads, reps=3):
 
         units, unit, desc = E, "elements/s", (f"P1 {n}^3x6 sample: J via assembled K and dJ/dkappa "
                                               "(no coordinate gradient)")
+    elif workload == "vp1_elasticity":
+        n = 24
+        p, t = mesh(n)
+        X, W = O.tet_quadrature_p1()
+        b = O.make_basis(p, t, False, comp=3, quadrature=(X, W), threads=threads)
+        dofs = b.dofs3.reshape(b.dofs3.shape[0], -1)
+        pat = O.Pattern(dofs, dofs)
+        run = lambda: O.bilinear_assemble(b, value=0.5, symmetric_gradient=2.0, divergence=10.0,  # noqa: E731
+                                          threads=threads, pattern=pat)
+        units, unit, desc = pat.nnz, "nnz/s", f"vector P1 elasticity {n}^3x6 sample, threaded colored assembly"
     else:
         n = 24
         p, t = mesh(n)

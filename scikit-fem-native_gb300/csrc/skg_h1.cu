@@ -61,6 +61,114 @@ __global__ void k_h1_local_tabulated(int64_t ne, int n, int C, int nq, const dou
     }
 }
 
+// Thread per element for the common element shapes (NN nodes, CC components):
+// the element's rows are produced node by node (the CC rows of node a, L
+// entries each), block (a, b) accumulated over the points in registers, and
+// staged through shared memory so that the block writes whole row bands with
+// coalesced stores.  Same entries as k_h1_local_tabulated (the point weight is
+// folded into each term).
+template <int NN, int CC, int BLK>
+__global__ void __launch_bounds__(BLK) k_h1_local_tab(int64_t ne, int nq, const double *__restrict__ shape,
+                                                      const double *__restrict__ grad, const double *__restrict__ w,
+                                                      const double *__restrict__ value,
+                                                      const double *__restrict__ gradient,
+                                                      const double *__restrict__ symgrad,
+                                                      const double *__restrict__ divc, double *__restrict__ Ke) {
+    constexpr int L = NN * CC, R = CC * L;  // entries of node a's row band
+    __shared__ double stage[BLK * (R + 1)];
+    const int64_t e0 = (int64_t)blockIdx.x * BLK;
+    const int64_t e = e0 + threadIdx.x;
+    const bool valid = e < ne;
+    const int nvalid = (int)(ne - e0 < BLK ? ne - e0 : BLK);
+    double *st = stage + threadIdx.x * (R + 1);
+#pragma unroll 1
+    for (int a = 0; a < NN; ++a) {
+        if (valid && NN * CC * CC <= 40) {
+            // whole band in registers: node a's point data loaded once per point
+            double acc[NN][CC][CC];
+#pragma unroll
+            for (int b = 0; b < NN; ++b)
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) acc[b][c][d] = 0.0;
+            for (int q = 0; q < nq; ++q) {
+                const int64_t eq = e * nq + q;
+                const double *ga = grad + (eq * NN + a) * 3;
+                const double ag[3] = {ga[0], ga[1], ga[2]};
+                const double wq = w[eq];
+                const double va = value ? value[eq] * shape[eq * NN + a] * wq : 0.0;
+                const double gw = gradient ? gradient[eq] * wq : 0.0;
+                const double sg = symgrad ? 0.5 * symgrad[eq] * wq : 0.0;
+                const double dv = divc ? divc[eq] * wq : 0.0;
+#pragma unroll
+                for (int b = 0; b < NN; ++b) {
+                    const double *gb = grad + (eq * NN + b) * 3;
+                    const double bg[3] = {gb[0], gb[1], gb[2]};
+                    const double gg = ag[0] * bg[0] + ag[1] * bg[1] + ag[2] * bg[2];
+                    double diag = (gw + sg) * gg;
+                    if (value) diag += va * shape[eq * NN + b];
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+#pragma unroll
+                        for (int d = 0; d < CC; ++d) {
+                            double v = sg * ag[d] * bg[c] + dv * ag[c] * bg[d];
+                            if (c == d) v += diag;
+                            acc[b][c][d] += v;
+                        }
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < NN; ++b)
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) st[c * L + b * CC + d] = acc[b][c][d];
+        } else if (valid) {
+#pragma unroll 1
+            for (int b = 0; b < NN; ++b) {
+                double blk[CC][CC];
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) blk[c][d] = 0.0;
+                for (int q = 0; q < nq; ++q) {
+                    const int64_t eq = e * nq + q;
+                    const double *ga = grad + (eq * NN + a) * 3, *gb = grad + (eq * NN + b) * 3;
+                    const double a0 = ga[0], a1 = ga[1], a2 = ga[2], b0 = gb[0], b1 = gb[1], b2 = gb[2];
+                    const double ag[3] = {a0, a1, a2}, bg[3] = {b0, b1, b2};
+                    const double gg = a0 * b0 + a1 * b1 + a2 * b2;
+                    const double wq = w[eq];
+                    double diag = 0.0;  // terms on c == d
+                    if (value) diag += value[eq] * shape[eq * NN + a] * shape[eq * NN + b] * wq;
+                    if (gradient) diag += gradient[eq] * gg * wq;
+                    const double sg = symgrad ? 0.5 * symgrad[eq] * wq : 0.0;
+                    const double dv = divc ? divc[eq] * wq : 0.0;
+                    diag += sg * gg;
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+#pragma unroll
+                        for (int d = 0; d < CC; ++d) {
+                            double v = sg * ag[d] * bg[c] + dv * ag[c] * bg[d];
+                            if (c == d) v += diag;
+                            blk[c][d] += v;
+                        }
+                }
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) st[c * L + b * CC + d] = blk[c][d];
+            }
+        }
+        __syncthreads();
+        for (int x = threadIdx.x; x < nvalid * R; x += BLK) {
+            const int el = x / R, k = x - el * R;
+            Ke[(e0 + el) * (int64_t)(L * L) + (int64_t)a * R + k] = stage[el * (R + 1) + k];
+        }
+        __syncthreads();
+    }
+}
+
 // Thread per (element, local row i = a*C + r): tensor coefficient on gradients.
 __global__ void k_h1_local_tensor(int64_t ne, int n, int C, int nq, const double *__restrict__ grad,
                                   const double *__restrict__ w, const double *__restrict__ coef,
@@ -216,8 +324,17 @@ extern "C" int skg_h1_assemble_tabulated(const skg_pattern *pat, const int32_t *
             Ke = tmp.get();
         }
         if (ne) {
-            k_h1_local_tabulated<<<grid_for(ne * L, 128), 128, 0, s>>>(ne, nodes, comp, nq, d_shape, d_grad, d_w,
-                                                                       d_value, d_gradient, d_symgrad, d_div, Ke);
+#define SKG_TAB(NN_, CC_, BLK_)                                                                                  \
+    k_h1_local_tab<NN_, CC_, BLK_><<<grid_for(ne, BLK_), BLK_, 0, s>>>(ne, nq, d_shape, d_grad, d_w, d_value,      \
+                                                                      d_gradient, d_symgrad, d_div, Ke)
+            if (nodes == 4 && comp == 1) SKG_TAB(4, 1, 128);
+            else if (nodes == 4 && comp == 3) SKG_TAB(4, 3, 128);
+            else if (nodes == 10 && comp == 1) SKG_TAB(10, 1, 128);
+            else if (nodes == 10 && comp == 3) SKG_TAB(10, 3, 64);
+            else
+                k_h1_local_tabulated<<<grid_for(ne * L, 128), 128, 0, s>>>(ne, nodes, comp, nq, d_shape, d_grad, d_w,
+                                                                           d_value, d_gradient, d_symgrad, d_div, Ke);
+#undef SKG_TAB
             SKG_LAUNCH_CHECK("h1_local_tabulated");
         }
         gather_element_matrices(pat, Ke, d_values, s);

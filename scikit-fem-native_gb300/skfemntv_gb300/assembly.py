@@ -334,13 +334,34 @@ class NativeBilinearForm:
         if prec != SKG_FP64:
             raise UnsupportedNativeForm("split precision is available on the affine scalar gradient path")
         tab = b._device_tabulation()
-        coefs = [None if c is None else dev.to_device(per_point(c, E, Q, n), np.float64)
+        coefs = [self._point_coefficient(c, E, Q, n)
                  for c, n in ((value, "value"), (gradient, "gradient"),
                               (symmetric_gradient, "symmetric_gradient"), (divergence, "divergence"))]
         call("skg_h1_assemble_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, b._comp, Q,
              dev.ptr(tab["shape"]), dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), *(dev.ptr(c) for c in coefs),
              dev.ptr(self.target.d_values), None, dev.stream_ptr())
         return self.target.d_values
+
+    def _point_coefficient(self, c, E, Q, name):
+        """(E, Q) float64 device array for a coefficient: a CUDA tensor of that
+        shape is used as is, a scalar becomes a cached device constant (no
+        host-to-device copy per call), anything else is broadcast and uploaded."""
+        if c is None:
+            return None
+        if hasattr(c, "is_cuda") and c.is_cuda:
+            return _device_tensor(c, (E, Q), name)
+        a = np.asarray(c, dtype=np.float64)
+        if a.ndim == 0:
+            import torch
+
+            cache = self.__dict__.setdefault("_constants", {})
+            t = cache.get(float(a))
+            if t is None:
+                if len(cache) >= 8:
+                    cache.clear()
+                t = cache[float(a)] = torch.full((E, Q), float(a), dtype=torch.float64, device="cuda")
+            return t
+        return dev.to_device(per_point(a, E, Q, name), np.float64)
 
     def assemble_torch(self, *, value=None, gradient=None, symmetric_gradient=None, divergence=None,
                        precision="fp64"):
