@@ -769,7 +769,7 @@ def wl_vp1_elasticity(args, world, timed, wall):
                 "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
         e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 0,
              "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
-        roofline=_roofline(alg, ms), gpu_launches=2 * args.steps)
+        roofline=_roofline(alg, ms), gpu_launches=3 * args.steps)  # element pass + one row pass per group class
 
 
 AUX_WORKLOADS = {"p1_laplace": wl_p1_laplace, "n1_maxwell": wl_n1_maxwell, "p1_adjoint": wl_p1_adjoint,
