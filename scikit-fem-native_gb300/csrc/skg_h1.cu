@@ -61,6 +61,87 @@ __global__ void k_h1_local_tabulated(int64_t ne, int n, int C, int nq, const dou
     }
 }
 
+// Thread per element for small element matrices (P1 scalar / vector, P2
+// scalar).  Every kind of the tabulated form gives a symmetric matrix when
+// test and trial basis coincide: K_(a,c),(b,d) = K_(b,d),(a,c) for the value,
+// gradient, symmetric-gradient and divergence terms alike.  So only the blocks
+// b >= a are summed over the points (in registers, two FMAs per entry and
+// point: sg a_d b_c + dv a_c b_d), each written with its transpose into the
+// thread's element matrix in shared memory, and the block stores all matrices
+// coalesced.  The kernel is FP64-pipe bound; this halves its FP64
+// instructions against the full block loop.
+template <int NN, int CC, int BLK>
+__global__ void __launch_bounds__(BLK) k_h1_local_sym(int64_t ne, int nq, const double *__restrict__ shape,
+                                                      const double *__restrict__ grad, const double *__restrict__ w,
+                                                      const double *__restrict__ value,
+                                                      const double *__restrict__ gradient,
+                                                      const double *__restrict__ symgrad,
+                                                      const double *__restrict__ divc, double *__restrict__ Ke) {
+    constexpr int L = NN * CC, LL = L * L, LP = LL + 1;
+    extern __shared__ double stage[];  // BLK x LP
+    const int64_t e0 = (int64_t)blockIdx.x * BLK;
+    const int64_t e = e0 + threadIdx.x;
+    const int nvalid = (int)(ne - e0 < BLK ? ne - e0 : BLK);
+    double *st = stage + threadIdx.x * LP;
+    if (e < ne) {
+#pragma unroll
+        for (int a = 0; a < NN; ++a) {
+            double acc[NN][CC][CC];
+#pragma unroll
+            for (int b = a; b < NN; ++b)
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) acc[b][c][d] = 0.0;
+            for (int q = 0; q < nq; ++q) {
+                const int64_t eq = e * nq + q;
+                const double wq = w[eq];
+                const double sg = symgrad ? 0.5 * symgrad[eq] * wq : 0.0;
+                const double dv = divc ? divc[eq] * wq : 0.0;
+                const double dg = (gradient ? gradient[eq] * wq : 0.0) + sg;
+                const double va = value ? value[eq] * wq * shape[eq * NN + a] : 0.0;
+                const double *gq = grad + eq * (NN * 3);
+                const double ag[3] = {gq[a * 3], gq[a * 3 + 1], gq[a * 3 + 2]};
+                double sa[CC], da[CC];
+#pragma unroll
+                for (int c = 0; c < CC; ++c) {
+                    sa[c] = sg * ag[c];
+                    da[c] = dv * ag[c];
+                }
+#pragma unroll
+                for (int b = a; b < NN; ++b) {
+                    const double bg[3] = {gq[b * 3], gq[b * 3 + 1], gq[b * 3 + 2]};
+                    double diag = dg * (ag[0] * bg[0] + ag[1] * bg[1] + ag[2] * bg[2]);
+                    if (value) diag += va * shape[eq * NN + b];
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+#pragma unroll
+                        for (int d = 0; d < CC; ++d) {
+                            double v = acc[b][c][d] + sa[d] * bg[c];
+                            v += da[c] * bg[d];
+                            if (c == d) v += diag;
+                            acc[b][c][d] = v;
+                        }
+                }
+            }
+#pragma unroll
+            for (int b = a; b < NN; ++b)
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) {
+                        st[(a * CC + c) * L + b * CC + d] = acc[b][c][d];
+                        if (b != a) st[(b * CC + d) * L + a * CC + c] = acc[b][c][d];
+                    }
+        }
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < nvalid * LL; x += BLK) {
+        const int el = x / LL, k = x - el * LL;
+        Ke[(e0 + el) * (int64_t)LL + k] = stage[el * LP + k];
+    }
+}
+
 // Thread per element for the common element shapes (NN nodes, CC components):
 // the element's rows are produced node by node (the CC rows of node a, L
 // entries each), block (a, b) accumulated over the points in registers, and
@@ -83,48 +164,7 @@ __global__ void __launch_bounds__(BLK) k_h1_local_tab(int64_t ne, int nq, const 
     double *st = stage + threadIdx.x * (R + 1);
 #pragma unroll 1
     for (int a = 0; a < NN; ++a) {
-        if (valid && NN * CC * CC <= 40) {
-            // whole band in registers: node a's point data loaded once per point
-            double acc[NN][CC][CC];
-#pragma unroll
-            for (int b = 0; b < NN; ++b)
-#pragma unroll
-                for (int c = 0; c < CC; ++c)
-#pragma unroll
-                    for (int d = 0; d < CC; ++d) acc[b][c][d] = 0.0;
-            for (int q = 0; q < nq; ++q) {
-                const int64_t eq = e * nq + q;
-                const double *ga = grad + (eq * NN + a) * 3;
-                const double ag[3] = {ga[0], ga[1], ga[2]};
-                const double wq = w[eq];
-                const double va = value ? value[eq] * shape[eq * NN + a] * wq : 0.0;
-                const double gw = gradient ? gradient[eq] * wq : 0.0;
-                const double sg = symgrad ? 0.5 * symgrad[eq] * wq : 0.0;
-                const double dv = divc ? divc[eq] * wq : 0.0;
-#pragma unroll
-                for (int b = 0; b < NN; ++b) {
-                    const double *gb = grad + (eq * NN + b) * 3;
-                    const double bg[3] = {gb[0], gb[1], gb[2]};
-                    const double gg = ag[0] * bg[0] + ag[1] * bg[1] + ag[2] * bg[2];
-                    double diag = (gw + sg) * gg;
-                    if (value) diag += va * shape[eq * NN + b];
-#pragma unroll
-                    for (int c = 0; c < CC; ++c)
-#pragma unroll
-                        for (int d = 0; d < CC; ++d) {
-                            double v = sg * ag[d] * bg[c] + dv * ag[c] * bg[d];
-                            if (c == d) v += diag;
-                            acc[b][c][d] += v;
-                        }
-                }
-            }
-#pragma unroll
-            for (int b = 0; b < NN; ++b)
-#pragma unroll
-                for (int c = 0; c < CC; ++c)
-#pragma unroll
-                    for (int d = 0; d < CC; ++d) st[c * L + b * CC + d] = acc[b][c][d];
-        } else if (valid) {
+        if (valid) {
 #pragma unroll 1
             for (int b = 0; b < NN; ++b) {
                 double blk[CC][CC];
@@ -327,14 +367,25 @@ extern "C" int skg_h1_assemble_tabulated(const skg_pattern *pat, const int32_t *
 #define SKG_TAB(NN_, CC_, BLK_)                                                                                  \
     k_h1_local_tab<NN_, CC_, BLK_><<<grid_for(ne, BLK_), BLK_, 0, s>>>(ne, nq, d_shape, d_grad, d_w, d_value,      \
                                                                       d_gradient, d_symgrad, d_div, Ke)
-            if (nodes == 4 && comp == 1) SKG_TAB(4, 1, 128);
-            else if (nodes == 4 && comp == 3) SKG_TAB(4, 3, 128);
-            else if (nodes == 10 && comp == 1) SKG_TAB(10, 1, 128);
+#define SKG_SYM(NN_, CC_, BLK_)                                                                                  \
+    do {                                                                                                         \
+        const int smem = BLK_ * (NN_ * CC_ * NN_ * CC_ + 1) * 8;                                                 \
+        if (smem > 48 * 1024)                                                                                    \
+            SKG_CUDA(cudaFuncSetAttribute(k_h1_local_sym<NN_, CC_, BLK_>,                                        \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem));                   \
+        k_h1_local_sym<NN_, CC_, BLK_><<<grid_for(ne, BLK_), BLK_, smem, s>>>(ne, nq, d_shape, d_grad, d_w,      \
+                                                                              d_value, d_gradient, d_symgrad,   \
+                                                                              d_div, Ke);                       \
+    } while (0)
+            if (nodes == 4 && comp == 1) SKG_SYM(4, 1, 128);
+            else if (nodes == 4 && comp == 3) SKG_SYM(4, 3, 64);
+            else if (nodes == 10 && comp == 1) SKG_SYM(10, 1, 64);
             else if (nodes == 10 && comp == 3) SKG_TAB(10, 3, 64);
             else
                 k_h1_local_tabulated<<<grid_for(ne * L, 128), 128, 0, s>>>(ne, nodes, comp, nq, d_shape, d_grad, d_w,
                                                                            d_value, d_gradient, d_symgrad, d_div, Ke);
 #undef SKG_TAB
+#undef SKG_SYM
             SKG_LAUNCH_CHECK("h1_local_tabulated");
         }
         gather_element_matrices(pat, Ke, d_values, s);

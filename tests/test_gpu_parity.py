@@ -494,3 +494,32 @@ def test_n1_split_precision_extreme_scales(scale):
     Ks = asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=nu, precision="split_fp32")
     assert np.all(np.isfinite(Ks.data))
     assert relerr(Ks.data, K64.data) < 1e-7
+
+
+KINDS = ("value", "gradient", "symmetric_gradient", "divergence")
+
+
+@pytest.mark.parametrize("quadratic,comp", [(False, 1), (False, 3), (True, 1), (True, 3)])
+@pytest.mark.parametrize("kinds", [KINDS, ("value",), ("symmetric_gradient", "divergence"), ("gradient",)])
+def test_tabulated_kinds_per_point_coefficients(quadratic, comp, kinds):
+    """Per-point coefficients of every kind on the default rules (4-point P1, 11-point Keast P2) through the
+    tabulated kernels (symmetric element-per-thread kernel for P1 and scalar P2, row-band kernel for vector
+    P2), against the oracle's BilinearFormAssembler restatement on a jittered mesh."""
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    rng = np.random.default_rng(101 + 10 * quadratic + comp)
+    n = 4
+    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+    inner = np.all((m.p > 1e-9) & (m.p < 1 - 1e-9), axis=0)
+    m.p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, (3, int(inner.sum())))
+    if quadratic:
+        m = sk.MeshTet2.from_mesh(m)
+    elem = sk.ElementTetP2() if quadratic else sk.ElementTetP1()
+    b = sk.Basis(m, sk.ElementVector(elem, dim=comp))
+    E, Q = b._coefficient_shape
+    co = {k: rng.uniform(0.5, 2.0, (E, Q)) for k in kinds}
+    K = NativeBilinearForm(b).assemble(**co)
+    ob = O.make_basis(m.p, m.t, quadratic, comp=comp)
+    d, indptr, indices = O.bilinear_assemble(ob, **co)
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, d) < RTOL
