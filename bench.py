@@ -428,7 +428,7 @@ AUX_METRIC = {
     "n1_maxwell": "assembled CSR nnz/s (FP64 Nedelec N1 Maxwell)",
     "p1_adjoint": "adjoint elements/s (J = u^T K(kappa) v with dJ/dkappa, dJ/dx, dJ/du, dJ/dv, P1)",
     "nh": "neo-Hookean residual+tangent elements/s (FP64 plain law)",
-    "vp1_elasticity": "assembled CSR nnz/s (FP64 vector P1 elasticity, tabulated path)",
+    "vp1_elasticity": "assembled CSR nnz/s (FP64 vector P1 elasticity)",
 }
 
 
@@ -594,7 +594,7 @@ def wl_n1_maxwell(args, world, timed, wall):
              dev.ptr(nb._ee_dev), dev.ptr(nb._signs_dev), E, Q, dev.hptr(nb.X), dev.hptr(nb.W), None, dev.ptr(dnu),
              1, 1, 0, dev.ptr(asmb.target.d_values), dev.stream_ptr())
 
-    ms, clk = timed(step)
+    ms, clk = timed(step, flush_l2=True)
     ref = asmb.target.d_values[:nnz].clone()
 
     def step_split():
@@ -602,7 +602,7 @@ def wl_n1_maxwell(args, world, timed, wall):
              dev.ptr(nb._ee_dev), dev.ptr(nb._signs_dev), E, Q, dev.hptr(nb.X), dev.hptr(nb.W), None, dev.ptr(dnu),
              1, 1, 1, dev.ptr(asmb.target.d_values), dev.stream_ptr())
 
-    ms_s, clk_s = timed(step_split)
+    ms_s, clk_s = timed(step_split, flush_l2=True)
     err_s = _relerr(asmb.target.d_values[:nnz], ref)
     curl = (1.0 / mu)[:, None]
     e2e_s = wall(lambda: asmb.assemble_maxwell(mass_coefficient=1.0, curl_coefficient=curl))
@@ -612,7 +612,7 @@ def wl_n1_maxwell(args, world, timed, wall):
         ms_per_step=ms, dtype="f64", clocks=clk,
         config={"workload": f"N1 curl-curl + mass, {n}^3x6 cube ({E} tets), relabelled vertices, "
                             f"{Q}-point Duffy rule, curl coefficient 1/mu_e, mass 1",
-                "elements": E, "dofs": nb.N, "nnz": nnz, "l2": "inputs larger than L2"},
+                "elements": E, "dofs": nb.N, "nnz": nnz, "l2": "inputs fit in L2: a 256 MiB buffer is written before every timed call"},
         e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 8 * E,
              "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
         roofline=_roofline(alg, ms),
@@ -709,10 +709,11 @@ def wl_nh(args, world, timed, wall):
         sur = sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    ms_plain, clk = timed(lambda: nh.assemble_device(du))
+    ms_plain, clk = timed(lambda: nh.assemble_device(du), flush_l2=True)
     r0 = nh.d_res[: b.N].clone()
     k0 = nh.target.d_values[:nnz].clone()
-    ms_sur, clk_s = timed(lambda: nh.assemble_device(du, surrogate=sur, tol=1e-2, count_fallback=False))
+    ms_sur, clk_s = timed(lambda: nh.assemble_device(du, surrogate=sur, tol=1e-2, count_fallback=False),
+                          flush_l2=True)
     nh.assemble_device(du, surrogate=sur, tol=1e-2)
     fallback = nh.last_fallback
     err_r = _relerr(nh.d_res[: b.N], r0)
@@ -728,7 +729,7 @@ def wl_nh(args, world, timed, wall):
                             "unit wavevectors, mu=1, lambda=10, 1-point rule",
                 "training": "short profiling schedule" if args.quick_train else
                             "2M samples, 3000 Adam steps, L-BFGS on 524,288 samples",
-                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
+                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs fit in L2: a 256 MiB buffer is written before every timed call"},
         e2e={"value": world * E / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": 8 * b.N,
              "d2h_bytes_per_step": 8 * (b.N + nnz), "ms_per_step": 1e3 * e2e_s},
         roofline=dict(_roofline(alg, ms_plain), fp64_pipe=_nh_fp64(E, ms_plain)),
@@ -742,8 +743,9 @@ def wl_nh(args, world, timed, wall):
 
 def wl_vp1_elasticity(args, world, timed, wall):
     """Vector P1 linear elasticity 2 mu eps(u):eps(v) + lambda div u div v + rho u.v (mu = 1, lambda = 10,
-    rho = 0.5) on a 48^3 x 6 cube with the reference's default 4-point rule: the general tabulated path
-    (value, symmetric-gradient and divergence kinds, bilinear_form_assembler.cpp:79-105)."""
+    rho = 0.5) on a 48^3 x 6 cube with the reference's default 4-point rule (value, symmetric-gradient and
+    divergence kinds, bilinear_form_assembler.cpp:79-105): constant coefficients through the fused affine P1
+    kernel, and the same form with per-point coefficients through the tabulated kernels."""
     import skfemntv_gb300 as sk
     from skfemntv_gb300.assembly import NativeBilinearForm
 
@@ -752,7 +754,17 @@ def wl_vp1_elasticity(args, world, timed, wall):
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3))
     form = NativeBilinearForm(b)
     nnz, E = form.pattern.nnz, m.nelements
-    ms, clk = timed(lambda: form.assemble_device(value=0.5, symmetric_gradient=2.0, divergence=10.0))
+    ms, clk = timed(lambda: form.assemble_device(value=0.5, symmetric_gradient=2.0, divergence=10.0), flush_l2=True)
+    # the same form with the coefficients given per point (device (E, Q) arrays): the tabulated kernels
+    import torch
+
+    Qn = len(b.W)
+    pts = {k: torch.full((E, Qn), v, dtype=torch.float64, device="cuda")
+           for k, v in (("value", 0.5), ("symmetric_gradient", 2.0), ("divergence", 10.0))}
+    ms_tab, _ = timed(lambda: form.assemble_device(**pts), flush_l2=True)
+    fused = form.assemble_device(value=0.5, symmetric_gradient=2.0, divergence=10.0)[:nnz].clone()
+    tab_err = _relerr(form.assemble_device(**pts)[:nnz], fused)
+    del pts
 
     @sk.BilinearForm
     def elast(u, v, w):
@@ -765,8 +777,11 @@ def wl_vp1_elasticity(args, world, timed, wall):
         metric=AUX_METRIC["vp1_elasticity"], unit="nnz/s", value=world * nnz / (ms * 1e-3), ms_per_step=ms,
         dtype="f64", clocks=clk,
         config={"workload": f"vector P1 elasticity, {n}^3x6 cube ({E} tets), {Q}-point rule, "
-                            "mu=1, lambda=10, rho=0.5",
-                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs larger than L2"},
+                            "mu=1, lambda=10, rho=0.5, constant coefficients (fused affine P1 path)",
+                "elements": E, "dofs": b.N, "nnz": nnz, "l2": "inputs fit in L2: a 256 MiB buffer is written before every timed call"},
+        per_point_tabulated={"ms_per_step": ms_tab, "value": world * nnz / (ms_tab * 1e-3),
+                             "max_rel_err_vs_fused": tab_err,
+                             "note": "same form, coefficients as device (E, Q) arrays: tabulated kernels"},
         e2e={"value": world * nnz / e2e_s, "unit": "nnz/s", "h2d_bytes_per_step": 0,
              "d2h_bytes_per_step": 8 * nnz, "ms_per_step": 1e3 * e2e_s},
         roofline=_roofline(alg, ms), gpu_launches=3 * args.steps)  # element pass + one row pass per group class

@@ -244,6 +244,29 @@ int skg_h1_assemble_affine_noalloc(const skg_pattern *pattern, const double *d_p
                                    const double *d_coef, int32_t precision,
                                    double *d_values, void *stream);
 
+/* P1 forms with per-element coefficients on affine tets: the value,
+ * gradient, symmetric-gradient and divergence kinds of
+ * BilinearFormAssembler.assemble (cpp/src/assembly/bilinear_form_assembler.cpp:79-105,
+ * reached from NativeBilinearForm.assemble, python/skfemntv/bilinear_form.py:13-99)
+ * for a scalar (comp 1) or vector (comp 3) P1 basis whose coefficients are
+ * constant on every element, straight from coordinates: no tabulated
+ * basis data is read.  Each kind takes a per-element array d_k (E) or, when
+ * that is NULL, the constant c_k (0 leaves the term out).  The point sums use
+ * the caller's rule h_X (3,Q), h_W (Q) (weight sum and P1 mass table), so
+ * results match the tabulated path to rounding.  d_t (G, E) with G >= 4
+ * vertex rows (a P1 field on a P2 geometry mesh uses its vertices; the map
+ * must be affine).  d_values (nnz) is overwritten; with h_values non-NULL
+ * (page-locked) the values are also delivered there in row chunks as in
+ * skg_h1_assemble_affine_host.  Stream-ordered. */
+int skg_p1_assemble_affine_forms(const skg_pattern *pattern, const double *d_p,
+                                 int64_t npts, const int32_t *d_t, int64_t n_elements,
+                                 int32_t comp, int32_t nq, const double *h_X,
+                                 const double *h_W, const double *d_value,
+                                 const double *d_gradient, const double *d_symgrad,
+                                 const double *d_div, double c_value, double c_gradient,
+                                 double c_symgrad, double c_div, double *d_values,
+                                 double *h_values, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Nedelec N1 (lowest-order H(curl)) on affine tets.                    */
 

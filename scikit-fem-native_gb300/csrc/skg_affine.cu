@@ -1105,6 +1105,155 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
 }
 
+namespace {
+
+// ------------------------------------------------ P1 forms, per-element coefficients
+// Scalar or vector (CC components) P1 element matrices of the value, gradient,
+// symmetric-gradient and divergence kinds of bilinear_form_assembler.cpp:79-105
+// when every coefficient is constant on each element.  The barycentric
+// gradients are constant on an affine tetrahedron, so the point sums collapse
+// to the rule's weight sum sw = sum_q w_q and its mass table
+// M_ab = sum_q w_q N_a(x_q) N_b(x_q):
+//   K_(a,c),(b,d) = sw / |det J| [ s/2 (B_a,d B_b,c + d_cd B_a.B_b) + dv B_a,c B_b,d + d_cd g B_a.B_b ]
+//                 + d_cd v |det J| M_ab
+// with B the adjugate rows (det J times the barycentric gradients).  Every
+// kind gives a symmetric matrix, so only the blocks b >= a are evaluated,
+// each written with its transpose into the thread's element matrix in shared
+// memory; the block then stores all matrices coalesced.  About 300 FP64
+// instructions per vector element, a quarter of the tabulated path, and no
+// per-point data is read.
+struct P1FormsConst {
+    double sw;
+    double mass[16];
+    double cst[4];  // value, gradient, symmetric gradient, divergence when the array is NULL
+};
+
+template <int CC, int BLK>
+__global__ void __launch_bounds__(BLK) k_p1_forms_ke(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                     const double *__restrict__ p, int64_t npts,
+                                                     const int32_t *__restrict__ t,
+                                                     const double *__restrict__ cv, const double *__restrict__ cg,
+                                                     const double *__restrict__ cs, const double *__restrict__ cd,
+                                                     P1FormsConst fc, double *__restrict__ Ke) {
+    constexpr int L = 4 * CC, LL = L * L, LP = LL + 1;
+    extern __shared__ double stage[];  // BLK x LP
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * BLK;
+    const int64_t e = e0 + threadIdx.x;
+    const int nvalid = (int)(e_end - e0 < BLK ? e_end - e0 : BLK);
+    double *st = stage + threadIdx.x * LP;
+    if (e < e_end) {
+        int32_t v[4];
+        const bool ok = load_vertices(t, ne, e, npts, v);
+        double J[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const double x0 = p[i * npts + v[0]];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
+        }
+        double b[4][3];
+        b[1][0] = J[4] * J[8] - J[5] * J[7];
+        b[1][1] = J[2] * J[7] - J[1] * J[8];
+        b[1][2] = J[1] * J[5] - J[2] * J[4];
+        b[2][0] = J[5] * J[6] - J[3] * J[8];
+        b[2][1] = J[0] * J[8] - J[2] * J[6];
+        b[2][2] = J[2] * J[3] - J[0] * J[5];
+        b[3][0] = J[3] * J[7] - J[4] * J[6];
+        b[3][1] = J[1] * J[6] - J[0] * J[7];
+        b[3][2] = J[0] * J[4] - J[1] * J[3];
+        const double ad = fabs(J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
+        const double inv = ok ? fc.sw / ad : __longlong_as_double(0x7ff8000000000000LL);
+        const double vm = (cv ? cv[e] : fc.cst[0]) * ad;
+        const double hs = 0.5 * (cs ? cs[e] : fc.cst[2]) * inv;
+        const double dv = (cd ? cd[e] : fc.cst[3]) * inv;
+        const double dg = (cg ? cg[e] : fc.cst[1]) * inv + hs;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double sa[CC], da[CC];
+#pragma unroll
+            for (int c = 0; c < CC; ++c) {
+                sa[c] = hs * b[a][c];
+                da[c] = dv * b[a][c];
+            }
+#pragma unroll
+            for (int bb = a; bb < 4; ++bb) {
+                const double gg = b[a][0] * b[bb][0] + b[a][1] * b[bb][1] + b[a][2] * b[bb][2];
+                const double diag = dg * gg + vm * fc.mass[a * 4 + bb];
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+#pragma unroll
+                    for (int d = 0; d < CC; ++d) {
+                        double val = sa[d] * b[bb][c] + da[c] * b[bb][d];
+                        if (c == d) val += diag;
+                        st[(a * CC + c) * L + bb * CC + d] = val;
+                        if (bb != a) st[(bb * CC + d) * L + a * CC + c] = val;
+                    }
+            }
+        }
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < nvalid * LL; x += BLK) {
+        const int el = x / LL, k = x - el * LL;
+        Ke[(e0 + el) * (int64_t)LL + k] = stage[el * LP + k];
+    }
+}
+
+template <int CC, int BLK>
+void launch_p1_forms(int64_t ne, int64_t e0, int64_t e1, const double *d_p, int64_t npts, const int32_t *d_t,
+                     const double *const coef[4], const P1FormsConst &fc, double *Ke, cudaStream_t s) {
+    if (e1 <= e0) return;
+    const int smem = BLK * (16 * CC * CC + 1) * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_p1_forms_ke<CC, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_p1_forms_ke<CC, BLK><<<grid_for(e1 - e0, BLK), BLK, smem, s>>>(ne, e0, e1, d_p, npts, d_t, coef[0], coef[1],
+                                                                     coef[2], coef[3], fc, Ke);
+    SKG_LAUNCH_CHECK("p1_forms_ke");
+}
+
+}  // namespace
+
+void p1_forms_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t, int64_t ne,
+                       int comp, int nq, const double *h_X, const double *h_W, const double *const coef[4],
+                       const double cst[4], double *d_values, double *h_values, cudaStream_t s) {
+    require(pat != nullptr, "pattern is NULL");
+    require(comp == 1 || comp == 3, "P1 forms take 1 or 3 components");
+    require(ne == pat->n_elements && pat->row_local == 4 * comp && pat->col_local == 4 * comp,
+            "mesh does not match the pattern");
+    require(nq > 0 && h_X && h_W, "quadrature rule is empty");
+    require(ne == 0 || (d_p && d_t), "mesh arrays are NULL");
+    require(pat->nnz == 0 || d_values, "output is NULL");
+    require(pat->max_row_len > 0, "pattern has no row groups");
+    P1FormsConst fc{};
+    for (int q = 0; q < nq; ++q) {
+        const double x = h_X[q], y = h_X[nq + q], z = h_X[2 * nq + q], w = h_W[q];
+        const double N[4] = {1.0 - x - y - z, x, y, z};
+        fc.sw += w;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) fc.mass[a * 4 + b] += w * N[a] * N[b];
+    }
+    for (int k = 0; k < 4; ++k) fc.cst[k] = coef[k] ? 0.0 : cst[k];
+    if (ne == 0) {
+        if (pat->nnz) SKG_CUDA(cudaMemsetAsync(d_values, 0, (size_t)pat->nnz * sizeof(double), s));
+        if (h_values && pat->nnz)
+            SKG_CUDA(cudaMemcpyAsync(h_values, d_values, (size_t)pat->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+        return;
+    }
+    const int L = 4 * comp;
+    DevBuf<double> Ke((size_t)ne * L * L, s);
+    run_passes(
+        pat, ne, d_values, h_values, s,
+        [&](int64_t e0, int64_t e1) {
+            if (comp == 3) launch_p1_forms<3, 64>(ne, e0, e1, d_p, npts, d_t, coef, fc, Ke.get(), s);
+            else launch_p1_forms<1, 128>(ne, e0, e1, d_p, npts, d_t, coef, fc, Ke.get(), s);
+        },
+        [&](const GroupSet &gs, cudaStream_t st) {
+            if (comp == 3) add_element_rows<12>(pat, Ke.get(), d_values, st, gs);
+            else add_element_rows<4>(pat, Ke.get(), d_values, st, gs);
+        });
+}
+
 }  // namespace skg
 
 using namespace skg;
@@ -1117,6 +1266,21 @@ extern "C" int skg_h1_assemble_affine(const skg_pattern *pat, const double *d_p,
         (void)d_dofs;
         affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values,
                         as_stream(stream), nullptr, nullptr);
+    });
+}
+
+extern "C" int skg_p1_assemble_affine_forms(const skg_pattern *pat, const double *d_p, int64_t npts,
+                                            const int32_t *d_t, int64_t ne, int32_t comp, int32_t nq,
+                                            const double *h_X, const double *h_W, const double *d_value,
+                                            const double *d_gradient, const double *d_symgrad,
+                                            const double *d_div, double c_value, double c_gradient,
+                                            double c_symgrad, double c_div, double *d_values, double *h_values,
+                                            void *stream) {
+    return guarded([&] {
+        const double *coef[4] = {d_value, d_gradient, d_symgrad, d_div};
+        const double cst[4] = {c_value, c_gradient, c_symgrad, c_div};
+        p1_forms_assemble(pat, d_p, npts, d_t, ne, comp, nq, h_X, h_W, coef, cst, d_values, h_values,
+                          as_stream(stream));
     });
 }
 

@@ -83,6 +83,9 @@ SIGNATURES = {
     "skg_nh_assemble_surrogate_host": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_double, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _i64p,
                                        _vp],
+    "skg_p1_assemble_affine_forms": [_vp, _vp, _i64, _vp, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp,
+                                     _vp],
     "skg_linear_assemble_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp,
                                       _vp, _vp],
 }

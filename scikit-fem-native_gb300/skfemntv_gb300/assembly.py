@@ -333,6 +333,10 @@ class NativeBilinearForm:
             return self.target.d_values
         if prec != SKG_FP64:
             raise UnsupportedNativeForm("split precision is available on the affine scalar gradient path")
+        forms = self._p1_forms(value, gradient, symmetric_gradient, divergence)
+        if forms is not None:
+            self._p1_forms_launch(forms, dev.ptr(self.target.d_values), None)
+            return self.target.d_values
         tab = b._device_tabulation()
         coefs = [self._point_coefficient(c, E, Q, n)
                  for c, n in ((value, "value"), (gradient, "gradient"),
@@ -341,6 +345,51 @@ class NativeBilinearForm:
              dev.ptr(tab["shape"]), dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), *(dev.ptr(c) for c in coefs),
              dev.ptr(self.target.d_values), None, dev.stream_ptr())
         return self.target.d_values
+
+    def _p1_forms(self, value, gradient, symmetric_gradient, divergence):
+        """The four coefficients as (E,) arrays, 0-d scalars or None when the
+        fused P1 path applies (affine P1 basis with 1 or 3 components, every
+        coefficient constant on each element, row-grouped pattern), else None."""
+        b = self.basis
+        if b._nodes != 4 or b._comp not in (1, 3) or not b.is_affine or not self.pattern.row_groups:
+            return None
+        E, Q = b._coefficient_shape
+        out = []
+        for c, name in ((value, "value"), (gradient, "gradient"),
+                        (symmetric_gradient, "symmetric_gradient"), (divergence, "divergence")):
+            if c is None:
+                out.append(None)
+                continue
+            if hasattr(c, "is_cuda"):
+                return None  # torch tensors of point values: the tabulated path reads them in place
+            pe = per_element(c, E, Q, name)
+            if pe is None:
+                return None
+            out.append(pe)
+        return out
+
+    def _p1_forms_launch(self, forms, d_values, h_values):
+        """skg_p1_assemble_affine_forms; per-element arrays are read in place
+        from host memory when `h_values` is given (the caller synchronises
+        before the arrays go away), else uploaded.  Returns the uploads."""
+        b = self.basis
+        E, Q = b._coefficient_shape
+        ptrs, consts, keep = [], [], []
+        for c in forms:
+            if c is None or np.ndim(c) == 0:
+                ptrs.append(None)
+                consts.append(0.0 if c is None else float(c))
+                continue
+            ptr = dev.host_readable(c) if h_values is not None else None
+            if ptr is None:
+                keep.append(dev.to_device(c, np.float64))
+                ptr = dev.ptr(keep[-1])
+            ptrs.append(ptr)
+            consts.append(0.0)
+        call("skg_p1_assemble_affine_forms", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
+             dev.ptr(b.mesh._dev("t")), E, b._comp, Q, dev.hptr(b.X), dev.hptr(b.W), *ptrs, *consts,
+             d_values, h_values, dev.stream_ptr())
+        return keep
 
     def _point_coefficient(self, c, E, Q, name):
         """(E, Q) float64 device array for a coefficient: a CUDA tensor of that
@@ -377,6 +426,10 @@ class NativeBilinearForm:
         fast = self._affine_coefficient(value, gradient, symmetric_gradient, divergence)
         if fast is not None:
             self._affine(fast, _precision(precision), self.target.pinned_ptr(), host=True)
+            return self.target.finish_direct()
+        forms = self._p1_forms(value, gradient, symmetric_gradient, divergence)
+        if forms is not None and _precision(precision) == SKG_FP64:
+            self._p1_forms_launch(forms, dev.ptr(self.target.d_values), self.target.pinned_ptr())
             return self.target.finish_direct()
         self.assemble_device(value=value, gradient=gradient, symmetric_gradient=symmetric_gradient,
                              divergence=divergence, precision=precision)

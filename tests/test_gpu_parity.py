@@ -523,3 +523,58 @@ def test_tabulated_kinds_per_point_coefficients(quadratic, comp, kinds):
     d, indptr, indices = O.bilinear_assemble(ob, **co)
     assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
     assert relerr(K.data, d) < RTOL
+
+
+@pytest.mark.parametrize("comp", [1, 3])
+@pytest.mark.parametrize("kinds", [KINDS, ("value", "gradient"), ("symmetric_gradient", "divergence")])
+@pytest.mark.parametrize("one_point", [False, True])
+def test_fused_p1_forms_per_element_coefficients(comp, kinds, one_point):
+    """Affine P1 forms with per-element coefficients go through the fused kernel (no tabulated point data:
+    the basis' tabulation is never built) and match the oracle, on the device and through the host matrix."""
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    rng = np.random.default_rng(7 + comp + 10 * one_point + len(kinds))
+    n = 5
+    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 2.0, n + 1),) * 3)
+    inner = np.all((m.p > 1e-9) & (m.p < 2 - 1e-9), axis=0)
+    m.p[:, inner] += rng.uniform(-0.3 / n, 0.3 / n, (3, int(inner.sum())))
+    quadrature = (X1, W1) if one_point else None
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=comp), quadrature=quadrature)
+    E, Q = b._coefficient_shape
+    co = {k: rng.uniform(0.5, 2.0, (E, 1)) for k in kinds}
+    form = NativeBilinearForm(b)
+    K = form.assemble(**co)
+    assert b._tab is None  # fused path: no per-point tabulation
+    ob = O.make_basis(m.p, m.t, False, comp=comp, quadrature=quadrature)
+    d, indptr, indices = O.bilinear_assemble(ob, **co)
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, d) < RTOL
+    dv = form.assemble_device(**co).cpu().numpy()[: len(d)]
+    assert np.array_equal(dv.view(np.int64), K.data.view(np.int64))
+    # scalar constants take no array at all
+    K2 = form.assemble(**{k: 1.5 for k in kinds}).data.copy()
+    d2, _, _ = O.bilinear_assemble(ob, **{k: 1.5 for k in kinds})
+    assert relerr(K2, d2) < RTOL
+
+
+def test_fused_p1_forms_chunked_host_output():
+    """Vector P1 elasticity above the chunking threshold (> 2^22 nnz): host values delivered in row chunks equal
+    the device values bit for bit, and the per-point path (tabulated kernels) agrees to rounding."""
+    import torch
+
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    n = 32
+    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, n + 1),) * 3)
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3))
+    form = NativeBilinearForm(b)
+    assert form.pattern.nnz > 1 << 22
+    co = dict(value=0.5, symmetric_gradient=2.0, divergence=10.0)
+    host = form.assemble(**co).data.copy()
+    dv = form.assemble_device(**co).cpu().numpy()[: form.pattern.nnz]
+    assert np.array_equal(host.view(np.int64), dv.view(np.int64))
+    E, Q = b._coefficient_shape
+    pts = {k: torch.full((E, Q), v, dtype=torch.float64, device="cuda") for k, v in co.items()}
+    tab = form.assemble_device(**pts).cpu().numpy()[: form.pattern.nnz]
+    assert b._tab is not None
+    assert relerr(tab, dv) < RTOL
