@@ -103,8 +103,11 @@ __device__ __forceinline__ void flush_stage(const float4 *stage, float4 *Gout, i
 }
 
 // G_kl = b_k . A b_l / |det J| of element e in FP64 (b: adjugate rows, the
-// scaled barycentric gradients).  Returns the element's symmetry (scalar
-// coefficient, or a tensor equal to its transpose).
+// scaled barycentric gradients).  Only the block k, l >= 1 takes dot products
+// (its upper triangle when A is symmetric): b_0 = -(b_1 + b_2 + b_3) gives
+// G_0l = -(G_1l + G_2l + G_3l), G_k0 likewise and G_00 = -(G_01 + G_02 + G_03),
+// and 1 / |det J| scales the coefficient, not the 16 results.  Returns the
+// element's symmetry (scalar coefficient, or a tensor equal to its transpose).
 __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                             const int32_t *__restrict__ t, int coef_kind,
                                             const double *__restrict__ coef, int64_t e, double g[16]) {
@@ -128,36 +131,57 @@ __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict
     b[3][1] = J[1] * J[6] - J[0] * J[7];
     b[3][2] = J[0] * J[4] - J[1] * J[3];
     const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) b[0][i] = -(b[1][i] + b[2][i] + b[3][i]);
     const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
+    bool sym = true;
     if (coef_kind == 0) {
         const double sc = (coef ? coef[e] : 1.0) * inv;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 1; k < 4; ++k)
 #pragma unroll
             for (int l = k; l < 4; ++l) {
                 const double val = sc * (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]);
                 g[k * 4 + l] = val;
                 g[l * 4 + k] = val;
             }
-        return true;
+    } else {
+        double A[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
+        // symmetric to rounding (A built as Q D Q^T in floating point is not bitwise
+        // symmetric): mirroring K_ab into K_ba then changes entries by ~1e-16 relative
+        const double scale = 1e-14 * (fabs(A[0]) + fabs(A[4]) + fabs(A[8]) + fabs(A[1]) + fabs(A[2]) + fabs(A[5]));
+        sym = fabs(A[1] - A[3]) <= scale && fabs(A[2] - A[6]) <= scale && fabs(A[5] - A[7]) <= scale;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] *= inv;
+#pragma unroll
+        for (int l = 1; l < 4; ++l) {
+            double Ab[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) Ab[i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {
+                if (k > l && sym) continue;  // mirrored below
+                g[k * 4 + l] = b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2];
+            }
+        }
+        if (sym) {
+#pragma unroll
+            for (int k = 2; k < 4; ++k)
+#pragma unroll
+                for (int l = 1; l < k; ++l) g[k * 4 + l] = g[l * 4 + k];
+        }
     }
-    double A[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
+    for (int l = 1; l < 4; ++l) g[l] = -(g[4 + l] + g[8 + l] + g[12 + l]);
+    if (sym) {
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-        double Ab[3];
+        for (int k = 1; k < 4; ++k) g[k * 4] = g[k];
+    } else {
 #pragma unroll
-        for (int i = 0; i < 3; ++i) Ab[i] = A[i * 3] * b[l][0] + A[i * 3 + 1] * b[l][1] + A[i * 3 + 2] * b[l][2];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) g[k * 4 + l] = inv * (b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2]);
+        for (int k = 1; k < 4; ++k) g[k * 4] = -(g[k * 4 + 1] + g[k * 4 + 2] + g[k * 4 + 3]);
     }
-    // symmetric to rounding (A built as Q D Q^T in floating point is not bitwise
-    // symmetric): mirroring K_ab into K_ba then changes entries by ~1e-16 relative
-    const double scale = 1e-14 * (fabs(A[0]) + fabs(A[4]) + fabs(A[8]) + fabs(A[1]) + fabs(A[2]) + fabs(A[5]));
-    return fabs(A[1] - A[3]) <= scale && fabs(A[2] - A[6]) <= scale && fabs(A[5] - A[7]) <= scale;
+    g[0] = -(g[1] + g[2] + g[3]);
+    return sym;
 }
 
 __global__ void __launch_bounds__(kElemBlock) k_elem_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
