@@ -242,7 +242,7 @@ def measured_peak():
 
 # FP64 instructions per element of the FP64 passes (DFMA + DMUL + DADD thread
 # instructions counted by ncu on the 32^3 case, profiles/fp64_ops_p2_aniso_32.md).
-FP64_OPS_PER_ELEMENT = {"k_elem_ke_fp64": 293.1, "k_rows_ke": 111.1}
+FP64_OPS_PER_ELEMENT = {"k_elem_ke_fp64": 253.0, "k_rows_ke": 111.1}
 # The same for the plain neo-Hookean call (profiles/fp64_ops_nh_32.md):
 # element matrices k_nh_ke + row pass k_rows_ke<12>.
 NH_FP64_OPS_PER_ELEMENT = 535.1 + 180.0

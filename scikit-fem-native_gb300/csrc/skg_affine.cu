@@ -1143,8 +1143,8 @@ namespace {
 // with B the adjugate rows (det J times the barycentric gradients).  Every
 // kind gives a symmetric matrix, so only the blocks b >= a are evaluated,
 // each written with its transpose into the thread's element matrix in shared
-// memory; the block then stores all matrices coalesced.  About 300 FP64
-// instructions per vector element, a quarter of the tabulated path, and no
+// memory; the block then stores all matrices coalesced.  About 260 FP64
+// instructions per vector element, a fifth of the tabulated path, and no
 // per-point data is read.
 struct P1FormsConst {
     double sw;
@@ -1195,11 +1195,12 @@ __global__ void __launch_bounds__(BLK) k_p1_forms_ke(int64_t ne, int64_t e_begin
         const double dg = (cg ? cg[e] : fc.cst[1]) * inv + hs;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            double sa[CC], da[CC];
+            double sa[CC], da[CC], ta[CC];  // (s/2) B_a, dv B_a and their sum (entries c == d)
 #pragma unroll
             for (int c = 0; c < CC; ++c) {
                 sa[c] = hs * b[a][c];
                 da[c] = dv * b[a][c];
+                ta[c] = sa[c] + da[c];
             }
 #pragma unroll
             for (int bb = a; bb < 4; ++bb) {
@@ -1209,10 +1210,11 @@ __global__ void __launch_bounds__(BLK) k_p1_forms_ke(int64_t ne, int64_t e_begin
                 for (int c = 0; c < CC; ++c)
 #pragma unroll
                     for (int d = 0; d < CC; ++d) {
-                        double val = sa[d] * b[bb][c] + da[c] * b[bb][d];
-                        if (c == d) val += diag;
+                        if (bb == a && d < c) continue;  // diagonal block: symmetric in (c, d)
+                        const double val =
+                            c == d ? diag + ta[c] * b[bb][c] : sa[d] * b[bb][c] + da[c] * b[bb][d];
                         st[(a * CC + c) * L + bb * CC + d] = val;
-                        if (bb != a) st[(bb * CC + d) * L + a * CC + c] = val;
+                        if (bb != a || c != d) st[(bb * CC + d) * L + a * CC + c] = val;
                     }
             }
         }
