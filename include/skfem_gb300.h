@@ -375,6 +375,19 @@ int skg_p1_energy_grad(const skg_pattern *vertex_incidence,
                        double grad_out, double *d_gkappa, double *d_gp,
                        double *d_gu, double *d_gv, void *stream);
 
+/* skg_p1_energy_grad that also writes J itself to d_energy (1): the element
+ * pass reduces the element energies exactly as skg_p1_energy does (same
+ * value, same summation order) while it forms the adjoint contributions, so
+ * one call gives J and its gradients (for a forward pass that knows the
+ * gradients will be needed).  The gradients are those of grad_out * J. */
+int skg_p1_energy_value_and_grad(const skg_pattern *vertex_incidence,
+                                 const skg_pattern *dof_incidence, const double *d_p,
+                                 int64_t npts, const int32_t *d_t, int64_t n_elements,
+                                 const int32_t *d_dofs, const double *d_kappa,
+                                 const double *d_u, const double *d_v, double wsum,
+                                 double grad_out, double *d_energy, double *d_gkappa,
+                                 double *d_gp, double *d_gu, double *d_gv, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Neo-Hookean residual and tangent on vector P1 tetrahedra.  Replaces   */
 /* the reference's oracle pipeline for the law of                        */

@@ -26,8 +26,11 @@
 namespace skg {
 namespace {
 
+// Geometry of element e: J and its cofactor matrix C = det J * J^-1 (row k of
+// C is det J times the gradient of lambda_{k+1}); the kernels apply the
+// powers of 1 / det J to a few scalars instead of forming J^-1.
 struct ElemAdj {
-    double J[9], Ji[9], det;
+    double C[9], det, id;  // id = 1 / det J
 };
 
 __device__ __forceinline__ bool elem_geom(const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
@@ -39,33 +42,31 @@ __device__ __forceinline__ bool elem_geom(const double *__restrict__ p, int64_t 
         ok = ok && v[k] >= 0 && v[k] < npts;
     }
     if (!ok) v[0] = v[1] = v[2] = v[3] = 0;
+    double J[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const double x0 = p[i * npts + v[0]];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) g.J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
+        for (int r = 0; r < 3; ++r) J[i * 3 + r] = p[i * npts + v[r + 1]] - x0;
     }
-    const double *J = g.J;
-    const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[2] * J[7] - J[1] * J[8], c02 = J[1] * J[5] - J[2] * J[4];
-    const double c10 = J[5] * J[6] - J[3] * J[8], c11 = J[0] * J[8] - J[2] * J[6], c12 = J[2] * J[3] - J[0] * J[5];
-    const double c20 = J[3] * J[7] - J[4] * J[6], c21 = J[1] * J[6] - J[0] * J[7], c22 = J[0] * J[4] - J[1] * J[3];
-    g.det = J[0] * c00 + J[1] * c10 + J[2] * c20;
-    const double id = 1.0 / g.det;
-    g.Ji[0] = c00 * id; g.Ji[1] = c01 * id; g.Ji[2] = c02 * id;
-    g.Ji[3] = c10 * id; g.Ji[4] = c11 * id; g.Ji[5] = c12 * id;
-    g.Ji[6] = c20 * id; g.Ji[7] = c21 * id; g.Ji[8] = c22 * id;
+    double *C = g.C;
+    C[0] = J[4] * J[8] - J[5] * J[7]; C[1] = J[2] * J[7] - J[1] * J[8]; C[2] = J[1] * J[5] - J[2] * J[4];
+    C[3] = J[5] * J[6] - J[3] * J[8]; C[4] = J[0] * J[8] - J[2] * J[6]; C[5] = J[2] * J[3] - J[0] * J[5];
+    C[6] = J[3] * J[7] - J[4] * J[6]; C[7] = J[1] * J[6] - J[0] * J[7]; C[8] = J[0] * J[4] - J[1] * J[3];
+    g.det = J[0] * C[0] + J[1] * C[3] + J[2] * C[6];
+    g.id = 1.0 / g.det;
     return ok;
 }
 
-// J^-T y (= rows of J^-1 weighted): out_j = sum_k Ji[k][j] y_k
-__device__ __forceinline__ void mul_JiT(const double Ji[9], const double y[3], double out[3]) {
+// C^T y: out_j = sum_k C[k][j] y_k  (det J times J^-T y)
+__device__ __forceinline__ void mul_CT(const double C[9], const double y[3], double out[3]) {
 #pragma unroll
-    for (int j = 0; j < 3; ++j) out[j] = Ji[0 * 3 + j] * y[0] + Ji[1 * 3 + j] * y[1] + Ji[2 * 3 + j] * y[2];
+    for (int j = 0; j < 3; ++j) out[j] = C[0 * 3 + j] * y[0] + C[1 * 3 + j] * y[1] + C[2 * 3 + j] * y[2];
 }
-// J^-1 y: out_i = sum_j Ji[i][j] y_j
-__device__ __forceinline__ void mul_Ji(const double Ji[9], const double y[3], double out[3]) {
+// C y: out_i = sum_j C[i][j] y_j  (det J times J^-1 y)
+__device__ __forceinline__ void mul_C(const double C[9], const double y[3], double out[3]) {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) out[i] = Ji[i * 3 + 0] * y[0] + Ji[i * 3 + 1] * y[1] + Ji[i * 3 + 2] * y[2];
+    for (int i = 0; i < 3; ++i) out[i] = C[i * 3 + 0] * y[0] + C[i * 3 + 1] * y[1] + C[i * 3 + 2] * y[2];
 }
 
 constexpr int kRed = 256;
@@ -86,10 +87,11 @@ __global__ void __launch_bounds__(kRed) k_energy(int64_t ne, const double *__res
         const int32_t d0 = dofs[e * 4], d1 = dofs[e * 4 + 1], d2 = dofs[e * 4 + 2], d3 = dofs[e * 4 + 3];
         const double gu[3] = {u[d1] - u[d0], u[d2] - u[d0], u[d3] - u[d0]};
         const double gv[3] = {v[d1] - v[d0], v[d2] - v[d0], v[d3] - v[d0]};
-        double a[3], b[3];
-        mul_JiT(g.Ji, gu, a);
-        mul_JiT(g.Ji, gv, b);
-        f = (kappa ? kappa[e] : 1.0) * fabs(g.det) * wsum * (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+        double a[3], b[3];  // det J times grad u_e, grad v_e
+        mul_CT(g.C, gu, a);
+        mul_CT(g.C, gv, b);
+        // kappa |det J| wsum (grad u_e . grad v_e) = kappa wsum (a . b) / |det J|
+        f = (kappa ? kappa[e] : 1.0) * wsum * fabs(g.id) * (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
     }
     red[threadIdx.x] = f;
     __syncthreads();
@@ -111,57 +113,94 @@ __global__ void k_sum_blocks(const double *__restrict__ in, int64_t n, double *_
     if (lane == 0) *out = s;
 }
 
-// Backward, element pass: dJ/dkappa and the per-element vertex / DOF
-// contributions (scaled by the upstream gradient).  contrib layout per
-// element: 12 doubles dx (vertex k, coordinate i at k*3+i), 4 du, 4 dv.
-__global__ void k_energy_grad_elem(int64_t ne, const double *__restrict__ p, int64_t npts,
-                                   const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
-                                   const double *__restrict__ kappa, const double *__restrict__ u,
-                                   const double *__restrict__ v, double wsum, double gout,
-                                   double *__restrict__ gkappa, double *__restrict__ contrib) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+// Element e's adjoint contributions (see k_energy_grad_elem); returns its energy.
+__device__ __forceinline__ double elem_adjoint(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                               const int32_t *__restrict__ t, const int32_t *__restrict__ dofs,
+                                               const double *__restrict__ kappa, const double *__restrict__ u,
+                                               const double *__restrict__ v, double wsum, double gout,
+                                               double *__restrict__ gkappa, double *__restrict__ contrib,
+                                               int64_t e) {
     int32_t vt[4];
     ElemAdj g;
     elem_geom(p, npts, t, ne, e, vt, g);
     const int32_t d0 = dofs[e * 4], d1 = dofs[e * 4 + 1], d2 = dofs[e * 4 + 2], d3 = dofs[e * 4 + 3];
     const double gu[3] = {u[d1] - u[d0], u[d2] - u[d0], u[d3] - u[d0]};
     const double gv[3] = {v[d1] - v[d0], v[d2] - v[d0], v[d3] - v[d0]};
+    // with tildes for the scaled quantities:  a = a~ / det, b = b~ / det,
+    // c = J^-1 b = c~ / det^2, d = J^-1 a = d~ / det^2, phi = a . b = phi~ / det^2
     double a[3], b[3], c[3], d[3];
-    mul_JiT(g.Ji, gu, a);
-    mul_JiT(g.Ji, gv, b);
-    mul_Ji(g.Ji, b, c);
-    mul_Ji(g.Ji, a, d);
+    mul_CT(g.C, gu, a);
+    mul_CT(g.C, gv, b);
+    mul_C(g.C, b, c);
+    mul_C(g.C, a, d);
     const double phi = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-    const double V = fabs(g.det) * wsum;
+    const double aid = fabs(g.id);
     const double k = kappa ? kappa[e] : 1.0;
-    if (gkappa) gkappa[e] = gout * V * phi;
-    const double s = gout * k * V;
+    if (gkappa) gkappa[e] = gout * wsum * aid * phi;  // V phi = wsum phi~ / |det|
+    const double s2 = gout * k * wsum * aid;           // s / det^2 with s = gout kappa V
+    const double s3 = s2 * g.id;                       // s / det^3
     double *out = contrib + e * 20;
-    // dJ/dJ_ij = s (phi Ji[j][i] - a_i c_j - b_i d_j)
+    // dJ/dJ_ij = s (phi Ji[j][i] - a_i c_j - b_i d_j) = s / det^3 (phi~ C[j][i] - a~_i c~_j - b~_i d~_j)
+    const double ph = s3 * phi;
+    double as[3], bs[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        as[i] = s3 * a[i];
+        bs[i] = s3 * b[i];
+    }
     double col_sum[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const double gJ = s * (phi * g.Ji[j * 3 + i] - a[i] * c[j] - b[i] * d[j]);
+            const double gJ = ph * g.C[j * 3 + i] - as[i] * c[j] - bs[i] * d[j];
             out[(j + 1) * 3 + i] = gJ;  // vertex j+1, coordinate i
             col_sum[i] += gJ;
         }
 #pragma unroll
     for (int i = 0; i < 3; ++i) out[i] = -col_sum[i];
-    // grad lambda_m = J^-T e_{m-1} (m = 1..3), grad lambda_0 = -(sum)
-    double gl[4][3];
+    // dJ/du_m = s grad lambda_m . b = s c_{m-1} (m = 1..3), dJ/dv_m = s d_{m-1};
+    // lambda_0's gradient is minus the sum of the others
+    double du[3], dv[3];
 #pragma unroll
-    for (int m = 1; m < 4; ++m)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) gl[m][j] = g.Ji[(m - 1) * 3 + j];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) gl[0][j] = -(gl[1][j] + gl[2][j] + gl[3][j]);
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        out[12 + m] = s * (gl[m][0] * b[0] + gl[m][1] * b[1] + gl[m][2] * b[2]);
-        out[16 + m] = s * (gl[m][0] * a[0] + gl[m][1] * a[1] + gl[m][2] * a[2]);
+    for (int m = 0; m < 3; ++m) {
+        du[m] = s2 * c[m];
+        dv[m] = s2 * d[m];
+        out[13 + m] = du[m];
+        out[17 + m] = dv[m];
+    }
+    out[12] = -(du[0] + du[1] + du[2]);
+    out[16] = -(dv[0] + dv[1] + dv[2]);
+    return k * wsum * aid * phi;  // the element energy, as k_energy forms it
+}
+
+// Backward, element pass: dJ/dkappa and the per-element vertex / DOF
+// contributions (scaled by the upstream gradient).  contrib layout per
+// element: 12 doubles dx (vertex k, coordinate i at k*3+i), 4 du, 4 dv.
+// WITH_J: the element energies are also reduced per block exactly as
+// k_energy does (same expression, same tree), so that one pass gives J and
+// its gradients.
+template <bool WITH_J>
+__global__ void __launch_bounds__(kRed) k_energy_grad_elem(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                           const int32_t *__restrict__ t,
+                                                           const int32_t *__restrict__ dofs,
+                                                           const double *__restrict__ kappa,
+                                                           const double *__restrict__ u,
+                                                           const double *__restrict__ v, double wsum, double gout,
+                                                           double *__restrict__ gkappa, double *__restrict__ contrib,
+                                                           double *__restrict__ block_sums) {
+    const int64_t e = (int64_t)blockIdx.x * kRed + threadIdx.x;
+    double f = 0.0;
+    if (e < ne) f = elem_adjoint(ne, p, npts, t, dofs, kappa, u, v, wsum, gout, gkappa, contrib, e);
+    if constexpr (WITH_J) {
+        __shared__ double red[kRed];
+        red[threadIdx.x] = f;
+        __syncthreads();
+        for (int off = kRed / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
     }
 }
 
@@ -223,24 +262,37 @@ extern "C" int skg_p1_energy(const double *d_p, int64_t npts, const int32_t *d_t
     });
 }
 
-extern "C" int skg_p1_energy_grad(const skg_pattern *vertex_inc, const skg_pattern *dof_inc, const double *d_p,
-                                  int64_t npts, const int32_t *d_t, int64_t ne, const int32_t *d_dofs,
-                                  const double *d_kappa, const double *d_u, const double *d_v, double wsum,
-                                  double grad_out, double *d_gkappa, double *d_gp, double *d_gu, double *d_gv,
-                                  void *stream) {
-    return guarded([&] {
+namespace {
+void energy_grad(const skg_pattern *vertex_inc, const skg_pattern *dof_inc, const double *d_p, int64_t npts,
+                 const int32_t *d_t, int64_t ne, const int32_t *d_dofs, const double *d_kappa, const double *d_u,
+                 const double *d_v, double wsum, double grad_out, double *d_energy, double *d_gkappa, double *d_gp,
+                 double *d_gu, double *d_gv, cudaStream_t s) {
+    {
         require(ne >= 0 && (ne == 0 || (d_p && d_t && d_dofs && d_u && d_v)), "invalid energy arguments");
         require(!d_gp || (vertex_inc && vertex_inc->row_local == 4 && vertex_inc->n_elements == ne &&
                           vertex_inc->n_rows == npts),
                 "coordinate gradients need the vertex incidence handle of this mesh");
         require((!d_gu && !d_gv) || (dof_inc && dof_inc->row_local == 4 && dof_inc->n_elements == ne),
                 "DOF gradients need the DOF incidence handle of this basis");
-        cudaStream_t s = as_stream(stream);
         DevBuf<double> contrib((size_t)(ne ? ne : 1) * 20, s);
+        const int64_t nb = ne ? (ne + kRed - 1) / kRed : 1;
+        DevBuf<double> partial(d_energy ? nb : 0, s);
         if (ne) {
-            k_energy_grad_elem<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_dofs, d_kappa, d_u, d_v, wsum,
-                                                                 grad_out, d_gkappa, contrib.get());
+            if (d_energy)
+                k_energy_grad_elem<true><<<(unsigned)nb, kRed, 0, s>>>(ne, d_p, npts, d_t, d_dofs, d_kappa, d_u, d_v,
+                                                                       wsum, grad_out, d_gkappa, contrib.get(),
+                                                                       partial.get());
+            else
+                k_energy_grad_elem<false><<<(unsigned)nb, kRed, 0, s>>>(ne, d_p, npts, d_t, d_dofs, d_kappa, d_u,
+                                                                        d_v, wsum, grad_out, d_gkappa, contrib.get(),
+                                                                        nullptr);
             SKG_LAUNCH_CHECK("energy_grad_elem");
+        } else if (d_energy) {
+            SKG_CUDA(cudaMemsetAsync(partial.get(), 0, 8, s));
+        }
+        if (d_energy) {
+            k_sum_blocks<<<1, 32, 0, s>>>(partial.get(), nb, d_energy);
+            SKG_LAUNCH_CHECK("energy_sum");
         }
         const bool shared = vertex_inc == dof_inc;  // one incidence structure for both
         if (d_gp && shared) {
@@ -261,5 +313,30 @@ extern "C" int skg_p1_energy_grad(const skg_pattern *vertex_inc, const skg_patte
                 dof_inc->n_rows, dof_inc->inc_ptr.get(), dof_inc->inc.get(), contrib.get(), nullptr, d_gu, d_gv);
             SKG_LAUNCH_CHECK("energy_grad_uv");
         }
+    }
+}
+}  // namespace
+
+extern "C" int skg_p1_energy_grad(const skg_pattern *vertex_inc, const skg_pattern *dof_inc, const double *d_p,
+                                  int64_t npts, const int32_t *d_t, int64_t ne, const int32_t *d_dofs,
+                                  const double *d_kappa, const double *d_u, const double *d_v, double wsum,
+                                  double grad_out, double *d_gkappa, double *d_gp, double *d_gu, double *d_gv,
+                                  void *stream) {
+    return guarded([&] {
+        energy_grad(vertex_inc, dof_inc, d_p, npts, d_t, ne, d_dofs, d_kappa, d_u, d_v, wsum, grad_out, nullptr,
+                    d_gkappa, d_gp, d_gu, d_gv, as_stream(stream));
+    });
+}
+
+extern "C" int skg_p1_energy_value_and_grad(const skg_pattern *vertex_inc, const skg_pattern *dof_inc,
+                                            const double *d_p, int64_t npts, const int32_t *d_t, int64_t ne,
+                                            const int32_t *d_dofs, const double *d_kappa, const double *d_u,
+                                            const double *d_v, double wsum, double grad_out, double *d_energy,
+                                            double *d_gkappa, double *d_gp, double *d_gu, double *d_gv,
+                                            void *stream) {
+    return guarded([&] {
+        require(d_energy != nullptr, "energy output is NULL");
+        energy_grad(vertex_inc, dof_inc, d_p, npts, d_t, ne, d_dofs, d_kappa, d_u, d_v, wsum, grad_out, d_energy,
+                    d_gkappa, d_gp, d_gu, d_gv, as_stream(stream));
     });
 }

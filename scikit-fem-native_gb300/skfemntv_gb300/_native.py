@@ -58,6 +58,8 @@ SIGNATURES = {
     "skg_p1_energy": [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp],
     "skg_p1_energy_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double,
                            ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
+    "skg_p1_energy_value_and_grad": [_vp, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, ctypes.c_double,
+                                     ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp],
     "skg_nh_assemble": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                         _vp, _vp, _vp],
     "skg_nh_assemble_host": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,

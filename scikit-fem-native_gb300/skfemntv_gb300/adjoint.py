@@ -3,11 +3,14 @@
 ``K(kappa)`` is the matrix ``asm(w.kappa * ddot(grad(u), grad(v)), basis)``
 assembles for a scalar P1 basis with one kappa per element.  ``P1Energy``
 evaluates J matrix-free on the GPU and exposes it as a
-``torch.autograd.Function`` whose backward pass is a hand-written adjoint
-kernel: it returns dJ/dkappa, dJ/d(node coordinates), dJ/du and dJ/dv,
-recomputing the element geometry instead of storing it.  (The reference has
-no autograd; this is the differentiation layer the GPU backend adds on top
-of its assembly path.)
+``torch.autograd.Function`` with a hand-written adjoint: dJ/dkappa,
+dJ/d(node coordinates), dJ/du and dJ/dv.  When an input requires a gradient
+the forward call runs one element pass that forms J and the adjoint
+contributions for a unit upstream gradient together (the geometry is
+computed once; nothing per element is kept), and the backward call scales
+the gathered gradients by the upstream gradient.  (The reference has no
+autograd; this is the differentiation layer the GPU backend adds on top of
+its assembly path.)
 """
 from __future__ import annotations
 
@@ -54,6 +57,21 @@ class P1Energy:
              dev.ptr(kappa), dev.ptr(u), dev.ptr(v), self.wsum, dev.ptr(out), dev.stream_ptr())
         return out[0]
 
+    def energy_and_gradients(self, kappa, coords, u, v, need=(True, True, True, True)):
+        """J and the gradients of J in one element pass (outputs not needed are None)."""
+        import torch
+
+        f64 = dict(dtype=torch.float64, device=coords.device)
+        out = torch.empty(1, **f64)
+        gk = torch.empty(self.E, **f64) if need[0] else None
+        gp = torch.empty((3, self.npts), **f64) if need[1] else None
+        gu = torch.empty(u.shape[0], **f64) if need[2] else None
+        gv = torch.empty(v.shape[0], **f64) if need[3] else None
+        call("skg_p1_energy_value_and_grad", self.vertex_inc.h, self.dof_inc.h, dev.ptr(coords), self.npts,
+             dev.ptr(self.t), self.E, dev.ptr(self.dofs), dev.ptr(kappa), dev.ptr(u), dev.ptr(v), self.wsum, 1.0,
+             dev.ptr(out), dev.ptr(gk), dev.ptr(gp), dev.ptr(gu), dev.ptr(gv), dev.stream_ptr())
+        return out[0], gk, gp, gu, gv
+
     def gradients(self, kappa, coords, u, v, need=(True, True, True, True)):
         import torch
 
@@ -88,15 +106,18 @@ try:
             coords = _check(coords, (3, op.npts), "coords")
             u = _check(u, (op.basis.N,), "u")
             v = _check(v, (op.basis.N,), "v")
-            ctx.op = op
-            ctx.save_for_backward(kappa, coords, u, v)
-            return op.energy(kappa, coords, u, v)
+            need = tuple(ctx.needs_input_grad[:4])
+            if not any(need):
+                return op.energy(kappa, coords, u, v)
+            # J and the unit-upstream gradients in one element pass
+            J, *grads = op.energy_and_gradients(kappa, coords, u, v, need=need)
+            ctx.unit_grads = grads
+            return J
 
         @staticmethod
         def backward(ctx, grad):
-            kappa, coords, u, v = ctx.saved_tensors
-            need = ctx.needs_input_grad[:4]
-            gk, gp, gu, gv = ctx.op.gradients(kappa, coords, u, v, need=need)
+            gk, gp, gu, gv = ctx.unit_grads
+            del ctx.unit_grads
             scale = lambda g: None if g is None else g * grad  # noqa: E731
             return scale(gk), scale(gp), scale(gu), scale(gv), None
 except ImportError:  # pragma: no cover

@@ -104,3 +104,30 @@ def test_shared_and_separate_incidence_walks_agree():
     g2 = op.gradients(kt, pt, ut, vt)
     for a, b in zip(g1, g2):
         assert torch.equal(a, b)
+
+
+def test_fused_value_and_gradients_match_separate_passes():
+    """The forward pass of the autograd function (J and unit-upstream gradients in one element pass) gives the
+    bits of the separate energy and gradient calls, for every subset of inputs that require a gradient."""
+    mesh, basis, kappa, u, v = problem(n=4, seed=6)
+    op = sk.P1Energy(basis)
+    base = [cuda(a) for a in (kappa, mesh.p, u, v)]
+    J0 = op.energy(*base)
+    g0 = op.gradients(*base)
+    J1, *g1 = op.energy_and_gradients(*base)
+    assert torch.equal(J0, J1)
+    for a, b in zip(g0, g1):
+        assert torch.equal(a, b)
+    for need in [(True, False, False, False), (False, True, False, False), (False, False, True, True),
+                 (True, True, True, True)]:
+        ins = [t.clone().requires_grad_(r) for t, r in zip(base, need)]
+        J = op(*ins)
+        assert torch.equal(J.detach(), J0)
+        (2.5 * J).backward()
+        for t, r, g in zip(ins, need, g0):
+            if r:
+                assert torch.equal(t.grad, g * 2.5)
+            else:
+                assert t.grad is None
+    with torch.no_grad():
+        assert torch.equal(op(*[t.clone().requires_grad_(True) for t in base]), J0)
