@@ -329,53 +329,72 @@ __device__ __forceinline__ bool elem_g_df64(int64_t ne, const double *__restrict
     b[3][2] = SKG_CROSS(0, 4, 1, 3);
 #undef SKG_CROSS
     df64 det = df_add_fast(df_add_fast(df_mul(J[0], b[1][0]), df_mul(J[1], b[2][0])), df_mul(J[2], b[3][0]));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) b[0][i] = df_neg(df_add_fast(df_add_fast(b[1][i], b[2][i]), b[3][i]));
     if (det.hi < 0.f) det = df_neg(det);
     ok = ok && det.hi > 1e-30f;
     df64 inv = df_recip(det);
     // exact-rule P2 path: G / 30 (the integer table carries 30 T)
     if (div30) inv = df_mul(inv, df64{0x1.111112p-5f, -0x1.dddddep-30f});
+    // as elem_g_fp64: dot products for the block k, l >= 1 only (upper triangle
+    // when symmetric), row and column 0 from b_0 = -(b_1 + b_2 + b_3)
+    bool sym = true;
     if (coef_kind == 0) {
         df64 sc = inv;
         if (coef) sc = df_mul(sc, df_from_double(coef[e], 0, ok));
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 1; k < 4; ++k)
 #pragma unroll
             for (int l = k; l < 4; ++l) {
                 df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], b[l][0]), df_mul(b[k][1], b[l][1])),
                                      df_mul(b[k][2], b[l][2]));
                 d = df_mul(sc, d);
-                ok = ok && df_in_range(d);
                 g[k * 4 + l] = d;
                 g[l * 4 + k] = d;
             }
-        return true;
-    }
-    double Ad[9];
+    } else {
+        double Ad[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Ad[k] = load_coef(coef, coef_kind, ne, e, k);
-    df64 A[9];
+        for (int k = 0; k < 9; ++k) Ad[k] = load_coef(coef, coef_kind, ne, e, k);
+        const double scale =
+            1e-14 * (fabs(Ad[0]) + fabs(Ad[4]) + fabs(Ad[8]) + fabs(Ad[1]) + fabs(Ad[2]) + fabs(Ad[5]));
+        sym = fabs(Ad[1] - Ad[3]) <= scale && fabs(Ad[2] - Ad[6]) <= scale && fabs(Ad[5] - Ad[7]) <= scale;
+        df64 A[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) A[k] = df_from_double(Ad[k], 0, ok);
+        for (int k = 0; k < 9; ++k) A[k] = df_mul(inv, df_from_double(Ad[k], 0, ok));
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-        df64 Ab[3];
+        for (int l = 1; l < 4; ++l) {
+            df64 Ab[3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-            Ab[i] = df_add_fast(df_add_fast(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
-                                df_mul(A[i * 3 + 2], b[l][2]));
+            for (int i = 0; i < 3; ++i)
+                Ab[i] = df_add_fast(df_add_fast(df_mul(A[i * 3], b[l][0]), df_mul(A[i * 3 + 1], b[l][1])),
+                                    df_mul(A[i * 3 + 2], b[l][2]));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            df64 d = df_add_fast(df_add_fast(df_mul(b[k][0], Ab[0]), df_mul(b[k][1], Ab[1])), df_mul(b[k][2], Ab[2]));
-            d = df_mul(inv, d);
-            ok = ok && df_in_range(d);
-            g[k * 4 + l] = d;
+            for (int k = 1; k < 4; ++k) {
+                if (k > l && sym) continue;  // mirrored below
+                g[k * 4 + l] =
+                    df_add_fast(df_add_fast(df_mul(b[k][0], Ab[0]), df_mul(b[k][1], Ab[1])), df_mul(b[k][2], Ab[2]));
+            }
+        }
+        if (sym) {
+#pragma unroll
+            for (int k = 2; k < 4; ++k)
+#pragma unroll
+                for (int l = 1; l < k; ++l) g[k * 4 + l] = g[l * 4 + k];
         }
     }
-    const double scale =
-        1e-14 * (fabs(Ad[0]) + fabs(Ad[4]) + fabs(Ad[8]) + fabs(Ad[1]) + fabs(Ad[2]) + fabs(Ad[5]));
-    return fabs(Ad[1] - Ad[3]) <= scale && fabs(Ad[2] - Ad[6]) <= scale && fabs(Ad[5] - Ad[7]) <= scale;
+#pragma unroll
+    for (int l = 1; l < 4; ++l) g[l] = df_neg(df_add_fast(df_add_fast(g[4 + l], g[8 + l]), g[12 + l]));
+    if (sym) {
+#pragma unroll
+        for (int k = 1; k < 4; ++k) g[k * 4] = g[k];
+    } else {
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+            g[k * 4] = df_neg(df_add_fast(df_add_fast(g[k * 4 + 1], g[k * 4 + 2]), g[k * 4 + 3]));
+    }
+    g[0] = df_neg(df_add_fast(df_add_fast(g[1], g[2]), g[3]));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) ok = ok && df_in_range(g[k]);
+    return sym;
 }
 
 __global__ void __launch_bounds__(kElemBlock, 6) k_elem_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
