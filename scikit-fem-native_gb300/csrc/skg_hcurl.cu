@@ -180,14 +180,25 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
         double J[9], b[4][3], det;
         n1_geometry(p, npts, t, ne, e, J, b, det);
         const double inv = 1.0 / fabs(det);
+        const double mu = inc_mass ? (mass ? mass[e] : 1.0) : 0.0;
+        const double nu = inc_curl ? (curl ? curl[e] : 1.0) * inv * tab.wsum : 0.0;
+        // mu b_k . b_l / |det J|: dot products for k, l >= 1, row 0 from
+        // b_0 = -(b_1 + b_2 + b_3); mu / |det J| scales the six products once
+        const double mi = mu * inv;
         double Gm[4][4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 1; k < 4; ++k)
 #pragma unroll
             for (int l = k; l < 4; ++l) {
-                Gm[k][l] = (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]) * inv;
+                Gm[k][l] = (b[k][0] * b[l][0] + b[k][1] * b[l][1] + b[k][2] * b[l][2]) * mi;
                 Gm[l][k] = Gm[k][l];
             }
+#pragma unroll
+        for (int l = 1; l < 4; ++l) {
+            Gm[0][l] = -(Gm[1][l] + Gm[2][l] + Gm[3][l]);
+            Gm[l][0] = Gm[0][l];
+        }
+        Gm[0][0] = -(Gm[0][1] + Gm[0][2] + Gm[0][3]);
         double Jc[6][3];
 #pragma unroll
         for (int a = 0; a < 6; ++a)
@@ -199,23 +210,23 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
                     if (ref_curl(a, r) != 0.0) v += J[i * 3 + r] * ref_curl(a, r);
                 Jc[a][i] = v;
             }
-        const double mu = inc_mass ? (mass ? mass[e] : 1.0) : 0.0;
-        const double nu = inc_curl ? (curl ? curl[e] : 1.0) * inv * tab.wsum : 0.0;
-        float sg[6];
+        // orientation signs (+1 / -1) applied as a sign-bit flip of the FP64 value
+        uint32_t neg[6];
 #pragma unroll
-        for (int a = 0; a < 6; ++a) sg[a] = (float)signs[a * ne + e];
+        for (int a = 0; a < 6; ++a) neg[a] = signs[a * ne + e] < 0 ? 1u : 0u;
         double *st = stage + threadIdx.x * 37;
 #pragma unroll
         for (int a = 0; a < 6; ++a)
 #pragma unroll
             for (int c = a; c < 6; ++c) {
-                double m = 0.0;
+                const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
+                double val = nu * cc;
 #pragma unroll
                 for (int u = 0; u < 2; ++u)
 #pragma unroll
-                    for (int v = 0; v < 2; ++v) m += Gm[edge_v(a, u)][edge_v(c, v)] * tab.Tm[a][c][u * 2 + v];
-                const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
-                const double val = (double)(sg[a] * sg[c]) * (mu * m + nu * cc);
+                    for (int v = 0; v < 2; ++v) val += Gm[edge_v(a, u)][edge_v(c, v)] * tab.Tm[a][c][u * 2 + v];
+                const unsigned long long flip = (unsigned long long)(neg[a] ^ neg[c]) << 63;
+                val = __longlong_as_double((long long)((unsigned long long)__double_as_longlong(val) ^ flip));
                 st[a * 6 + c] = val;
                 st[c * 6 + a] = val;
             }
