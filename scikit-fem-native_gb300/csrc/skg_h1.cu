@@ -66,7 +66,8 @@ __global__ void k_h1_local_tabulated(int64_t ne, int n, int C, int nq, const dou
 // test and trial basis coincide: K_(a,c),(b,d) = K_(b,d),(a,c) for the value,
 // gradient, symmetric-gradient and divergence terms alike.  So only the blocks
 // b >= a are summed over the points (in registers, two FMAs per entry and
-// point: sg a_d b_c + dv a_c b_d), each written with its transpose into the
+// point: sg a_d b_c + dv a_c b_d, one on c == d, the diagonal blocks from their
+// upper half), each written with its transpose into the
 // thread's element matrix in shared memory, and the block stores all matrices
 // coalesced.  The kernel is FP64-pipe bound; this halves its FP64
 // instructions against the full block loop.
@@ -86,13 +87,17 @@ __global__ void __launch_bounds__(BLK) k_h1_local_sym(int64_t ne, int nq, const 
     if (e < ne) {
 #pragma unroll
         for (int a = 0; a < NN; ++a) {
-            double acc[NN][CC][CC];
+            // acc: the sg / dv products (diagonal blocks: d >= c only); accd: the
+            // terms on c == d (value, gradient and the trace part of sg), per block
+            double acc[NN][CC][CC], accd[NN];
 #pragma unroll
-            for (int b = a; b < NN; ++b)
+            for (int b = a; b < NN; ++b) {
+                accd[b] = 0.0;
 #pragma unroll
                 for (int c = 0; c < CC; ++c)
 #pragma unroll
                     for (int d = 0; d < CC; ++d) acc[b][c][d] = 0.0;
+            }
             for (int q = 0; q < nq; ++q) {
                 const int64_t eq = e * nq + q;
                 const double wq = w[eq];
@@ -102,25 +107,30 @@ __global__ void __launch_bounds__(BLK) k_h1_local_sym(int64_t ne, int nq, const 
                 const double va = value ? value[eq] * wq * shape[eq * NN + a] : 0.0;
                 const double *gq = grad + eq * (NN * 3);
                 const double ag[3] = {gq[a * 3], gq[a * 3 + 1], gq[a * 3 + 2]};
-                double sa[CC], da[CC];
+                double sa[CC], da[CC], ta[CC];
 #pragma unroll
                 for (int c = 0; c < CC; ++c) {
                     sa[c] = sg * ag[c];
                     da[c] = dv * ag[c];
+                    ta[c] = sa[c] + da[c];
                 }
 #pragma unroll
                 for (int b = a; b < NN; ++b) {
                     const double bg[3] = {gq[b * 3], gq[b * 3 + 1], gq[b * 3 + 2]};
-                    double diag = dg * (ag[0] * bg[0] + ag[1] * bg[1] + ag[2] * bg[2]);
+                    double diag = accd[b] + dg * (ag[0] * bg[0] + ag[1] * bg[1] + ag[2] * bg[2]);
                     if (value) diag += va * shape[eq * NN + b];
+                    accd[b] = diag;
 #pragma unroll
                     for (int c = 0; c < CC; ++c)
 #pragma unroll
                         for (int d = 0; d < CC; ++d) {
-                            double v = acc[b][c][d] + sa[d] * bg[c];
-                            v += da[c] * bg[d];
-                            if (c == d) v += diag;
-                            acc[b][c][d] = v;
+                            if (b == a && d < c) continue;  // diagonal block: symmetric in (c, d)
+                            if (c == d) {
+                                acc[b][c][c] += ta[c] * bg[c];
+                            } else {
+                                double v = acc[b][c][d] + sa[d] * bg[c];
+                                acc[b][c][d] = v + da[c] * bg[d];
+                            }
                         }
                 }
             }
@@ -130,8 +140,10 @@ __global__ void __launch_bounds__(BLK) k_h1_local_sym(int64_t ne, int nq, const 
                 for (int c = 0; c < CC; ++c)
 #pragma unroll
                     for (int d = 0; d < CC; ++d) {
-                        st[(a * CC + c) * L + b * CC + d] = acc[b][c][d];
-                        if (b != a) st[(b * CC + d) * L + a * CC + c] = acc[b][c][d];
+                        if (b == a && d < c) continue;
+                        const double v = c == d ? acc[b][c][c] + accd[b] : acc[b][c][d];
+                        st[(a * CC + c) * L + b * CC + d] = v;
+                        if (b != a || c != d) st[(b * CC + d) * L + a * CC + c] = v;
                     }
         }
     }

@@ -83,3 +83,32 @@ def test_single_element_n1_maxwell():
     assert K.shape == (6, 6) and K.nnz == 36
     assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
     assert relerr(K.data, data) < 1e-12
+
+
+def test_fused_p1_forms_degenerate_meshes():
+    """The fused affine P1 forms path (per-element coefficients) on a single element, with an unused vertex
+    (compacted out of the DOF numbering) and as a P1 field on a P2 geometry mesh (affine: vertex rows only)."""
+    from skfemntv_gb300.assembly import NativeBilinearForm
+
+    kinds = dict(value=0.5, gradient=1.25, symmetric_gradient=2.0, divergence=10.0)
+    for comp in (1, 3):
+        # single element, and the same element with a far vertex no element uses (DOF numbering compacts it)
+        for p, t in ((P, T), (np.concatenate([np.array([[5.0], [5.0], [5.0]]), P], axis=1), T + 1)):
+            b = sk.Basis(sk.MeshTet(p, t), sk.ElementVector(sk.ElementTetP1(), dim=comp))
+            K = NativeBilinearForm(b).assemble(**kinds)
+            assert b._tab is None  # fused path
+            ob = O.make_basis(p, t, False, comp=comp)
+            data, indptr, indices = O.bilinear_assemble(ob, **kinds)
+            assert K.shape == (4 * comp, 4 * comp)
+            assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+            assert relerr(K.data, data) < 1e-12
+        # P1 field on the quadratic geometry mesh of a jittered cube: the map is affine, vertex rows are used
+        m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, 3),) * 3)
+        m2 = sk.MeshTet2.from_mesh(m)
+        b = sk.Basis(m2, sk.ElementVector(sk.ElementTetP1(), dim=comp))
+        assert b.is_affine
+        K = NativeBilinearForm(b).assemble(**kinds)
+        ob = O.make_basis(m2.p, m2.t, False, comp=comp)
+        data, indptr, indices = O.bilinear_assemble(ob, **kinds)
+        assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+        assert relerr(K.data, data) < 1e-12
