@@ -106,11 +106,12 @@ __device__ __forceinline__ void flush_stage(const float4 *stage, float4 *Gout, i
 // scaled barycentric gradients).  Only the block k, l >= 1 takes dot products
 // (its upper triangle when A is symmetric): b_0 = -(b_1 + b_2 + b_3) gives
 // G_0l = -(G_1l + G_2l + G_3l), G_k0 likewise and G_00 = -(G_01 + G_02 + G_03),
-// and 1 / |det J| scales the coefficient, not the 16 results.  Returns the
+// and gscale / |det J| scales the coefficient, not the 16 results.  Returns the
 // element's symmetry (scalar coefficient, or a tensor equal to its transpose).
 __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                             const int32_t *__restrict__ t, int coef_kind,
-                                            const double *__restrict__ coef, int64_t e, double g[16]) {
+                                            const double *__restrict__ coef, int64_t e, double g[16],
+                                            double gscale = 1.0) {
     int32_t v[4];
     const bool ok = load_vertices(t, ne, e, npts, v);
     double J[9];
@@ -131,7 +132,7 @@ __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict
     b[3][1] = J[1] * J[6] - J[0] * J[7];
     b[3][2] = J[0] * J[4] - J[1] * J[3];
     const double det = J[0] * b[1][0] + J[1] * b[2][0] + J[2] * b[3][0];
-    const double inv = ok ? 1.0 / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
+    const double inv = ok ? gscale / fabs(det) : __longlong_as_double(0x7ff8000000000000LL);
     bool sym = true;
     if (coef_kind == 0) {
         const double sc = (coef ? coef[e] : 1.0) * inv;
@@ -763,6 +764,73 @@ __device__ __forceinline__ df64 exact_entry(const df64 g[16]) {
     return fast_two_sum(S, L);
 }
 
+// FP64 entry K_ab = sum t30 G (G carrying the 1/30) with compile-time integer
+// factors: -1 terms become additions, a vertex-edge entry one FMA.
+template <int A, int BB>
+__device__ __forceinline__ double exact_entry_fp64(const double g[16]) {
+    constexpr int ka0 = sup_lo(A), ka1 = sup_hi(A), kb0 = sup_lo(BB), kb1 = sup_hi(BB);
+    constexpr double t00 = t30(A, BB, 0, 0), t01 = t30(A, BB, 0, 1), t10 = t30(A, BB, 1, 0), t11 = t30(A, BB, 1, 1);
+    double v = t00 * g[ka0 * 4 + kb0];
+    if constexpr (kb1 != kb0) v += t01 * g[ka0 * 4 + kb1];
+    if constexpr (ka1 != ka0) {
+        v += t10 * g[ka1 * 4 + kb0];
+        if constexpr (kb1 != kb0) v += t11 * g[ka1 * 4 + kb1];
+    }
+    return v;
+}
+
+// k_elem_ke_fp64 for a rule exact on quadratics (the 4-point and the 11-point
+// Keast rule): the entries from the integer table with compile-time factors
+// (about 30 FP64 instructions per element fewer than the table read from
+// shared memory); same staging and coalesced stores.
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64_exact(int64_t ne, int64_t e_begin, int64_t e_end,
+                                                                 const double *__restrict__ p, int64_t npts,
+                                                                 const int32_t *__restrict__ t, int coef_kind,
+                                                                 const double *__restrict__ coef,
+                                                                 double *__restrict__ Ke) {
+    __shared__ double stage[kKeBlock * kKeChunk];
+    const int64_t e0 = e_begin + (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    double g[16];
+    bool sym = true;
+    if (e < e_end) {
+        sym = elem_g_fp64(ne, p, npts, t, coef_kind, coef, e, g, 1.0 / 30.0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = 0.0;
+    }
+    double U[55];
+    if (sym) {
+        static_for<0, 100>([&](auto kk) {
+            constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+            if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry_fp64<A, BB>(g);
+        });
+    }
+    const int nvalid = (int)(e_end - e0 < kKeBlock ? e_end - e0 : kKeBlock);
+    double *st = stage + threadIdx.x * kKeChunk;
+    static_for<0, 100 / kKeChunk>([&](auto rr) {
+        constexpr int r = decltype(rr)::value;
+        if (sym) {
+            static_for<0, kKeChunk>([&](auto qq) {
+                constexpr int q = decltype(qq)::value, k = r * kKeChunk + q, A = k / 10, BB = k % 10;
+                st[q] = U[A <= BB ? tri10(A, BB) : tri10(BB, A)];
+            });
+        } else {
+            static_for<0, kKeChunk>([&](auto qq) {
+                constexpr int q = decltype(qq)::value, k = r * kKeChunk + q, A = k / 10, BB = k % 10;
+                st[q] = exact_entry_fp64<A, BB>(g);
+            });
+        }
+        __syncthreads();
+        // coalesced copy-out: element rows are 100 doubles apart
+        for (int i = threadIdx.x; i < nvalid * kKeChunk; i += kKeBlock) {
+            const int el = i / kKeChunk, q = i - el * kKeChunk;
+            Ke[(e0 + el) * 100 + r * kKeChunk + q] = stage[el * kKeChunk + q];
+        }
+        __syncthreads();
+    });
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                                            const int32_t *__restrict__ t, int coef_kind,
@@ -1089,13 +1157,18 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     if (mode == MODE_FP64 && nodes == 10 && blocked) {
         // FP64 P2: element matrices, then row sums
         // (with a host output the two passes interleave, see run_passes)
+        const bool exact_fp64 = p2_rule_is_exact(T);
         DevBuf<double> Ke((size_t)ne * 100, s);
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
         run_passes(
             pat, ne, d_values, h_values, s,
             [&](int64_t e0, int64_t e1) {
-                k_elem_ke_fp64<<<grid_for(e1 - e0, kKeBlock), kKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t, coef_kind,
-                                                                             d_coef, Tg, Ke.get());
+                if (exact_fp64)
+                    k_elem_ke_fp64_exact<<<grid_for(e1 - e0, kKeBlock), kKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t,
+                                                                                       coef_kind, d_coef, Ke.get());
+                else
+                    k_elem_ke_fp64<<<grid_for(e1 - e0, kKeBlock), kKeBlock, 0, s>>>(ne, e0, e1, d_p, npts, d_t,
+                                                                                 coef_kind, d_coef, Tg, Ke.get());
                 SKG_LAUNCH_CHECK("elem_ke_fp64");
                 if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
             },

@@ -578,3 +578,25 @@ def test_fused_p1_forms_chunked_host_output():
     tab = form.assemble_device(**pts).cpu().numpy()[: form.pattern.nnz]
     assert b._tab is not None
     assert relerr(tab, dv) < RTOL
+
+
+@pytest.mark.parametrize("rule", ["one_point", "vertices"])
+def test_p2_anisotropic_fused_rule_not_exact_on_quadratics(rule):
+    """P2 anisotropic diffusion through the fused FP64 path with a rule that does not integrate quadratics
+    exactly: the element pass reads the rule's table (the exact-rule kernel with integer factors is not
+    eligible), symmetric and nonsymmetric A, against the oracle on the reference's algorithm."""
+    g = load_golden("p2_aniso")
+    if rule == "one_point":
+        X, W = X1, W1
+    else:  # the four vertices with weight 1/24: exact on linears only
+        X, W = np.array([[0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]]), np.full(4, 1.0 / 24.0)
+    b = p2_basis(g, (X, W))
+    assert b.is_affine
+    E, Q = b._coefficient_shape
+    ob = O.make_basis(g["p"], g["t"], True, quadrature=(X, W))
+    for key in ("A", "Ans"):
+        Apub = np.broadcast_to(np.moveaxis(g[key], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+        K = sk.asm(aniso, b, A=Apub)
+        d, indptr, indices = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(Apub, (E, Q)))
+        assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+        assert relerr(K.data, d) < RTOL
