@@ -4,7 +4,8 @@
 // One warp per row group (<= 32 / P consecutive CSR rows whose slots, times
 // P accumulator copies, fit SLOTS in shared memory); thread part p of row r
 // walks the row's incidence records p, p + P, ... (ascending element order),
-// loads row a of K_e (N doubles, the next record's row one step ahead) and
+// loads row a of K_e (N doubles, the next record's row one step ahead, the
+// records themselves two steps ahead) and
 // adds it into its accumulator copy at the record's column offsets; the
 // warp sums the copies in copy order and writes the group's slot range with
 // coalesced stores.  No atomics: bitwise reproducible.  Optionally the same
@@ -49,7 +50,9 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
         const int32_t it1 = inc_ptr[r + 1];
         int32_t it = inc_ptr[r] + part;
         if (it < it1) {
+            // records run two incidences ahead of the rows they address, rows one
             int4 rc = rec[it];
+            int4 rcn = it + P < it1 ? rec[it + P] : make_int4(0, 0, 0, 0);
             double2 cur[N / 2];
             {
                 const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rc.x * N);
@@ -58,14 +61,13 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
             }
             for (; it < it1; it += P) {
                 const bool has_next = it + P < it1;
-                int4 rcn = make_int4(0, 0, 0, 0);
                 double2 nxt[N / 2];
                 if (has_next) {
-                    rcn = rec[it + P];
                     const double2 *src = reinterpret_cast<const double2 *>(Ke + (int64_t)rcn.x * N);
 #pragma unroll
                     for (int q = 0; q < N / 2; ++q) nxt[q] = __ldg(src + q);
                 }
+                const int4 rcnn = it + 2 * P < it1 ? rec[it + 2 * P] : make_int4(0, 0, 0, 0);
                 if (re) rsum += __ldg(re + rc.x);
                 const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
                 int off[N];
@@ -81,6 +83,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
                 }
                 if (has_next) {
                     rc = rcn;
+                    rcn = rcnn;
 #pragma unroll
                     for (int q = 0; q < N / 2; ++q) cur[q] = nxt[q];
                 }
