@@ -910,7 +910,9 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
         const int32_t it1 = inc_ptr[r + 1];
         int32_t it = inc_ptr[r] + part;
         if (it < it1) {
+            // records two incidences ahead of the rows they address, rows one
             int4 rc = rec[it];
+            int4 rcn = it + P < it1 ? rec[it + P] : make_int4(0, 0, 0, 0);
             float4 cur[5];
             {
                 const float4 *src = reinterpret_cast<const float4 *>(Ke + (int64_t)rc.x * 10);
@@ -919,14 +921,13 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
             }
             for (; it < it1; it += P) {
                 const bool has_next = it + P < it1;
-                int4 rcn = make_int4(0, 0, 0, 0);
                 float4 nxt[5];
                 if (has_next) {
-                    rcn = rec[it + P];
                     const float4 *src = reinterpret_cast<const float4 *>(Ke + (int64_t)rcn.x * 10);
 #pragma unroll
                     for (int q = 0; q < 5; ++q) nxt[q] = __ldg(src + q);
                 }
+                const int4 rcnn = it + 2 * P < it1 ? rec[it + 2 * P] : make_int4(0, 0, 0, 0);
                 const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
                 int off[10];
 #pragma unroll
@@ -943,6 +944,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
                 for (int bb = 0; bb < 10; ++bb) acc[off[bb]] = a[bb];
                 if (has_next) {
                     rc = rcn;
+                    rcn = rcnn;
 #pragma unroll
                     for (int q = 0; q < 5; ++q) cur[q] = nxt[q];
                 }

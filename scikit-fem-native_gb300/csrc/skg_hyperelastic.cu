@@ -235,8 +235,11 @@ __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
     if (live) {
         const int base = indptr[r] - s0 + part * nslots;
         const int32_t it1 = inc_ptr[r + 1];
-        for (int32_t it = inc_ptr[r] + part; it < it1; it += P) {
-            const int4 rc = rec_inc[it];
+        int32_t it = inc_ptr[r] + part;
+        int4 rcn = it < it1 ? rec_inc[it] : make_int4(0, 0, 0, 0);  // records one incidence ahead
+        for (; it < it1; it += P) {
+            const int4 rc = rcn;
+            if (it + P < it1) rcn = rec_inc[it + P];
             const int32_t e = rc.x / 12;
             const int l = rc.x - e * 12;
             const int a = l / 3, i = l - 3 * (l / 3);
