@@ -33,6 +33,24 @@ def test_library_exports_every_declared_symbol():
     assert lib.skg_version() >= 100
 
 
+def header_parameter_counts():
+    """Number of parameters of every function the header declares (comments stripped)."""
+    text = open(os.path.join(ROOT, "include", "skfem_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"^(?:int|const char \*)\s*(skg_\w+)\(([^)]*)\);", text, re.M):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_ctypes_signatures_match_header_parameter_counts():
+    counts = header_parameter_counts()
+    assert set(counts) == set(header_symbols())
+    for name, n in counts.items():
+        assert len(_native.SIGNATURES[name]) == n, (name, len(_native.SIGNATURES[name]), n)
+
+
 def test_nvcc_targets_sm103a_only():
     import build_native
 
