@@ -221,3 +221,25 @@ def test_bench_reference_arm_prints_the_contract_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_coefficient_classification_routes_fused_and_tabulated_paths():
+    """per_element decides between the fused per-element kernels and the tabulated per-point ones: a scalar
+    stays 0-d, a coefficient constant over each element's points becomes (E,), one that varies gives None;
+    shapes that do not broadcast to (E, Q) raise ValueError as the reference does."""
+    from skfemntv_gb300.assembly import per_element, per_point
+
+    E, Q = 5, 4
+    assert np.ndim(per_element(2.5, E, Q, "value")) == 0
+    c = np.arange(E, dtype=float)
+    for form in (c[:, None], np.broadcast_to(c[:, None], (E, Q)), np.repeat(c[:, None], Q, axis=1)):
+        got = per_element(form, E, Q, "value")
+        assert got.shape == (E,) and np.array_equal(got, c)
+    varying = np.arange(E * Q, dtype=float).reshape(E, Q)
+    assert per_element(varying, E, Q, "value") is None
+    assert per_point(varying, E, Q, "value").shape == (E, Q)
+    assert per_point(1.0, E, Q, "value").shape == (E, Q)
+    with pytest.raises(ValueError):
+        per_element(np.ones((E + 1, Q)), E, Q, "value")
+    with pytest.raises(ValueError):
+        per_point(np.ones((E, Q + 1)), E, Q, "value")
