@@ -25,3 +25,11 @@ def load_golden(name):
 @pytest.fixture
 def golden():
     return load_golden
+
+
+@pytest.fixture(scope="session")
+def surrogate():
+    """The learned neo-Hookean closure trained by the default recipe (2M samples,
+    3000 Adam steps, L-BFGS on 524,288 samples); trained once per test session."""
+    sk = pytest.importorskip("skfemntv_gb300")
+    return sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)

@@ -28,12 +28,6 @@ def test_plain_law_matches_reference():
     assert relerr(K.data, g["data"]) < 1e-12
 
 
-@pytest.fixture(scope="module")
-def surrogate():
-    # the default recipe: 2M samples, 3000 Adam steps, L-BFGS on 524,288 samples
-    return sk.EnergySurrogate.train(mu=1.0, lmbda=10.0, sigma=0.1, seed=1)
-
-
 def test_network_derivatives_match_cpu_oracle(surrogate):
     rng = np.random.default_rng(3)
     x = rng.standard_normal((257, 3)).astype(np.float32)
