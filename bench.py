@@ -148,8 +148,10 @@ class ClockSampler:
 # ----------------------------------------------------------------- CPU side
 
 class OracleSample:
-    """The workload at n^3 x 6 on the CPU oracle (threaded colored assembly,
-    the reference's multi-thread scheme); set up once, one assembly per step."""
+    """The workload at n^3 x 6 on the CPU oracle (the reference's assembly
+    algorithm: per-point contributions summed into the CSR slots, threaded by
+    element coloring as bilinear_form_assembler.cpp:62-70 does); set up once,
+    one assembly per step."""
 
     def __init__(self, n, threads):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -168,13 +170,17 @@ class OracleSample:
                                       (E, Q))
         dofs = self.basis.dofs3.reshape(E, -1)
         self.pattern = O.Pattern(dofs, dofs)
-        self.nnz, self.E = self.pattern.nnz, E
-        self.desc = (f"P2 anisotropic {n}^3x6 jittered cube ({E} tets, nnz {self.nnz}), "
-                     f"threaded colored assembly on {threads} threads")
+        self.nnz, self.E, self.n = self.pattern.nnz, E, n
+        self.values = None
 
-    def step(self):
+    def desc(self, threads):
+        return (f"P2 anisotropic {self.n}^3x6 jittered cube ({self.E} tets, nnz {self.nnz}), "
+                f"colored assembly on {threads} thread{'s' if threads > 1 else ''}")
+
+    def step(self, threads=None):
         t0 = time.perf_counter()
-        self.O.cross_gradient_tensor_assemble(self.basis, self.T, threads=self.threads, pattern=self.pattern)
+        self.values, _, _ = self.O.cross_gradient_tensor_assemble(self.basis, self.T, threads=threads or self.threads,
+                                                                  pattern=self.pattern)
         return time.perf_counter() - t0
 
 
@@ -185,7 +191,18 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-REFERENCE_SAMPLE_CELLS = 32
+def cpu_baseline_of(sample, reps):
+    """All host cores over `reps` timed assemblies (after one warm-up), and one
+    timed single-thread assembly (the reference's default thread count,
+    cpp/src/runtime.cpp:10)."""
+    sample.step()
+    times = [sample.step() for _ in range(reps)]
+    t_one = sample.step(threads=1)
+    return {"value": sample.nnz * len(times) / sum(times), "unit": UNIT, "cores": sample.threads, "kind": "port",
+            "sample": sample.desc(sample.threads) + f", {reps} timed assemblies",
+            "same_config": sample.n == N_CELLS,
+            "one_thread": {"value": sample.nnz / t_one, "unit": UNIT, "cores": 1, "seconds": t_one,
+                           "sample": sample.desc(1) + ", 1 timed assembly"}}
 
 
 def run_reference(args, rank):
@@ -201,18 +218,25 @@ def run_reference(args, rank):
                 "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
-    sample = OracleSample(REFERENCE_SAMPLE_CELLS, threads)
+    # the full workload (same mesh, tensors and rule as the GPU arm), every
+    # step one complete assembly on all host cores
+    sample = OracleSample(args.cells, threads)
     for _ in range(args.warmup):
         sample.step()
     times = [sample.step() for _ in range(args.steps)]
+    t_one = sample.step(threads=1)
     elapsed = sum(times)
     value = sample.nnz * args.steps / elapsed
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(CONFIG, sample=sample.desc),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample.desc},
+        "config": dict(CONFIG, sample=sample.desc(threads), cells=args.cells),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample.desc(threads) + f", {args.steps} timed assemblies",
+                         "same_config": args.cells == N_CELLS,
+                         "one_thread": {"value": sample.nnz / t_one, "unit": UNIT, "cores": 1, "seconds": t_one,
+                                        "sample": sample.desc(1) + ", 1 timed assembly"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -240,11 +264,20 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-# FP64 instructions per element of the FP64 passes (DFMA + DMUL + DADD thread
-# instructions counted by ncu on the 32^3 case, profiles/fp64_ops_p2_aniso_32.md).
-FP64_OPS_PER_ELEMENT = {"k_elem_ke_fp64_exact": 221.0, "k_rows_ke": 111.1}
-# The same for the plain neo-Hookean call (profiles/fp64_ops_nh_32.md):
-# element matrices k_nh_ke + row pass k_rows_ke<12>.
+# Counters behind the FP64 roofline, kept as data (measured, not recomputed
+# here): FP64 thread instructions (DFMA + DMUL + DADD, ncu
+# smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum of one
+# launch divided by the elements) and DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch at 48^3, scaled to 64^3 by the element
+# count) of each FP64 pass of the headline workload.
+FP64_PROFILE = {
+    "source": "ncu --metrics ... --clock-control none on python bench.py --cells 32 (instructions) / --cells 48 "
+              "(DRAM) --steps 2 --warmup 3 --no-cpu-baseline --modes fp64, GB300",
+    "commit": "3b1e0c4",
+    "ops_per_element": {"k_elem_ke_fp64_exact": 221.0, "k_rows_ke": 95.3},
+    "dram_bytes_64": {"k_elem_ke_fp64_exact": 1261945000.0, "k_rows_ke": 2217479000.0},
+}
+# The plain neo-Hookean call: element matrices k_nh_ke + row pass k_rows_ke<12>.
 NH_FP64_OPS_PER_ELEMENT = 535.1 + 180.0
 
 
@@ -256,26 +289,22 @@ def fp64_roof(call, passes, elements):
     rate = ctypes.c_double()
     call("skg_fp64_fma_rate", ctypes.byref(rate), None)
     out = {"peak_gops": rate.value, "peak_source": "skg_fp64_fma_rate: independent FMA chains, measured in this run",
-           "passes": {}}
+           "counts": {k: FP64_PROFILE[k] for k in ("source", "commit")}, "passes": {}}
     for name, _, _, ms in passes:
-        ops = FP64_OPS_PER_ELEMENT.get(name)
-        if ops is None:
+        ops = FP64_PROFILE["ops_per_element"].get(name)
+        if ops is None or ms <= 0:
             continue
         achieved = ops * elements / (ms * 1e-3) / 1e9
         out["passes"][name] = {"ops_per_element": ops, "achieved_gops": achieved, "frac": achieved / rate.value}
     return out
 
 
-def profiled_traffic(key):
-    """DRAM bytes of one FP64 pass at 64^3 (element or row pass) from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_affine_fp64_p2_aniso_48.md")
-    try:
-        for ln in open(path):
-            if ln.startswith(f"dram_bytes_per_{key}_pass_full:"):
-                return float(ln.split(":")[1])
-    except OSError:
-        pass
-    return None
+def oracle_errors(sample, mode_values):
+    """Largest error of each precision mode's values relative to the largest
+    oracle entry, on the full workload (the oracle assembled it last)."""
+    ref = sample.values
+    scale = float(np.max(np.abs(ref)))
+    return {m: float(np.max(np.abs(v - ref)) / scale) for m, v in mode_values.items()}
 
 
 def run_gpu(args, rank, world):
@@ -331,7 +360,7 @@ def run_gpu(args, rank, world):
         k_el, k_rows = [], []
         for _ in range(args.steps):
             call("skg_h1_assemble_affine_profiled", form.pattern.h, dev.ptr(m2._dev("p")), m2.p.shape[1],
-                 dev.ptr(m2._dev("t")), 10, E, dev.ptr(basis._dev_dofs()), Q, dev.hptr(basis.X), dev.hptr(basis.W),
+                 dev.ptr(m2._dev("t")), 10, E, Q, dev.hptr(basis.X), dev.hptr(basis.W),
                  2, dev.ptr(dA), prec[mode], dev.ptr(form.target.d_values), kms, dev.stream_ptr())
             k_el.append(kms[0])
             k_rows.append(kms[1])
@@ -339,9 +368,11 @@ def run_gpu(args, rank, world):
 
     results = {}
     reference_values = None
+    mode_values = {}  # host copies for the comparison with the oracle
     for mode in args.modes:
         ms, t_el, t_rows, clk = time_mode(mode)
         vals = form.target.d_values[:nnz].clone()
+        mode_values[mode] = vals.cpu().numpy()
         if reference_values is None:
             reference_values = vals
             err = 0.0
@@ -369,15 +400,20 @@ def run_gpu(args, rank, world):
     # ---- roofline of the dominant kernel (headline mode)
     peak, peak_kind = measured_peak()
     npts_vertex = (args.cells + 1) ** 3
-    bytes_elem = 24 * npts_vertex + 16 * E + 72 * E     # vertex coords + 4 vertex ids + A
-    bytes_rows = 40 * E + 8 * nnz                       # 10 dof ids per element + CSR values
+    # compulsory bytes, each counted once: vertex coordinates, 10 int32 DOF
+    # ids per element (4 vertex ids read by the element pass, 6 edge ids
+    # charged to the row pass), A (9 float64 per element), the CSR values
+    bytes_elem = 24 * npts_vertex + 16 * E + 72 * E
+    bytes_rows = 24 * E + 8 * nnz
     head_mode = args.modes[0]
     # the workload's 4-point rule integrates quadratics exactly: the integer-factor element kernel runs
-    names = (("k_elem_ke_fp64_exact", "k_rows_ke") if head_mode == "fp64" else ("k_elem_df64", "k_rows_group"))
-    passes = [(names[0], "element", bytes_elem, t_el), (names[1], "row", bytes_rows, t_rows)]
+    names = {"fp64": ("k_elem_ke_fp64_exact", "k_rows_ke"), "fp64_emulated": ("k_elem_ke_df64", "k_rows_ke_df"),
+             "split_fp32": ("k_elem_df64", "k_rows_group")}[head_mode]
+    passes = [q for q in [(names[0], "element", bytes_elem, t_el), (names[1], "row", bytes_rows, t_rows)] if q[3] > 0]
     dominant = max(passes, key=lambda q: q[3])
     achieved = dominant[2] / (dominant[3] * 1e-3) / 1e9
-    traffic = (profiled_traffic(dominant[1]) if head_mode == "fp64" and args.cells == N_CELLS else None)
+    traffic = (FP64_PROFILE["dram_bytes_64"].get(dominant[0])
+               if head_mode == "fp64" and args.cells == N_CELLS else None)
 
     config = dict(CONFIG, cells=args.cells, parallelism=f"replicas x{world}" if world > 1 else "single GPU")
     if args.cells != N_CELLS:
@@ -393,10 +429,11 @@ def run_gpu(args, rank, world):
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes_per_launch": dominant[2],
-                     "limiter": ("FP64 pipe (ncu: 80% active in the element pass, 51-54% in the row pass)"
-                                 if head_mode == "fp64" else "CUDA-core issue / shared-memory latency"),
+                     "limiter": ("FP64 pipe in the element pass; load latency and the FP64 pipe in the row pass"
+                                 if head_mode == "fp64" else "load latency of the row pass"),
                      "passes": {q[0]: {"ms": q[3], "algorithmic_bytes": q[2],
                                        "achieved_gbs": q[2] / (q[3] * 1e-3) / 1e9} for q in passes},
+                     "whole_assembly_bytes": bytes_elem + bytes_rows,
                      "whole_assembly_hbm_frac": (bytes_elem + bytes_rows) / ((t_el + t_rows) * 1e-3) / 1e9 / peak,
                      "fp64_pipe": fp64_roof(call, passes, E) if head_mode == "fp64" else None},
         "precision_variants": results,
@@ -404,13 +441,11 @@ def run_gpu(args, rank, world):
         "clocks": head["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
-        sample = OracleSample(REFERENCE_SAMPLE_CELLS, host_threads())
-        sample.step()
-        times = [sample.step() for _ in range(3)]
-        line["cpu_baseline"] = {
-            "value": sample.nnz * len(times) / sum(times), "unit": UNIT, "cores": sample.threads, "kind": "port",
-            "sample": sample.desc + ", 3 timed assemblies",
-        }
+        sample = OracleSample(args.cells, host_threads())
+        line["cpu_baseline"] = cpu_baseline_of(sample, 3)
+        sample.step()  # all cores, leaves the oracle's values for the comparison
+        for mode, err in oracle_errors(sample, mode_values).items():
+            results[mode]["max_rel_err_vs_oracle"] = err
     if rank == 0:
         print(json.dumps(line), flush=True)
 

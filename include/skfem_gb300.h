@@ -126,6 +126,18 @@ int skg_tabulate_geometry(const double *d_p, int64_t npts, const int32_t *d_t,
                           double *d_x, double *d_det, double *d_tol,
                           double *d_cond, int64_t *h_bad, void *stream);
 
+/* Geometry diagnostics of a tabulated basis in one device reduction:    */
+/* replaces the host-side reductions of Basis._update_geometry_diagnostics */
+/* (python/skfemntv/basis.py:2296-2356) over det, tol, cond (E,Q).      */
+/* h_values = {min det, max det, min |det| / (tol / (64 eps)), max cond} */
+/* h_indices = {flat index of that smallest scaled determinant, flat     */
+/* index of the largest condition number (first occurrence each, as      */
+/* numpy's argmin / argmax), elements whose first point has det < 0}.    */
+/* Requires E, Q > 0.  Synchronous.                                      */
+int skg_geometry_diagnostics(const double *d_det, const double *d_tol, const double *d_cond,
+                             int64_t n_elements, int32_t nq, double *h_values,
+                             int64_t *h_indices, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Nodal H1 bilinear assembly from tabulated geometry.                  */
 /* Replaces BilinearFormAssembler.assemble                              */
@@ -182,8 +194,8 @@ int skg_cross_assemble_tabulated(const skg_pattern *pattern, int64_t n_elements,
 /* geometry, element contraction and the fixed-order CSR sum in one     */
 /* pass, without tabulated per-point arrays.                            */
 /*  d_p (3, npts); d_t (nodes, E) with nodes 4 (P1) or 10 (P2, the      */
-/*  mesh must be affine: edge nodes at midpoints); d_dofs (E, nodes)    */
-/*  scalar DOFs.  h_X (3,Q), h_W (Q): the quadrature rule.              */
+/*  mesh must be affine: edge nodes at midpoints).  The scalar DOFs are  */
+/*  the pattern's (skg_pattern_create).  h_X (3,Q), h_W (Q): the rule.   */
 /*  coef_kind 0: d_coef per element (E) or NULL for 1.                   */
 /*  coef_kind 1: d_coef per element (E,3,3), row-major A[i][j].          */
 /*  coef_kind 2: d_coef per element, component-first (3,3,E) (the        */
@@ -194,21 +206,20 @@ int skg_cross_assemble_tabulated(const skg_pattern *pattern, int64_t n_elements,
 /*  d_values (nnz) is overwritten.                                       */
 int skg_h1_assemble_affine(const skg_pattern *pattern, const double *d_p,
                            int64_t npts, const int32_t *d_t, int32_t nodes,
-                           int64_t n_elements, const int32_t *d_dofs,
-                           int32_t nq, const double *h_X, const double *h_W,
-                           int32_t coef_kind, const double *d_coef,
-                           int32_t precision, double *d_values, void *stream);
+                           int64_t n_elements, int32_t nq, const double *h_X,
+                           const double *h_W, int32_t coef_kind,
+                           const double *d_coef, int32_t precision,
+                           double *d_values, void *stream);
 
 /* Same as skg_h1_assemble_affine, and writes the duration of its two
  * kernels (element pass, row pass) in milliseconds to h_kernel_ms[0..1],
  * measured with CUDA events on `stream`.  Synchronous. */
 int skg_h1_assemble_affine_profiled(const skg_pattern *pattern, const double *d_p,
                                     int64_t npts, const int32_t *d_t, int32_t nodes,
-                                    int64_t n_elements, const int32_t *d_dofs,
-                                    int32_t nq, const double *h_X, const double *h_W,
-                                    int32_t coef_kind, const double *d_coef,
-                                    int32_t precision, double *d_values,
-                                    float *h_kernel_ms, void *stream);
+                                    int64_t n_elements, int32_t nq, const double *h_X,
+                                    const double *h_W, int32_t coef_kind,
+                                    const double *d_coef, int32_t precision,
+                                    double *d_values, float *h_kernel_ms, void *stream);
 /* As skg_h1_assemble_affine, the values also delivered to page-locked host
  * memory h_values (nnz): the row pass runs in row chunks and each chunk's
  * values are copied while the next chunk is assembled (d_values is the
@@ -216,8 +227,8 @@ int skg_h1_assemble_affine_profiled(const skg_pattern *pattern, const double *d_
  * stream is.  No counterpart in the reference (host-only). */
 int skg_h1_assemble_affine_host(const skg_pattern *pattern, const double *d_p,
                                 int64_t npts, const int32_t *d_t, int32_t nodes,
-                                int64_t n_elements, const int32_t *d_dofs, int32_t nq,
-                                const double *h_X, const double *h_W, int32_t coef_kind,
+                                int64_t n_elements, int32_t nq, const double *h_X,
+                                const double *h_W, int32_t coef_kind,
                                 const double *d_coef, int32_t precision, double *d_values,
                                 double *h_values, void *stream);
 
@@ -226,16 +237,25 @@ int skg_h1_assemble_affine_host(const skg_pattern *pattern, const double *d_p,
  * memory: applications that give all device memory to their own pool
  * allocator and forbid other allocations, and solvers that re-assemble
  * inside a time-stepping loop where cudaMalloc / cudaFree (which may
- * synchronise the device) is not allowed.  Same arguments and results as
- * skg_h1_assemble_affine; it calls no cudaMalloc, cudaFree or allocating
- * library routine.  Its scratch is a fixed static device array of the
- * library (32 MiB plus a small table), held on every GPU that loads the
- * library until the process exits; meshes of more than
- * SKG_NOALLOC_MAX_ELEMENTS elements are rejected with SKG_EINVAL.  The first
- * call on a device looks up the array's device address on that device (so
- * make that first call before any stream capture).  All calls share the
- * array: calls that overlap on the GPU (on different streams, or from
- * different host threads) race and must be serialised by the caller. */
+ * synchronise the device) is not allowed.  Same arguments as
+ * skg_h1_assemble_affine and the same results to rounding (P1, and P2 in
+ * FP64 or double-float, sum rows evaluated from per-element G instead of
+ * stored element matrices: same mathematics, slower at scale); it calls no
+ * cudaMalloc, cudaFree or allocating library routine.  Its scratch is a
+ * fixed static device array of the library (32 MiB plus a small table),
+ * held on every GPU that loads the library until the process exits;
+ * meshes of more than SKG_NOALLOC_MAX_ELEMENTS elements are rejected with
+ * SKG_EINVAL.  The first call on a device looks up the array's device
+ * address on that device and keeps it for the life of the process (so make
+ * that first call before any stream capture; after cudaDeviceReset the
+ * kept address is stale and the process must not call this again).  Each
+ * call copies the quadrature table from host memory into the array.  In
+ * SKG_FP64_EMULATED and SKG_SPLIT_FP32 it synchronises the host with
+ * `stream` once per call, to read the range flag that decides between the
+ * FP32-pair kernels and SKG_FP64; SKG_FP64 does not synchronise.  All calls
+ * share the array and each call overwrites what the last one left there:
+ * calls that overlap on the GPU (on different streams, or from different
+ * host threads) race and must be serialised by the caller. */
 #define SKG_NOALLOC_MAX_ELEMENTS 262144
 int skg_h1_assemble_affine_noalloc(const skg_pattern *pattern, const double *d_p,
                                    int64_t npts, const int32_t *d_t, int32_t nodes,

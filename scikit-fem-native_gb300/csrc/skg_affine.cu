@@ -919,6 +919,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
 #pragma unroll
                 for (int q = 0; q < 5; ++q) cur[q] = __ldg(src + q);
             }
+            bool first = true;
             for (; it < it1; it += P) {
                 const bool has_next = it + P < it1;
                 float4 nxt[5];
@@ -932,16 +933,25 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_df(int n_groups, con
                 int off[10];
 #pragma unroll
                 for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                df64 a[10];
+                if (first) {  // the part's first incidence: its row initialises the slots
 #pragma unroll
-                for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
+                    for (int q = 0; q < 5; ++q) {
+                        acc[off[2 * q]] = df64{cur[q].x, cur[q].y};
+                        acc[off[2 * q + 1]] = df64{cur[q].z, cur[q].w};
+                    }
+                    first = false;
+                } else {
+                    df64 a[10];
 #pragma unroll
-                for (int q = 0; q < 5; ++q) {
-                    df_acc(a[2 * q], df64{cur[q].x, cur[q].y});
-                    df_acc(a[2 * q + 1], df64{cur[q].z, cur[q].w});
+                    for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) {
+                        df_acc(a[2 * q], df64{cur[q].x, cur[q].y});
+                        df_acc(a[2 * q + 1], df64{cur[q].z, cur[q].w});
+                    }
+#pragma unroll
+                    for (int bb = 0; bb < 10; ++bb) acc[off[bb]] = a[bb];
                 }
-#pragma unroll
-                for (int bb = 0; bb < 10; ++bb) acc[off[bb]] = a[bb];
                 if (has_next) {
                     rc = rcn;
                     rcn = rcnn;
@@ -1379,11 +1389,10 @@ void p1_forms_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, 
 using namespace skg;
 
 extern "C" int skg_h1_assemble_affine(const skg_pattern *pat, const double *d_p, int64_t npts, const int32_t *d_t,
-                                      int32_t nodes, int64_t ne, const int32_t *d_dofs, int32_t nq,
-                                      const double *h_X, const double *h_W, int32_t coef_kind,
-                                      const double *d_coef, int32_t precision, double *d_values, void *stream) {
+                                      int32_t nodes, int64_t ne, int32_t nq, const double *h_X, const double *h_W,
+                                      int32_t coef_kind, const double *d_coef, int32_t precision, double *d_values,
+                                      void *stream) {
     return guarded([&] {
-        (void)d_dofs;
         affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values,
                         as_stream(stream), nullptr, nullptr);
     });
@@ -1405,12 +1414,11 @@ extern "C" int skg_p1_assemble_affine_forms(const skg_pattern *pat, const double
 }
 
 extern "C" int skg_h1_assemble_affine_host(const skg_pattern *pat, const double *d_p, int64_t npts,
-                                           const int32_t *d_t, int32_t nodes, int64_t ne, const int32_t *d_dofs,
-                                           int32_t nq, const double *h_X, const double *h_W, int32_t coef_kind,
+                                           const int32_t *d_t, int32_t nodes, int64_t ne, int32_t nq,
+                                           const double *h_X, const double *h_W, int32_t coef_kind,
                                            const double *d_coef, int32_t precision, double *d_values,
                                            double *h_values, void *stream) {
     return guarded([&] {
-        (void)d_dofs;
         require(h_values != nullptr, "host output is NULL");
         affine_assemble(pat, d_p, npts, d_t, nodes, ne, nq, h_X, h_W, coef_kind, d_coef, precision, d_values,
                         as_stream(stream), nullptr, h_values);
@@ -1418,13 +1426,11 @@ extern "C" int skg_h1_assemble_affine_host(const skg_pattern *pat, const double 
 }
 
 extern "C" int skg_h1_assemble_affine_profiled(const skg_pattern *pat, const double *d_p, int64_t npts,
-                                               const int32_t *d_t, int32_t nodes, int64_t ne,
-                                               const int32_t *d_dofs, int32_t nq, const double *h_X,
-                                               const double *h_W, int32_t coef_kind, const double *d_coef,
-                                               int32_t precision, double *d_values, float *h_kernel_ms,
-                                               void *stream) {
+                                               const int32_t *d_t, int32_t nodes, int64_t ne, int32_t nq,
+                                               const double *h_X, const double *h_W, int32_t coef_kind,
+                                               const double *d_coef, int32_t precision, double *d_values,
+                                               float *h_kernel_ms, void *stream) {
     return guarded([&] {
-        (void)d_dofs;
         require(h_kernel_ms != nullptr, "timing output is NULL");
         cudaStream_t s = as_stream(stream);
         cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

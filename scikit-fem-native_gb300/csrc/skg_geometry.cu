@@ -11,6 +11,9 @@
 #include <iomanip>
 #include <vector>
 
+#include <algorithm>
+#include <climits>
+
 #include "skg_common.cuh"
 
 namespace skg {
@@ -98,10 +101,110 @@ __global__ void k_validate(int64_t ne, int nq, const double *__restrict__ det, c
     if (badq) atomicMin(bad, (unsigned long long)e);
 }
 
+// Geometry diagnostics (basis.py:2296-2356) as one reduction over the
+// (element, point) arrays: smallest and largest determinant, the smallest
+// scaled determinant |det| / (tol / (64 eps)) with its first flat index (the
+// first occurrence, as numpy's argmin), the largest condition number with its
+// first flat index, and the elements whose first point has a negative
+// determinant.  Per block, then one block over the block results.
+struct GeomDiag {
+    double det_min, det_max, scaled_min, cond_max;
+    long long scaled_at, cond_at, negative;
+};
+
+__device__ __forceinline__ void diag_merge(GeomDiag &a, const GeomDiag &b) {
+    a.det_min = fmin(a.det_min, b.det_min);
+    a.det_max = fmax(a.det_max, b.det_max);
+    if (b.scaled_min < a.scaled_min || (b.scaled_min == a.scaled_min && b.scaled_at < a.scaled_at)) {
+        a.scaled_min = b.scaled_min;
+        a.scaled_at = b.scaled_at;
+    }
+    if (b.cond_max > a.cond_max || (b.cond_max == a.cond_max && b.cond_at < a.cond_at)) {
+        a.cond_max = b.cond_max;
+        a.cond_at = b.cond_at;
+    }
+    a.negative += b.negative;
+}
+
+__device__ __forceinline__ GeomDiag diag_identity() {
+    return GeomDiag{INFINITY, -INFINITY, INFINITY, -INFINITY, LLONG_MAX, LLONG_MAX, 0};
+}
+
+constexpr int kDiagThreads = 256;
+
+__device__ __forceinline__ void diag_block_reduce(GeomDiag v, GeomDiag *out) {
+    __shared__ GeomDiag sh[kDiagThreads];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kDiagThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) diag_merge(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void __launch_bounds__(kDiagThreads) k_geom_diag(int64_t n, int nq, const double *__restrict__ det,
+                                                            const double *__restrict__ tol,
+                                                            const double *__restrict__ cond, GeomDiag *part) {
+    const double unit = 64.0 * __DBL_EPSILON__;
+    GeomDiag v = diag_identity();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double d = det[i];
+        v.det_min = fmin(v.det_min, d);
+        v.det_max = fmax(v.det_max, d);
+        const double sc = fabs(d) / (tol[i] / unit);
+        if (sc < v.scaled_min) {  // i increases along the thread's walk: the first index wins ties
+            v.scaled_min = sc;
+            v.scaled_at = i;
+        }
+        const double c = cond[i];
+        if (c > v.cond_max) {
+            v.cond_max = c;
+            v.cond_at = i;
+        }
+        if (i % nq == 0 && d < 0.0) ++v.negative;
+    }
+    diag_block_reduce(v, part + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kDiagThreads) k_geom_diag_final(int n_parts, const GeomDiag *__restrict__ part,
+                                                                  GeomDiag *out) {
+    GeomDiag v = diag_identity();
+    for (int i = threadIdx.x; i < n_parts; i += blockDim.x) diag_merge(v, part[i]);
+    diag_block_reduce(v, out);
+}
+
 }  // namespace
 }  // namespace skg
 
 using namespace skg;
+
+extern "C" int skg_geometry_diagnostics(const double *d_det, const double *d_tol, const double *d_cond,
+                                        int64_t n_elements, int32_t nq, double *h_values, int64_t *h_indices,
+                                        void *stream) {
+    return guarded([&] {
+        require(n_elements > 0 && nq > 0, "geometry diagnostics need at least one element and point");
+        require(d_det && d_tol && d_cond && h_values && h_indices, "diagnostics arrays are NULL");
+        cudaStream_t s = as_stream(stream);
+        const int64_t n = n_elements * (int64_t)nq;
+        const int parts = (int)std::min<int64_t>(2 * kSmCount, (n + kDiagThreads - 1) / kDiagThreads);
+        DevBuf<GeomDiag> part((size_t)parts + 1, s);
+        k_geom_diag<<<parts, kDiagThreads, 0, s>>>(n, nq, d_det, d_tol, d_cond, part.get());
+        SKG_LAUNCH_CHECK("geom_diag");
+        k_geom_diag_final<<<1, kDiagThreads, 0, s>>>(parts, part.get(), part.get() + parts);
+        SKG_LAUNCH_CHECK("geom_diag_final");
+        GeomDiag r;
+        SKG_CUDA(cudaMemcpyAsync(&r, part.get() + parts, sizeof(r), cudaMemcpyDeviceToHost, s));
+        SKG_CUDA(cudaStreamSynchronize(s));
+        h_values[0] = r.det_min;
+        h_values[1] = r.det_max;
+        h_values[2] = r.scaled_min;
+        h_values[3] = r.cond_max;
+        h_indices[0] = r.scaled_at;
+        h_indices[1] = r.cond_at;
+        h_indices[2] = r.negative;
+    });
+}
 
 extern "C" int skg_tabulate_geometry(const double *d_p, int64_t npts, const int32_t *d_t, int32_t gnodes,
                                      int64_t ne, int32_t nq, int32_t nodes, const double *h_shape,

@@ -5,8 +5,9 @@
 // P accumulator copies, fit SLOTS in shared memory); thread part p of row r
 // walks the row's incidence records p, p + P, ... (ascending element order),
 // loads row a of K_e (N doubles, the next record's row one step ahead, the
-// records themselves two steps ahead) and
-// adds it into its accumulator copy at the record's column offsets; the
+// records themselves two steps ahead) and adds it into its accumulator copy
+// at the record's column offsets (the first incidence stores instead: an
+// element's columns are distinct slots, so no slot is touched twice); the
 // warp sums the copies in copy order and writes the group's slot range with
 // coalesced stores.  No atomics: bitwise reproducible.  Optionally the same
 // walk sums a per-incidence vector re (E * row_local, e.g. element residual
@@ -22,21 +23,19 @@ namespace skg {
 
 constexpr int kRowWarps = 4;  // warps per CTA in the row passes
 
+// One warp's share of the row pass: row group grp (rows [grp.x, grp.y)),
+// accumulators in `acc` (SLOTS doubles of shared memory).  Each part's first
+// incidence stores its row into the accumulators (the other slots start at
+// zero), later incidences add.  See k_rows_ke.
 template <int N, int SLOTS, int P>
-__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const int2 *__restrict__ groups,
-                                                           const int32_t *__restrict__ indptr,
-                                                           const int32_t *__restrict__ inc_ptr,
-                                                           const int4 *__restrict__ rec, const double *__restrict__ Ke,
-                                                           double *__restrict__ values, const double *__restrict__ re,
-                                                           double *__restrict__ residual) {
+__device__ __forceinline__ void rows_ke_warp(int2 grp, const int32_t *__restrict__ indptr,
+                                             const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec,
+                                             const double *__restrict__ Ke, double *__restrict__ values,
+                                             const double *__restrict__ re, double *__restrict__ residual,
+                                             double *acc) {
     static_assert(N % 2 == 0 && N <= 12, "rows are loaded as 16-byte pairs, at most 12 columns");
     static_assert(P == 1 || P == 2, "one or two accumulator copies");
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gi = blockIdx.x * kRowWarps + warp;
-    if (gi >= n_groups) return;
-    double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
-    const int2 grp = groups[gi];
+    const int lane = threadIdx.x & 31;
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
     for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.0;
@@ -59,6 +58,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
 #pragma unroll
                 for (int q = 0; q < N / 2; ++q) cur[q] = __ldg(src + q);
             }
+            bool first = true;
             for (; it < it1; it += P) {
                 const bool has_next = it + P < it1;
                 double2 nxt[N / 2];
@@ -73,13 +73,23 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
                 int off[N];
 #pragma unroll
                 for (int bb = 0; bb < N; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                double a[N];
+                if (first) {
+                    // an element's columns are distinct slots: no add needed
 #pragma unroll
-                for (int bb = 0; bb < N; ++bb) a[bb] = acc[off[bb]];
+                    for (int q = 0; q < N / 2; ++q) {
+                        acc[off[2 * q]] = cur[q].x;
+                        acc[off[2 * q + 1]] = cur[q].y;
+                    }
+                    first = false;
+                } else {
+                    double a[N];
 #pragma unroll
-                for (int q = 0; q < N / 2; ++q) {
-                    acc[off[2 * q]] = a[2 * q] + cur[q].x;
-                    acc[off[2 * q + 1]] = a[2 * q + 1] + cur[q].y;
+                    for (int bb = 0; bb < N; ++bb) a[bb] = acc[off[bb]];
+#pragma unroll
+                    for (int q = 0; q < N / 2; ++q) {
+                        acc[off[2 * q]] = a[2 * q] + cur[q].x;
+                        acc[off[2 * q + 1]] = a[2 * q + 1] + cur[q].y;
+                    }
                 }
                 if (has_next) {
                     rc = rcn;
@@ -101,6 +111,21 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const 
         for (int c = 1; c < P; ++c) v += acc[c * nslots + j];
         values[s0 + j] = v;
     }
+}
+
+template <int N, int SLOTS, int P>
+__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke(int n_groups, const int2 *__restrict__ groups,
+                                                           const int32_t *__restrict__ indptr,
+                                                           const int32_t *__restrict__ inc_ptr,
+                                                           const int4 *__restrict__ rec, const double *__restrict__ Ke,
+                                                           double *__restrict__ values, const double *__restrict__ re,
+                                                           double *__restrict__ residual) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5;
+    const int gi = blockIdx.x * kRowWarps + warp;
+    if (gi >= n_groups) return;
+    double *acc = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
+    rows_ke_warp<N, SLOTS, P>(groups[gi], indptr, inc_ptr, rec, Ke, values, re, residual, acc);
 }
 
 template <int N, int SLOTS, int P>

@@ -36,15 +36,16 @@ SIGNATURES = {
     "skg_pattern_destroy": [_vp],
     "skg_pattern_info": [_vp, _i64p, _i64p, _i64p],
     "skg_pattern_export": [_vp, _vp, _vp, _vp],
+    "skg_geometry_diagnostics": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp],
     "skg_tabulate_geometry": [_vp, _i64, _vp, _i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64p, _vp],
     "skg_h1_assemble_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp,
                                   _vp, _vp, _vp, _vp],
     "skg_h1_assemble_tensor_tabulated": [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp,
                                          _vp, _vp],
-    "skg_h1_assemble_affine": [_vp, _vp, _i64, _vp, _i32, _i64, _vp, _i32, _vp, _vp, _i32, _vp,
+    "skg_h1_assemble_affine": [_vp, _vp, _i64, _vp, _i32, _i64, _i32, _vp, _vp, _i32, _vp,
                                _i32, _vp, _vp],
-    "skg_h1_assemble_affine_profiled": [_vp, _vp, _i64, _vp, _i32, _i64, _vp, _i32, _vp, _vp, _i32,
+    "skg_h1_assemble_affine_profiled": [_vp, _vp, _i64, _vp, _i32, _i64, _i32, _vp, _vp, _i32,
                                         _vp, _i32, _vp, ctypes.POINTER(ctypes.c_float), _vp],
     "skg_h1_assemble_affine_noalloc": [_vp, _vp, _i64, _vp, _i32, _i64, _i32, _vp, _vp, _i32, _vp, _i32,
                                        _vp, _vp],
@@ -74,7 +75,7 @@ SIGNATURES = {
     "skg_mlp_eval": [_vp, _vp, _i64, _vp, _vp],
     "skg_fp64_fma_rate": [_vp, _vp],
     "skg_device_pageable_access": [ctypes.POINTER(ctypes.c_int32)],
-    "skg_h1_assemble_affine_host": [_vp, _vp, _i64, _vp, _i32, _i64, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp,
+    "skg_h1_assemble_affine_host": [_vp, _vp, _i64, _vp, _i32, _i64, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp,
                                     _vp],
     "skg_cross_assemble_tabulated": [_vp, _i64, _i32, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp,
                                      _vp, _vp, _vp],

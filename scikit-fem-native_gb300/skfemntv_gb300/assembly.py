@@ -296,11 +296,11 @@ class NativeBilinearForm:
                 coef = dev.ptr(keep)
         if host:  # values to the host matrix: copies overlap the row pass
             call("skg_h1_assemble_affine_host", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, Q, dev.hptr(b.X),
                  dev.hptr(b.W), 0, coef, prec, dev.ptr(self.target.d_values), out, dev.stream_ptr())
         else:
             call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, Q, dev.hptr(b.X),
                  dev.hptr(b.W), 0, coef, prec, out, dev.stream_ptr())
         return keep
 
@@ -316,7 +316,7 @@ class NativeBilinearForm:
 
         def launch():
             call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, Q, dev.hptr(b.X),
                  dev.hptr(b.W), 0, dev.ptr(kappa), SKG_FP64, dev.ptr(self.target.d_values), dev.stream_ptr())
 
         return AssemblyGraph(launch, self.target)
@@ -481,11 +481,11 @@ class NativeTensorForm:
         if coef is not None:
             if out is not None:  # values to the host matrix: copies overlap the row pass
                 call("skg_h1_assemble_affine_host", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                     dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                     dev.ptr(b.mesh._dev("t")), b._nodes, E, Q, dev.hptr(b.X),
                      dev.hptr(b.W), kind, coef, prec, dev.ptr(self.target.d_values), out, dev.stream_ptr())
                 return True
             call("skg_h1_assemble_affine", self.pattern.h, dev.ptr(b.mesh._dev("p")), b.mesh.p.shape[1],
-                 dev.ptr(b.mesh._dev("t")), b._nodes, E, dev.ptr(b._dev_dofs()), Q, dev.hptr(b.X),
+                 dev.ptr(b.mesh._dev("t")), b._nodes, E, Q, dev.hptr(b.X),
                  dev.hptr(b.W), kind, coef, prec, dev.ptr(self.target.d_values), dev.stream_ptr())
             return False
         if prec != SKG_FP64:

@@ -177,26 +177,27 @@ class Basis:
 
     @property
     def geometry_diagnostics(self):
-        """Same fields and selection rules as basis.py:2296-2356."""
-        det = self._geometry_determinants
-        tol = self._geometry_tolerances
-        cond = self._geometry_condition_numbers
-        if det.size == 0:
-            return GeometryDiagnostics(0, det.shape[1] if det.ndim == 2 else 0, float("inf"), float("-inf"),
-                                       float("inf"), -1, -1, 0.0, 0, 0.0, -1, -1)
-        scaled = np.abs(det) / (tol / (64.0 * np.finfo(np.float64).eps))
-        flat = int(np.argmin(scaled))
-        e, q = np.unravel_index(flat, det.shape)
-        cflat = int(np.argmax(cond))
-        ce, cq = np.unravel_index(cflat, cond.shape)
+        """Same fields and selection rules as basis.py:2296-2356, reduced on the
+        device (skg_geometry_diagnostics): nothing of size (E, Q) is copied."""
+        det = self._geom["det"]
+        E, Q = (int(det.shape[0]), int(det.shape[1])) if det.dim() == 2 else (0, 0)
+        if E == 0 or Q == 0:
+            return GeometryDiagnostics(0, Q, float("inf"), float("-inf"), float("inf"), -1, -1, 0.0, 0, 0.0, -1, -1)
+        vals = np.empty(4, dtype=np.float64)
+        idx = np.empty(3, dtype=np.int64)
+        call("skg_geometry_diagnostics", dev.ptr(det), dev.ptr(self._geom["tol"]), dev.ptr(self._geom["cond"]),
+             E, Q, dev.hptr(vals), dev.hptr(idx), dev.stream_ptr())
+        e, q = divmod(int(idx[0]), Q)
+        ce, cq = divmod(int(idx[1]), Q)
+        tol = float(self._geom["tol"].view(-1)[int(idx[0])].item())
         return GeometryDiagnostics(
-            element_count=int(det.shape[0]), quadrature_points_per_element=int(det.shape[1]),
-            minimum_determinant=float(np.min(det)), maximum_determinant=float(np.max(det)),
-            minimum_scaled_determinant=float(scaled.flat[flat]), worst_element=int(e),
-            worst_quadrature_point=int(q), determinant_tolerance=float(tol.flat[flat]),
-            negative_orientation_elements=int(np.count_nonzero(det[:, 0] < 0.0)),
-            maximum_condition_number=float(cond.flat[cflat]), worst_condition_element=int(ce),
-            worst_condition_quadrature_point=int(cq))
+            element_count=E, quadrature_points_per_element=Q,
+            minimum_determinant=float(vals[0]), maximum_determinant=float(vals[1]),
+            minimum_scaled_determinant=float(vals[2]), worst_element=e,
+            worst_quadrature_point=q, determinant_tolerance=tol,
+            negative_orientation_elements=int(idx[2]),
+            maximum_condition_number=float(vals[3]), worst_condition_element=ce,
+            worst_condition_quadrature_point=cq)
 
     # ------------------------------------------------------------ device maps
     def _dev_dofs(self):

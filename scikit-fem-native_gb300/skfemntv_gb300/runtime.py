@@ -29,13 +29,13 @@ def has_capability(name: str) -> bool:
 
 
 def available_num_threads() -> int:
-    affinity = getattr(os, "sched_getaffinity", None)
-    if affinity is not None:
-        try:
-            return max(1, len(affinity(0)))
-        except OSError:
-            pass
-    return max(1, os.cpu_count() or 1)
+    """Host CPUs this process may run on (its affinity mask where the OS
+    reports one, else the machine's CPU count); at least 1."""
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        usable = os.cpu_count() or 1
+    return usable if usable > 0 else 1
 
 
 def get_num_threads() -> int:

@@ -600,3 +600,40 @@ def test_p2_anisotropic_fused_rule_not_exact_on_quadratics(rule):
         d, indptr, indices = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(Apub, (E, Q)))
         assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
         assert relerr(K.data, d) < RTOL
+
+
+def _numpy_diagnostics(det, tol, cond):
+    """The reference's host reductions (python/skfemntv/basis.py:2296-2356)."""
+    scaled = np.abs(det) / (tol / (64.0 * np.finfo(np.float64).eps))
+    flat = int(np.argmin(scaled))
+    cflat = int(np.argmax(cond))
+    Q = det.shape[1]
+    return dict(element_count=det.shape[0], quadrature_points_per_element=Q,
+                minimum_determinant=float(np.min(det)), maximum_determinant=float(np.max(det)),
+                minimum_scaled_determinant=float(scaled.flat[flat]), worst_element=flat // Q,
+                worst_quadrature_point=flat % Q, determinant_tolerance=float(tol.flat[flat]),
+                negative_orientation_elements=int(np.count_nonzero(det[:, 0] < 0.0)),
+                maximum_condition_number=float(cond.flat[cflat]), worst_condition_element=cflat // Q,
+                worst_condition_quadrature_point=cflat % Q)
+
+
+@pytest.mark.parametrize("flip", [False, True])
+def test_geometry_diagnostics_device_reduction(flip):
+    """Basis.geometry_diagnostics reduces det / tol / cond on the device; every
+    field equals the reference's numpy reductions over the same arrays,
+    including the first-occurrence choice of the worst point."""
+    g = load_golden("p2_aniso")
+    t = g["t"].copy()
+    if flip:  # every third element with vertices 1 and 2 (and the edge nodes) swapped: negative orientation
+        sel = np.arange(t.shape[1]) % 3 == 0
+        t[:, sel] = g["t"][[0, 2, 1, 3, 6, 5, 4, 7, 9, 8]][:, sel]
+    b = sk.Basis(sk.MeshTet2(g["p"], t), sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(g["X"], g["W"]))
+    d = b.geometry_diagnostics
+    want = _numpy_diagnostics(b._geometry_determinants, b._geometry_tolerances, b._geometry_condition_numbers)
+    for k, v in want.items():
+        assert getattr(d, k) == v, (k, getattr(d, k), v)
+    if not flip:
+        assert d.minimum_determinant == float(np.min(g["det"]))
+        assert d.maximum_condition_number == float(np.max(g["cond"]))
+    else:
+        assert 0 < d.negative_orientation_elements < t.shape[1]
