@@ -131,3 +131,51 @@ def test_fused_value_and_gradients_match_separate_passes():
                 assert t.grad is None
     with torch.no_grad():
         assert torch.equal(op(*[t.clone().requires_grad_(True) for t in base]), J0)
+
+
+def patch_energy(p, t, patch, kappa, u, v):
+    """J restricted to the elements `patch` (every other element's term is
+    unchanged by the perturbations below), through the oracle's assembly."""
+    sub = np.ascontiguousarray(t[:, patch])
+    active = np.unique(sub)  # the oracle compacts to these vertices, in this order
+    J, _ = oracle_energy(p, sub, kappa[patch], u[active], v[active])
+    return J
+
+
+def test_fd_gradients_on_the_64_cube():
+    """The benchmark's adjoint size, 64^3 x 6 (1,572,864 tets), interior
+    vertices jittered: dJ/dkappa on 100 seeded elements and dJ/dx on 100
+    seeded interior coordinates against central differences (h = 1e-6).
+    J is a sum of element terms, so each difference is taken over the
+    elements the perturbed kappa_e or vertex touches (the oracle assembles
+    that patch); the other terms cancel exactly."""
+    mesh, basis, kappa, u, v = problem(n=64, seed=4)
+    assert mesh.nelements == 1572864
+    op = sk.P1Energy(basis)
+    kt, pt, ut, vt = (cuda(a).requires_grad_(True) for a in (kappa, mesh.p, u, v))
+    op(kt, pt, ut, vt).backward()
+    gk, gp = kt.grad.cpu().numpy(), pt.grad.cpu().numpy()
+    p, t = mesh.p, mesh.t
+    h = 1e-6
+    rng = np.random.default_rng(np.random.SeedSequence(200))
+    worst = 0.0
+    for e in rng.choice(mesh.nelements, 100, replace=False):
+        kp, km = kappa.copy(), kappa.copy()
+        kp[e] += h
+        km[e] -= h
+        fd = (patch_energy(p, t, [e], kp, u, v) - patch_energy(p, t, [e], km, u, v)) / (2 * h)
+        err = abs(gk[e] - fd) / max(abs(fd), 1e-3 * np.max(np.abs(gk)))
+        worst = max(worst, err)
+        assert err <= 1e-7, (e, gk[e], fd)
+    inner = np.flatnonzero(np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0))
+    scale = np.max(np.abs(gp[:, inner]))
+    for node, i in zip(rng.choice(inner, 100, replace=False), rng.integers(0, 3, 100)):
+        patch = np.flatnonzero(np.any(t == node, axis=0))
+        pp, pm = p.copy(), p.copy()
+        pp[i, node] += h
+        pm[i, node] -= h
+        fd = (patch_energy(pp, t, patch, kappa, u, v) - patch_energy(pm, t, patch, kappa, u, v)) / (2 * h)
+        err = abs(gp[i, node] - fd) / max(abs(fd), 1e-3 * scale)
+        worst = max(worst, err)
+        assert err <= 1e-6, (node, i, gp[i, node], fd)
+    print(f"64^3 adjoint vs central differences: worst relative error {worst:.2e}")
