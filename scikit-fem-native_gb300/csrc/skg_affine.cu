@@ -779,6 +779,75 @@ __device__ __forceinline__ double exact_entry_fp64(const double g[16]) {
     return v;
 }
 
+// The 55 entries of a symmetric element matrix with fewer FP64 instructions
+// than one exact_entry_fp64 per entry (about 85 against 112).  With S_v(b) =
+// G_v,lo(b) + G_v,hi(b) (vertex v, edge b, 24 sums), the integer table gives
+//   vertex a, vertex b:      3 G_aa (a = b), -G_ab
+//   vertex a, edge b:        -S_a(b) (a not on b), 3 G_a,hi - G_a,lo (a = lo(b)), 3 G_a,lo - G_a,hi (a = hi(b))
+//   edge a = (i, j), edge b: 4 (S_i(b) + S_j(b) + X), X = G_ii + G_jj (a = b),
+//                            G_(other end of a),(other end of b) (one shared vertex), 0 (disjoint)
+// (t30 = 4 (1 + d) - 5 on vertex functions, 4 (1 + d) on edge pairs).  The
+// sign flips and the factor 4 act on the bits (integer instructions): exact,
+// provided every sum stays a normal number below the overflow threshold,
+// which shared_entries_ok checks on G first.
+__device__ __forceinline__ double neg_bits(double x) {
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+__device__ __forceinline__ double times4_bits(double x) {  // zero stays zero
+    const int hi = __double2hiint(x);
+    return __hiloint2double(hi + ((hi & 0x7ff00000) ? 0x00200000 : 0), __double2loint(x));
+}
+
+// Every nonzero G entry with a biased exponent in [64, 2032]: then any sum of
+// up to six of them is zero or a normal number (a multiple of the smallest
+// entry's unit in the last place, above 2^-1022) and four times it is finite.
+__device__ __forceinline__ bool shared_entries_ok(const double g[16]) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        const int hi = __double2hiint(g[k]), lo = __double2loint(g[k]);
+        const int ex = (hi >> 20) & 0x7ff;
+        ok = ok && (((hi & 0x7fffffff) | lo) == 0 || (ex >= 64 && ex <= 2032));
+    }
+    return ok;
+}
+
+template <int A, int BB>
+__device__ __forceinline__ double shared_entry(const double g[16], const double S[4][6]) {
+    if constexpr (A < 4 && BB < 4) {
+        if constexpr (A == BB) return 3.0 * g[A * 4 + A];
+        else return neg_bits(g[A * 4 + BB]);
+    } else if constexpr (A < 4) {
+        constexpr int lo = sup_lo(BB), hi = sup_hi(BB);
+        if constexpr (A != lo && A != hi) return neg_bits(S[A][BB - 4]);
+        else if constexpr (A == lo) return fma(3.0, g[A * 4 + hi], -g[A * 4 + lo]);
+        else return fma(3.0, g[A * 4 + lo], -g[A * 4 + hi]);
+    } else {
+        constexpr int i = sup_lo(A), j = sup_hi(A), lb = sup_lo(BB), hb = sup_hi(BB);
+        const double T = S[i][BB - 4] + S[j][BB - 4];
+        if constexpr (A == BB) {
+            return times4_bits(T + (g[i * 4 + i] + g[j * 4 + j]));
+        } else if constexpr (i == lb || i == hb || j == lb || j == hb) {
+            constexpr int na = (i == lb || i == hb) ? j : i, nb = (lb == i || lb == j) ? hb : lb;
+            return times4_bits(T + g[na * 4 + nb]);
+        } else {
+            return times4_bits(T);
+        }
+    }
+}
+
+__device__ __forceinline__ void shared_entries(const double g[16], double U[55]) {
+    double S[4][6];
+    static_for<0, 24>([&](auto kk) {
+        constexpr int k = decltype(kk)::value, v = k / 6, e = k % 6;
+        S[v][e] = g[v * 4 + sup_lo(4 + e)] + g[v * 4 + sup_hi(4 + e)];
+    });
+    static_for<0, 100>([&](auto kk) {
+        constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+        if constexpr (A <= BB) U[tri10(A, BB)] = shared_entry<A, BB>(g, S);
+    });
+}
+
 // k_elem_ke_fp64 for a rule exact on quadratics (the 4-point and the 11-point
 // Keast rule): the entries from the integer table with compile-time factors
 // (about 30 FP64 instructions per element fewer than the table read from
@@ -801,10 +870,14 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64_exact(int64_t ne, int
     }
     double U[55];
     if (sym) {
-        static_for<0, 100>([&](auto kk) {
-            constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
-            if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry_fp64<A, BB>(g);
-        });
+        if (shared_entries_ok(g)) {
+            shared_entries(g, U);
+        } else {
+            static_for<0, 100>([&](auto kk) {
+                constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+                if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry_fp64<A, BB>(g);
+            });
+        }
     }
     const int nvalid = (int)(e_end - e0 < kKeBlock ? e_end - e0 : kKeBlock);
     double *st = stage + threadIdx.x * kKeChunk;
