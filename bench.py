@@ -537,10 +537,11 @@ def _relerr(a, b):
     return float((a - b).abs().max() / b.abs().max())
 
 
-def sine_displacement(doflocs, seed=5, amplitude=0.05):
+def sine_displacement(doflocs, seed=5, amplitude=0.05, wavevectors="unit"):
     """Vector P1 displacement: 8 modes amplitude * d_m sin(pi k_m . x + phi_m)
-    with seeded unit directions d_m, phases phi_m and unit wavevectors
-    k_m = +-e_axis (node-major DOFs, component fastest)."""
+    with seeded unit directions d_m, phases phi_m and wavevectors k_m =
+    +-e_axis ("unit") or drawn from {-1, 0, 1}^3 without 0 ("int3") (node-major
+    DOFs, component fastest)."""
     rng = np.random.default_rng(np.random.SeedSequence(seed))
     n = doflocs.shape[1]
     u = np.zeros(n)
@@ -548,8 +549,13 @@ def sine_displacement(doflocs, seed=5, amplitude=0.05):
     for _ in range(8):
         d = rng.standard_normal(3)
         d /= np.linalg.norm(d)
-        kv = np.zeros(3)
-        kv[rng.integers(0, 3)] = rng.choice([-1.0, 1.0])
+        if wavevectors == "unit":
+            kv = np.zeros(3)
+            kv[rng.integers(0, 3)] = rng.choice([-1.0, 1.0])
+        else:
+            kv = np.zeros(3)
+            while not kv.any():
+                kv = rng.integers(-1, 2, size=3).astype(np.float64)
         ph = rng.uniform(0, 2 * np.pi)
         u += amplitude * d[comp] * np.sin(np.pi * (kv @ doflocs) + ph)
     return u
@@ -753,6 +759,30 @@ def wl_nh(args, world, timed, wall):
     fallback = nh.last_fallback
     err_r = _relerr(nh.d_res[: b.N], r0)
     err_k = _relerr(nh.target.d_values[:nnz], k0)
+    # the same law and network on the other displacement recipe (integer
+    # wavevectors in {-1, 0, 1}^3): deformation gradients farther from the
+    # training distribution, so some elements take the plain-law fallback
+    u_int = sine_displacement(b.doflocs, wavevectors="int3")
+    du_int = dev.to_device(u_int, np.float64)
+    ms_plain_i, _ = timed(lambda: nh.assemble_device(du_int), flush_l2=True)
+    r0i = nh.d_res[: b.N].clone()
+    k0i = nh.target.d_values[:nnz].clone()
+    ms_sur_i, _ = timed(lambda: nh.assemble_device(du_int, surrogate=sur, tol=1e-2, count_fallback=False),
+                        flush_l2=True)
+    nh.assemble_device(du_int, surrogate=sur, tol=1e-2)
+    int3 = {"tol_1e-2": {"fallback_elements": nh.last_fallback, "fallback_fraction": nh.last_fallback / E,
+                         "plain_ms": ms_plain_i, "surrogate_ms": ms_sur_i, "speedup_vs_plain": ms_plain_i / ms_sur_i,
+                         "max_rel_err_residual": _relerr(nh.d_res[: b.N], r0i),
+                         "max_rel_err_tangent": _relerr(nh.target.d_values[:nnz], k0i)}}
+    # a tighter stress check sends more of these elements to the plain law
+    ms_sur_t, _ = timed(lambda: nh.assemble_device(du_int, surrogate=sur, tol=1e-4, count_fallback=False),
+                        flush_l2=True)
+    nh.assemble_device(du_int, surrogate=sur, tol=1e-4)
+    int3["tol_1e-4"] = {"fallback_elements": nh.last_fallback, "fallback_fraction": nh.last_fallback / E,
+                        "surrogate_ms": ms_sur_t, "speedup_vs_plain": ms_plain_i / ms_sur_t,
+                        "max_rel_err_residual": _relerr(nh.d_res[: b.N], r0i),
+                        "max_rel_err_tangent": _relerr(nh.target.d_values[:nnz], k0i)}
+    del du_int, r0i, k0i
     hu = torch.empty(b.N, dtype=torch.float64, pin_memory=True)
     hu.numpy()[:] = u
     e2e_s = wall(lambda: nh.assemble(hu.numpy()))
@@ -772,7 +802,8 @@ def wl_nh(args, world, timed, wall):
                          "speedup_vs_plain": ms_plain / ms_sur, "max_rel_err_residual": err_r,
                          "max_rel_err_tangent": err_k, "fallback_elements": fallback,
                          "training_seconds": t_train, "training_history": sur.history[-2:],
-                         "roofline": _roofline(alg, ms_sur), "clocks": clk_s},
+                         "roofline": _roofline(alg, ms_sur), "clocks": clk_s,
+                         "integer_wavevectors": int3},
         gpu_launches=3 * args.steps)
 
 

@@ -285,6 +285,7 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64(int64_t ne, int64_t e
 // integer pipes; only the winner's exponent is decoded.
 __global__ void k_scale(const double *__restrict__ p, int64_t n, int *__restrict__ s_out) {
     unsigned long long m = 0;
+#pragma unroll 8
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const unsigned long long b = (unsigned long long)__double_as_longlong(p[i]) & 0x7fffffffffffffffULL;
         if (b < 0x7ff0000000000000ULL) m = b > m ? b : m;  // finite values only
@@ -904,14 +905,15 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_fp64_exact(int64_t ne, int
     });
 }
 
+// Tile `tile` (kKeBlock elements) of k_elem_ke_df64; `stage` kKeBlock *
+// kKeChunk pairs of shared memory.
 template <int MODE>
-__global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
-                                                           const int32_t *__restrict__ t, int coef_kind,
-                                                           const double *__restrict__ coef,
-                                                           const int *__restrict__ s_ptr, float2 *__restrict__ Ke,
-                                                           int *__restrict__ range_flag) {
-    __shared__ float2 stage[kKeBlock * kKeChunk];
-    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+__device__ __forceinline__ void elem_ke_df64_tile(int64_t tile, int64_t ne, const double *__restrict__ p,
+                                                  int64_t npts, const int32_t *__restrict__ t, int coef_kind,
+                                                  const double *__restrict__ coef, const int *__restrict__ s_ptr,
+                                                  float2 *__restrict__ Ke, int *__restrict__ range_flag,
+                                                  float2 *stage) {
+    const int64_t e0 = tile * kKeBlock;
     const int64_t e = e0 + threadIdx.x;
     const bool valid = e < ne;
     df64 g[16];
@@ -955,6 +957,146 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64(int64_t ne, const dou
         __syncthreads();
     });
 }
+
+// The blocks walk the tiles (grid-stride); with `only` non-NULL they
+// assemble only the tiles with only[tile] set.
+template <int MODE>
+__global__ void __launch_bounds__(kKeBlock, 3) k_elem_ke_df64(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                           const int32_t *__restrict__ t, int coef_kind,
+                                                           const double *__restrict__ coef,
+                                                           const int *__restrict__ s_ptr, float2 *__restrict__ Ke,
+                                                           int *__restrict__ range_flag,
+                                                           const uint8_t *__restrict__ only = nullptr) {
+    __shared__ float2 stage[kKeBlock * kKeChunk];
+    __shared__ uint8_t flag[kKeBlock];
+    const int64_t n_tiles = (ne + kKeBlock - 1) / kKeBlock;
+    if (!only) {
+        for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+            elem_ke_df64_tile<MODE>(tile, ne, p, npts, t, coef_kind, coef, s_ptr, Ke, range_flag, stage);
+        return;
+    }
+    // kKeBlock flags per round, read by the block at once
+    for (int64_t base = (int64_t)blockIdx.x * kKeBlock; base < n_tiles; base += (int64_t)gridDim.x * kKeBlock) {
+        flag[threadIdx.x] = base + threadIdx.x < n_tiles ? only[base + threadIdx.x] : 0;
+        if (!__syncthreads_or(flag[threadIdx.x])) continue;
+        for (int j = 0; j < kKeBlock; ++j)
+            if (flag[j])
+                elem_ke_df64_tile<MODE>(base + j, ne, p, npts, t, coef_kind, coef, s_ptr, Ke, range_flag, stage);
+        __syncthreads();  // flags of the next round
+    }
+}
+
+// Element matrices of SKG_SPLIT_FP32 (P2, exact rule): G in double-float, each
+// entry's integer-factor terms summed in FP32 with split products
+// (exact_entry<MODE_SPLIT>), the entry rounded to FP32.  Each entry goes to
+// shared memory as it is computed (the packed upper triangle of a symmetric
+// matrix, mirrored by the copy-out; every entry, in two rounds of five rows,
+// when a tile holds a nonsymmetric coefficient), so no entry array is held
+// in registers: enough warps to hide the coordinate and coefficient loads.
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_split(int64_t ne, const double *__restrict__ p, int64_t npts,
+                                                            const int32_t *__restrict__ t, int coef_kind,
+                                                            const double *__restrict__ coef,
+                                                            const int *__restrict__ s_ptr, float *__restrict__ Ke,
+                                                            int *__restrict__ range_flag) {
+    constexpr int kPacked = 55, kHalf = 51;  // odd strides: conflict-free per-thread stores
+    __shared__ float stage[kKeBlock * kPacked];
+    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    df64 g[16];
+    bool ok = true, sym = true;
+    if (e < ne) {
+        sym = elem_g_df64(ne, p, npts, t, coef_kind, coef, *s_ptr, true, e, g, ok);
+        if (!ok) atomicExch(range_flag, 1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = df64{0.f, 0.f};
+    }
+    const int nvalid = (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock);
+    if (__syncthreads_and(sym)) {
+        float *st = stage + threadIdx.x * kPacked;
+        static_for<0, 100>([&](auto kk) {
+            constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+            if constexpr (A <= BB) {
+                const df64 v = exact_entry<A, BB, MODE_SPLIT>(g);
+                st[tri10(A, BB)] = v.hi + v.lo;
+            }
+        });
+        __syncthreads();
+        for (int i = threadIdx.x; i < nvalid * 100; i += kKeBlock) {
+            const int el = i / 100, k = i - el * 100, a = k / 10, b = k - a * 10;
+            Ke[(e0 + el) * 100 + k] = stage[el * kPacked + (a <= b ? tri10(a, b) : tri10(b, a))];
+        }
+    } else {
+        float *st = stage + threadIdx.x * kHalf;
+        static_for<0, 2>([&](auto rr) {
+            constexpr int r = decltype(rr)::value;
+            static_for<0, 50>([&](auto qq) {
+                constexpr int q = decltype(qq)::value, k = r * 50 + q;
+                const df64 v = exact_entry<k / 10, k % 10, MODE_SPLIT>(g);
+                st[q] = v.hi + v.lo;
+            });
+            __syncthreads();
+            for (int i = threadIdx.x; i < nvalid * 50; i += kKeBlock) {
+                const int el = i / 50, q = i - el * 50;
+                Ke[(e0 + el) * 100 + r * 50 + q] = stage[el * kHalf + q];
+            }
+            __syncthreads();
+        });
+    }
+}
+
+// SKG_FP64_EMULATED element matrices with a symmetric coefficient: each of
+// the 55 distinct entries is stored to shared memory as it is computed
+// (packed upper triangle, mirrored by the copy-out) instead of being held in
+// registers until its row is staged as in k_elem_ke_df64: 64 registers
+// against 168, so more warps per SM (0.53 -> 0.41 ms at 64^3).  A tile with a
+// nonsymmetric coefficient is flagged in `redo` and left to k_elem_ke_df64.
+template <typename T>
+__device__ __forceinline__ void copy_packed(const T *stage, int nvalid, int64_t e0, T *__restrict__ Ke) {
+    for (int i = threadIdx.x; i < nvalid * 100; i += kKeBlock) {
+        const int el = i / 100, k = i - el * 100, a = k / 10, b = k - a * 10;
+        Ke[(e0 + el) * 100 + k] = stage[el * 55 + (a <= b ? tri10(a, b) : tri10(b, a))];
+    }
+}
+
+__global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64_packed(int64_t ne, const double *__restrict__ p,
+                                                                  int64_t npts, const int32_t *__restrict__ t,
+                                                                  int coef_kind, const double *__restrict__ coef,
+                                                                  const int *__restrict__ s_ptr,
+                                                                  float2 *__restrict__ Ke,
+                                                                  int *__restrict__ range_flag,
+                                                                  uint8_t *__restrict__ redo) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *stage = reinterpret_cast<float2 *>(smem);  // kKeBlock x 55
+    const int64_t e0 = (int64_t)blockIdx.x * kKeBlock;
+    const int64_t e = e0 + threadIdx.x;
+    df64 g[16];
+    bool ok = true, sym = true;
+    if (e < ne) {
+        sym = elem_g_df64(ne, p, npts, t, coef_kind, coef, *s_ptr, true, e, g, ok);
+        if (!ok) atomicExch(range_flag, 1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = df64{0.f, 0.f};
+    }
+    if (!__syncthreads_and(sym)) {  // a nonsymmetric coefficient: k_elem_ke_df64 redoes this tile
+        if (threadIdx.x == 0) redo[blockIdx.x] = 1;
+        return;
+    }
+    float2 *st = stage + threadIdx.x * 55;
+    static_for<0, 100>([&](auto kk) {
+        constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
+        if constexpr (A <= BB) {
+            const df64 v = exact_entry<A, BB, MODE_DF64>(g);
+            st[tri10(A, BB)] = make_float2(v.hi, v.lo);
+        }
+    });
+    __syncthreads();
+    copy_packed(stage, (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock), e0, Ke);
+}
+
+constexpr int kPackedSmem = kKeBlock * 55 * 8;  // 56,320 bytes
+
 
 // Row pass over double-float element matrices: rows of 10 (hi, lo) pairs added
 // into double-float slots, converted to FP64 at write-out.
@@ -1055,6 +1197,108 @@ void launch_ke_df_class(int n_groups, const int2 *groups, const skg_pattern *pat
     k_rows_ke_df<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
                                                               pat->rec.get(), Ke, s_ptr, values);
     SKG_LAUNCH_CHECK("rows_ke_df");
+}
+
+// Row pass over FP32 element matrices (SKG_SPLIT_FP32): rows of 10 floats
+// added into double-float slots, converted to FP64 at write-out; otherwise as
+// k_rows_ke_df (40-byte rows: half the element-matrix bytes).
+template <int SLOTS, int P>
+__global__ void __launch_bounds__(kRowWarps * 32) k_rows_ke_f32(int n_groups, const int2 *__restrict__ groups,
+                                                               const int32_t *__restrict__ indptr,
+                                                               const int32_t *__restrict__ inc_ptr,
+                                                               const int4 *__restrict__ rec,
+                                                               const float *__restrict__ Ke,
+                                                               const int *__restrict__ s_ptr,
+                                                               double *__restrict__ values) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kRowWarps + warp;
+    if (gi >= n_groups) return;
+    df64 *acc = reinterpret_cast<df64 *>(smem + (size_t)warp * SLOTS * 8);
+    const int2 grp = groups[gi];
+    const int32_t s0 = indptr[grp.x];
+    const int nslots = indptr[grp.y] - s0;
+    for (int j = lane; j < P * nslots; j += 32) acc[j] = df64{0.f, 0.f};
+    __syncwarp();
+    const int ridx = lane / P, part = lane - (lane / P) * P;
+    const int32_t r = grp.x + ridx;
+    if (ridx < 32 / P && r < grp.y) {
+        const int base = indptr[r] - s0 + part * nslots;
+        const int32_t it1 = inc_ptr[r + 1];
+        int32_t it = inc_ptr[r] + part;
+        if (it < it1) {
+            // records two incidences ahead of the rows they address, rows one
+            int4 rc = rec[it];
+            int4 rcn = it + P < it1 ? rec[it + P] : make_int4(0, 0, 0, 0);
+            float2 cur[5];
+            {
+                const float2 *src = reinterpret_cast<const float2 *>(Ke + (int64_t)rc.x * 10);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) cur[q] = __ldg(src + q);
+            }
+            bool first = true;
+            for (; it < it1; it += P) {
+                const bool has_next = it + P < it1;
+                float2 nxt[5];
+                if (has_next) {
+                    const float2 *src = reinterpret_cast<const float2 *>(Ke + (int64_t)rcn.x * 10);
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) nxt[q] = __ldg(src + q);
+                }
+                const int4 rcnn = it + 2 * P < it1 ? rec[it + 2 * P] : make_int4(0, 0, 0, 0);
+                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+                int off[10];
+#pragma unroll
+                for (int bb = 0; bb < 10; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+                if (first) {  // the part's first incidence: its row initialises the slots
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) {
+                        acc[off[2 * q]] = df64{cur[q].x, 0.f};
+                        acc[off[2 * q + 1]] = df64{cur[q].y, 0.f};
+                    }
+                    first = false;
+                } else {
+                    df64 a[10];
+#pragma unroll
+                    for (int bb = 0; bb < 10; ++bb) a[bb] = acc[off[bb]];
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) {
+                        df_acc(a[2 * q], df64{cur[q].x, 0.f});
+                        df_acc(a[2 * q + 1], df64{cur[q].y, 0.f});
+                    }
+#pragma unroll
+                    for (int bb = 0; bb < 10; ++bb) acc[off[bb]] = a[bb];
+                }
+                if (has_next) {
+                    rc = rcn;
+                    rcn = rcnn;
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) cur[q] = nxt[q];
+                }
+            }
+        }
+    }
+    __syncwarp();
+    const int sc = *s_ptr;
+    for (int j = lane; j < nslots; j += 32) {
+        df64 v = fast_two_sum(acc[j].hi, acc[j].lo);
+#pragma unroll
+        for (int c = 1; c < P; ++c) v = df_add(v, fast_two_sum(acc[c * nslots + j].hi, acc[c * nslots + j].lo));
+        values[s0 + j] = df_to_double(v, sc);
+    }
+}
+
+template <int SLOTS, int P>
+void launch_ke_f32_class(int n_groups, const int2 *groups, const skg_pattern *pat, const float *Ke, const int *s_ptr,
+                         double *values, cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)kRowWarps * SLOTS * 8;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_rows_ke_f32<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kRowWarps - 1) / kRowWarps);
+    k_rows_ke_f32<SLOTS, P><<<grid, kRowWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(), pat->inc_ptr.get(),
+                                                               pat->rec.get(), Ke, s_ptr, values);
+    SKG_LAUNCH_CHECK("rows_ke_f32");
 }
 
 // Fallback row pass (patterns without row blocks): thread per row, global
@@ -1194,18 +1438,34 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
     int mode = precision == SKG_FP64 ? MODE_FP64 : precision == SKG_SPLIT_FP32 ? MODE_SPLIT : MODE_DF64;
     if (!blocked) mode = MODE_FP64;
     DevBuf<int> misc(2, s);  // [0] scale exponent, [1] range flag
-    if (mode == MODE_DF64 && exact) {
-        // P2, exact rule, double-float: element matrices, then row sums (the
-        // split mode keeps the row-by-row evaluation, which is faster there)
+    if (mode != MODE_FP64 && exact) {
+        // P2, exact rule, FP32 pairs: element matrices (double-float entries
+        // for SKG_FP64_EMULATED, FP32 entries summed in FP32 for
+        // SKG_SPLIT_FP32), then the row sums in double-float slots
         const int init[2] = {INT_MIN, 0};
         SKG_CUDA(cudaMemcpyAsync(misc.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
         k_scale<<<2 * kSmCount, 256, 0, s>>>(d_p, 3 * npts, misc.get());
         SKG_LAUNCH_CHECK("scale");
-        DevBuf<float2> Kf((size_t)ne * 100, s);
+        DevBuf<float2> Kf(mode == MODE_DF64 ? (size_t)ne * 100 : 0, s);
+        DevBuf<float> Kh(mode == MODE_SPLIT ? (size_t)ne * 100 : 0, s);
+        DevBuf<uint8_t> redo(mode == MODE_DF64 ? (size_t)grid_for(ne, kKeBlock) : 0, s);  // tiles left to k_elem_ke_df64
         if (ev) SKG_CUDA(cudaEventRecord(ev[0], s));
         if (ne) {
-            k_elem_ke_df64<MODE_DF64><<<grid_for(ne, kKeBlock), kKeBlock, 0, s>>>(
-                ne, d_p, npts, d_t, coef_kind, d_coef, misc.get(), Kf.get(), misc.get() + 1);
+            if (mode == MODE_DF64) {
+                const unsigned tiles = grid_for(ne, kKeBlock);
+                SKG_CUDA(cudaMemsetAsync(redo.get(), 0, tiles, s));
+                SKG_CUDA(cudaFuncSetAttribute(k_elem_ke_df64_packed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              kPackedSmem));
+                k_elem_ke_df64_packed<<<tiles, kKeBlock, kPackedSmem, s>>>(
+                    ne, d_p, npts, d_t, coef_kind, d_coef, misc.get(), Kf.get(), misc.get() + 1, redo.get());
+                SKG_LAUNCH_CHECK("elem_ke_df64_packed");
+                k_elem_ke_df64<MODE_DF64><<<std::min<unsigned>((tiles + kKeBlock - 1) / kKeBlock, 2 * kSmCount),
+                                            kKeBlock, 0, s>>>(
+                    ne, d_p, npts, d_t, coef_kind, d_coef, misc.get(), Kf.get(), misc.get() + 1, redo.get());
+            }
+            else
+                k_elem_ke_split<<<grid_for(ne, kKeBlock), kKeBlock, 0, s>>>(ne, d_p, npts, d_t, coef_kind, d_coef,
+                                                                             misc.get(), Kh.get(), misc.get() + 1);
             SKG_LAUNCH_CHECK("elem_ke_df64");
         }
         int h_misc[2];
@@ -1214,8 +1474,17 @@ void affine_assemble(const skg_pattern *pat, const double *d_p, int64_t npts, co
         if (h_misc[1] == 0 && h_misc[0] != INT_MIN) {
             if (ev) SKG_CUDA(cudaEventRecord(ev[1], s));
             run_row_pass(pat, d_values, h_values, s, [&](const GroupSet &gs, cudaStream_t st) {
-                launch_ke_df_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kf.get(), misc.get(), d_values, st);
-                launch_ke_df_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kf.get(), misc.get(), d_values, st);
+                if (mode == MODE_DF64) {
+                    launch_ke_df_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kf.get(), misc.get(), d_values,
+                                                            st);
+                    launch_ke_df_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kf.get(), misc.get(), d_values,
+                                                            st);
+                } else {
+                    launch_ke_f32_class<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, Kh.get(), misc.get(),
+                                                             d_values, st);
+                    launch_ke_f32_class<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, Kh.get(), misc.get(),
+                                                             d_values, st);
+                }
             });
             if (ev) SKG_CUDA(cudaEventRecord(ev[2], s));
             return;

@@ -31,13 +31,13 @@ def _rule4():
     return np.array([[a, b, b, b], [b, a, b, b], [b, b, a, b]]), np.full(4, 1.0 / 24.0)
 
 
-def _tensors(E, rng):
+def _tensors(E, rng, scale=1.0):
     A = rng.standard_normal((3, 3, E))
-    A = np.ascontiguousarray(np.einsum("ije,kje->ike", A, A) + 3.0 * np.eye(3)[:, :, None])
+    A = np.ascontiguousarray(np.einsum("ije,kje->ike", A, A) + 3.0 * np.eye(3)[:, :, None]) * scale
     return dev.to_device(A, np.float64)
 
 
-def _problem(n, quadratic, seed, scale=1.0):
+def _problem(n, quadratic, seed, scale=1.0, coef_scale=1.0):
     rng = np.random.default_rng(seed)
     m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
     p = m.p.copy()
@@ -49,7 +49,7 @@ def _problem(n, quadratic, seed, scale=1.0):
     X, W = _rule4()
     elem = sk.ElementTetP2() if quadratic else sk.ElementTetP1()
     basis = sk.Basis(mesh, sk.ElementVector(elem, dim=1), quadrature=(X, W))
-    return mesh, basis, X, W, _tensors(mesh.nelements, rng)
+    return mesh, basis, X, W, _tensors(mesh.nelements, rng, coef_scale)
 
 
 def _fan(k, seed):
@@ -100,10 +100,19 @@ def test_no_alloc_matches_allocating_entry_point(quadratic, precision):
 
 
 @pytest.mark.parametrize("precision", [SKG_FP64_EMULATED, SKG_SPLIT_FP32])
+def test_no_alloc_mesh_far_from_unit_scale(precision):
+    """A mesh scaled by 1e40: the FP32-pair modes work in coordinates rescaled
+    by a power of two, so both entry points stay in their mode (each within
+    the mode's accuracy of the other)."""
+    rtol = 1e-7 if precision == SKG_SPLIT_FP32 else RTOL
+    _compare(*_problem(4, True, 5, scale=1e40), precision, rtol)
+
+
+@pytest.mark.parametrize("precision", [SKG_FP64_EMULATED, SKG_SPLIT_FP32])
 def test_no_alloc_out_of_fp32_range_falls_back_to_fp64(precision):
-    """A mesh scaled by 1e40 leaves FP32 range: both entry points detect it
-    and assemble in FP64 instead."""
-    _compare(*_problem(4, True, 5, scale=1e40), precision, RTOL)
+    """A coefficient scaled by 1e40 leaves FP32 range: both entry points detect
+    it and assemble in FP64 instead."""
+    _compare(*_problem(4, True, 5, coef_scale=1e40), precision, RTOL)
 
 
 def test_no_alloc_unblocked_pattern():
