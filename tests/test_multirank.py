@@ -47,3 +47,23 @@ def test_single_rank_is_identity():
     import bench
 
     assert bench.reduce_max(3.25, 1) == 3.25
+
+
+def test_reference_arm_under_two_ranks_prints_one_line():
+    """`bench.py --impl reference` launched as two ranks (as the scaling runs
+    launch it): rank 0 alone runs the CPU oracle and prints the one JSON line,
+    rank 1 exits 0 without work."""
+    import json
+    import subprocess
+
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
+           os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--cells", "6", "--steps", "1",
+           "--warmup", "1"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["one_thread"]["value"] > 0
