@@ -102,12 +102,47 @@ __device__ __forceinline__ void flush_stage(const float4 *stage, float4 *Gout, i
     for (int i = threadIdx.x; i < nvalid * 8; i += kElemBlock) dst[i] = stage[(i >> 3) * kStagePad + (i & 7)];
 }
 
+// Off-diagonal pair (a, b) of a coefficient whose largest diagonal entry has
+// biased exponent emax, decided on the bits: same sign, finite, and at most
+// 2^(emax - e + 5) units in the last place apart, e the larger biased exponent
+// of the pair (at least 1).  Then |a - b| <= 2^(emax - 1070) < 1e-14 |A_dd|,
+// so a pair that passes also passes the floating-point test of
+// coef_symmetric; a pair that fails goes to that test.  Integer instructions
+// only, in place of FP64 additions, a multiplication and comparisons on the
+// FP64 pipe.
+__device__ __forceinline__ bool bits_close(double a, double b, int emax) {
+    const unsigned long long ia = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ib = (unsigned long long)__double_as_longlong(b);
+    const unsigned long long ma = ia & 0x7fffffffffffffffull, mb = ib & 0x7fffffffffffffffull;
+    const int e = max(max((int)(ma >> 52), (int)(mb >> 52)), 1);
+    if (((ia ^ ib) >> 63) != 0 || e == 0x7ff || emax == 0x7ff) return false;
+    const unsigned long long d = ma > mb ? ma - mb : mb - ma;
+    const int sh = emax - e + 5;
+    if (sh < 0) return d == 0;
+    return sh >= 63 || d <= (1ull << sh);
+}
+
+// A (3 x 3, row-major) symmetric to 1e-14 of its size: |A_kl - A_lk| <=
+// 1e-14 (|A_00| + |A_11| + |A_22| + |A_01| + |A_02| + |A_12|) for the three
+// off-diagonal pairs (a tensor built as Q D Q^T in floating point is not
+// bitwise symmetric; mirroring K_ab into K_ba then changes entries by ~1e-16
+// relative).  The bit test decides first; the same decision as the
+// floating-point test alone.
+__device__ __forceinline__ bool coef_symmetric(const double A[9]) {
+    const auto bexp = [](double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); };
+    const int emax = max(max(bexp(A[0]), bexp(A[4])), bexp(A[8]));
+    if (bits_close(A[1], A[3], emax) && bits_close(A[2], A[6], emax) && bits_close(A[5], A[7], emax)) return true;
+    const double scale = 1e-14 * (fabs(A[0]) + fabs(A[4]) + fabs(A[8]) + fabs(A[1]) + fabs(A[2]) + fabs(A[5]));
+    return fabs(A[1] - A[3]) <= scale && fabs(A[2] - A[6]) <= scale && fabs(A[5] - A[7]) <= scale;
+}
+
 // G_kl = b_k . A b_l / |det J| of element e in FP64 (b: adjugate rows, the
 // scaled barycentric gradients).  Only the block k, l >= 1 takes dot products
 // (its upper triangle when A is symmetric): b_0 = -(b_1 + b_2 + b_3) gives
-// G_0l = -(G_1l + G_2l + G_3l), G_k0 likewise and G_00 = -(G_01 + G_02 + G_03),
-// and gscale / |det J| scales the coefficient, not the 16 results.  Returns the
-// element's symmetry (scalar coefficient, or a tensor equal to its transpose).
+// G_0l = -(G_1l + G_2l + G_3l), G_k0 likewise and G_00 = -(G_01 + G_02 + G_03);
+// gscale / |det J| scales the dot products of that block (6 of them when A
+// is symmetric, where scaling A would take 9).  Returns the element's
+// symmetry (scalar coefficient, or a tensor equal to its transpose).
 __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict__ p, int64_t npts,
                                             const int32_t *__restrict__ t, int coef_kind,
                                             const double *__restrict__ coef, int64_t e, double g[16],
@@ -148,12 +183,7 @@ __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict
         double A[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) A[k] = load_coef(coef, coef_kind, ne, e, k);
-        // symmetric to rounding (A built as Q D Q^T in floating point is not bitwise
-        // symmetric): mirroring K_ab into K_ba then changes entries by ~1e-16 relative
-        const double scale = 1e-14 * (fabs(A[0]) + fabs(A[4]) + fabs(A[8]) + fabs(A[1]) + fabs(A[2]) + fabs(A[5]));
-        sym = fabs(A[1] - A[3]) <= scale && fabs(A[2] - A[6]) <= scale && fabs(A[5] - A[7]) <= scale;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) A[k] *= inv;
+        sym = coef_symmetric(A);
 #pragma unroll
         for (int l = 1; l < 4; ++l) {
             double Ab[3];
@@ -162,7 +192,7 @@ __device__ __forceinline__ bool elem_g_fp64(int64_t ne, const double *__restrict
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
                 if (k > l && sym) continue;  // mirrored below
-                g[k * 4 + l] = b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2];
+                g[k * 4 + l] = inv * (b[k][0] * Ab[0] + b[k][1] * Ab[1] + b[k][2] * Ab[2]);
             }
         }
         if (sym) {
@@ -356,9 +386,7 @@ __device__ __forceinline__ bool elem_g_df64(int64_t ne, const double *__restrict
         double Ad[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) Ad[k] = load_coef(coef, coef_kind, ne, e, k);
-        const double scale =
-            1e-14 * (fabs(Ad[0]) + fabs(Ad[4]) + fabs(Ad[8]) + fabs(Ad[1]) + fabs(Ad[2]) + fabs(Ad[5]));
-        sym = fabs(Ad[1] - Ad[3]) <= scale && fabs(Ad[2] - Ad[6]) <= scale && fabs(Ad[5] - Ad[7]) <= scale;
+        sym = coef_symmetric(Ad);
         df64 A[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) A[k] = df_mul(inv, df_from_double(Ad[k], 0, ok));

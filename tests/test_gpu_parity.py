@@ -350,6 +350,64 @@ def test_device_resident_csr_handoff():
     assert relerr(yn, Kn @ xn) < 1e-13
 
 
+def _asymmetry_cases():
+    """Per-element tensors around the symmetry tolerance |A_kl - A_lk| <=
+    1e-14 (|A_00| + |A_11| + |A_22| + |A_01| + |A_02| + |A_12|)."""
+    base = np.array([[2.0, 0.3, 0.1], [0.3, 1.5, 0.2], [0.1, 0.2, 1.2]])
+    size = np.abs(base[np.triu_indices(3)]).sum()
+    cases = {"exact": base.copy()}
+    a = base.copy()
+    a[1, 0] = np.nextafter(np.nextafter(np.nextafter(a[0, 1], 1.0), 1.0), 1.0)  # 3 units in the last place
+    cases["ulps"] = a
+    a = base.copy()
+    a[0, 2], a[2, 0] = 1e-20, -1e-20  # opposite signs, far inside the tolerance
+    cases["tiny_opposite"] = a
+    a = base.copy()
+    a[0, 1], a[1, 0] = 0.0, -0.0
+    cases["signed_zeros"] = a
+    a = base.copy()
+    a[2, 1] = a[1, 2] + 0.9e-14 * size  # inside, beyond what the bit test accepts
+    cases["inside"] = a
+    a = base.copy()
+    a[2, 1] = a[1, 2] + 1.1e-14 * size
+    cases["outside"] = a
+    a = base.copy()
+    a[1, 0] = a[0, 1] * (1 + 2.0 ** -40)
+    cases["outside_relative"] = a
+    return cases
+
+
+def _symmetric_to_tolerance(A):
+    scale = 1e-14 * (abs(A[0, 0]) + abs(A[1, 1]) + abs(A[2, 2]) + abs(A[0, 1]) + abs(A[0, 2]) + abs(A[1, 2]))
+    return bool(abs(A[0, 1] - A[1, 0]) <= scale and abs(A[0, 2] - A[2, 0]) <= scale
+                and abs(A[1, 2] - A[2, 1]) <= scale)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_emulated", "split_fp32"])
+def test_p2_coefficient_symmetry_decision(precision):
+    """The element pass mirrors the upper triangle exactly when the element's
+    tensor is symmetric to 1e-14 of its size (a bit-level test first, the
+    floating-point test when that one fails; the same decision).  One tet per
+    case: the assembled 10 x 10 matrix is exactly symmetric where mirrored;
+    in FP64 an unmirrored one shows its tensor's asymmetry."""
+    from skfemntv_gb300.assembly import NativeTensorForm
+
+    g = load_golden("p2_aniso")
+    m = sk.MeshTet(np.array([[0.0, 1.0, 0.1, 0.2], [0.0, 0.1, 0.9, 0.3], [0.0, 0.2, 0.1, 1.1]]),
+                   np.array([[0], [1], [2], [3]]))
+    b = sk.Basis(sk.MeshTet2.from_mesh(m), sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(g["X"], g["W"]))
+    form = NativeTensorForm(b)
+    for name, A in _asymmetry_cases().items():
+        expect = _symmetric_to_tolerance(A)
+        assert expect == (name not in ("outside", "outside_relative")), name
+        K = form.assemble(np.broadcast_to(A[:, :, None, None], (3, 3, 1, 4)), precision=precision).toarray()
+        mirrored = bool(np.array_equal(K, K.T))
+        if expect:
+            assert mirrored, (precision, name)
+        elif precision == "fp64":
+            assert not mirrored, name
+
+
 def _mixed_orientation_meshes():
     axis = np.linspace(0.0, 1.0, 3)
     original = sk.MeshTet.init_tensor(axis, axis, axis)
