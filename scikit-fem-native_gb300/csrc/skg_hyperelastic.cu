@@ -207,125 +207,267 @@ __device__ __forceinline__ df64 df_split(double v) {
 // surrogate records (FP32 entries, double-float slot sums) with plain FP64
 // records for the elements flagged as fallback; otherwise plain records and
 // FP64 slot sums.
+//
+// With `fallbacks` (the call's count of elements sent to the plain law) the
+// kernel runs only when that count is nonzero, k_nh_rows_f32 otherwise; its
+// warps then take groups grid-stride, so that the launch that finds nothing
+// to do is a small grid.
 template <bool SUR, int SLOTS, int P>
 __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
     int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
     const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec_inc, const double *__restrict__ recd,
-    const float *__restrict__ recf, const unsigned char *__restrict__ flags, double *__restrict__ residual,
-    double *__restrict__ values) {
+    const float *__restrict__ recf, const unsigned char *__restrict__ flags,
+    const unsigned long long *__restrict__ fallbacks, double *__restrict__ residual, double *__restrict__ values) {
+    if (fallbacks && *fallbacks == 0) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *accd = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
+    df64 *accf = reinterpret_cast<df64 *>(accd);
+    for (int gi = blockIdx.x * kNhWarps + warp; gi < n_groups; gi += gridDim.x * kNhWarps) {
+        const int2 grp = groups[gi];
+        const int32_t s0 = indptr[grp.x];
+        const int nslots = indptr[grp.y] - s0;
+        for (int j = lane; j < P * nslots; j += 32) {
+            if constexpr (SUR) accf[j] = df64{0.f, 0.f};
+            else accd[j] = 0.0;
+        }
+        __syncwarp();
+        const int ridx = lane / P, part = lane - (lane / P) * P;
+        const int32_t r = grp.x + ridx;
+        const bool live = ridx < 32 / P && r < grp.y;
+        double rd = 0.0;
+        df64 rf{0.f, 0.f};
+        if (live) {
+            const int base = indptr[r] - s0 + part * nslots;
+            const int32_t it1 = inc_ptr[r + 1];
+            int32_t it = inc_ptr[r] + part;
+            int4 rcn = it < it1 ? rec_inc[it] : make_int4(0, 0, 0, 0);  // records one incidence ahead
+            for (; it < it1; it += P) {
+                const int4 rc = rcn;
+                if (it + P < it1) rcn = rec_inc[it + P];
+                const int32_t e = rc.x / 12;
+                const int l = rc.x - e * 12;
+                const int a = l / 3, i = l - 3 * (l / 3);
+                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+                int off[12];
+    #pragma unroll
+                for (int bb = 0; bb < 12; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+                if (!SUR || flags[e]) {
+                    double val[12], rr;
+                    nh_plain_row(recd + (int64_t)e * kNhRecD, a, i, val, rr);
+                    if constexpr (SUR) {
+                        df64 acc[12];
+    #pragma unroll
+                        for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
+    #pragma unroll
+                        for (int bb = 0; bb < 12; ++bb) accf[off[bb]] = df_add(acc[bb], df_split(val[bb]));
+                        rf = df_add(rf, df_split(rr));
+                    } else {
+                        double acc[12];
+    #pragma unroll
+                        for (int bb = 0; bb < 12; ++bb) acc[bb] = accd[off[bb]];
+    #pragma unroll
+                        for (int bb = 0; bb < 12; ++bb) accd[off[bb]] = acc[bb] + val[bb];
+                        rd += rr;
+                    }
+                } else {
+                    float val[12], rr;
+                    nh_surrogate_row(recf + (int64_t)e * kNhRecF, a, i, val, rr);
+                    df64 acc[12];
+    #pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
+    #pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) {
+                        const df64 sm = two_sum(acc[bb].hi, val[bb]);
+                        accf[off[bb]] = df64{sm.hi, acc[bb].lo + sm.lo};
+                    }
+                    const df64 sm = two_sum(rf.hi, rr);
+                    rf = df64{sm.hi, rf.lo + sm.lo};
+                }
+            }
+        }
+        // residual: combine the P parts of each row (lane order), part 0 writes
+        if constexpr (P == 2) {
+            if constexpr (SUR) {
+                const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
+                rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
+            } else {
+                rd += __shfl_down_sync(0xffffffffu, rd, 1);
+            }
+        }
+        if (live && part == 0 && residual) {
+            if constexpr (SUR) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
+            else residual[r] = rd;
+        }
+        __syncwarp();
+        if (values) {
+            for (int j = lane; j < nslots; j += 32) {
+                if constexpr (SUR) {
+                    // copies summed in double-float, converted by integer arithmetic (no FP64 pipe)
+                    df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
+    #pragma unroll
+                    for (int c = 1; c < P; ++c)
+                        v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
+                    values[s0 + j] = df_to_double(v, 0);
+                } else {
+                    double v = accd[j];
+    #pragma unroll
+                    for (int c = 1; c < P; ++c) v += accd[c * nslots + j];
+                    values[s0 + j] = v;
+                }
+            }
+        }
+        __syncwarp();  // the slots are zeroed again for the next group
+    }
+}
+
+// Exact float -> double by integer arithmetic (FP32 subnormals through the
+// conversion instruction: they do not occur in practice).
+__device__ __forceinline__ double float_to_double_exact(float v) {
+    const unsigned b = __float_as_uint(v);
+    if ((b & 0x7f800000u) == 0 && (b & 0x7fffffu) != 0) return (double)v;
+    return __longlong_as_double((long long)float_to_double_bits(v, 0));
+}
+
+// Surrogate row pass of a call in which no element fell back to the plain
+// law (`*fallbacks` == 0; otherwise k_nh_rows runs instead): every incidence
+// adds a precomputed FP32 tangent row, summed in FP32 slots (the network's
+// own error, ~1e-5, is far above FP32 rounding), half the shared memory of
+// double-float slots and so twice the resident warps; the residual entries in
+// double-float registers.  Records run two incidences ahead of the rows they
+// address, rows one (as k_rows_ke); each thread part's first incidence stores
+// its row.  One warp per row group.
+template <int SLOTS, int P>
+__global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows_f32(
+    int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
+    const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec_inc, const float *__restrict__ recf,
+    const unsigned long long *__restrict__ fallbacks, double *__restrict__ residual, double *__restrict__ values) {
+    if (*fallbacks != 0) return;
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gi = blockIdx.x * kNhWarps + warp;
     if (gi >= n_groups) return;
-    double *accd = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
-    df64 *accf = reinterpret_cast<df64 *>(accd);
+    float *acc = reinterpret_cast<float *>(smem + (size_t)warp * SLOTS * 4);
     const int2 grp = groups[gi];
     const int32_t s0 = indptr[grp.x];
     const int nslots = indptr[grp.y] - s0;
-    for (int j = lane; j < P * nslots; j += 32) {
-        if constexpr (SUR) accf[j] = df64{0.f, 0.f};
-        else accd[j] = 0.0;
-    }
+    for (int j = lane; j < P * nslots; j += 32) acc[j] = 0.f;
     __syncwarp();
     const int ridx = lane / P, part = lane - (lane / P) * P;
     const int32_t r = grp.x + ridx;
     const bool live = ridx < 32 / P && r < grp.y;
-    double rd = 0.0;
     df64 rf{0.f, 0.f};
+    // row l = 3a + i of element e: 12 FP32 tangent entries and the residual entry
+    const auto load_row = [&](int32_t item, float v[12], float &rr) {
+        const int32_t e = item / 12;
+        const int l = item - e * 12;
+        const float *R = recf + (int64_t)e * kNhRecF;
+        const float4 *src = reinterpret_cast<const float4 *>(R + 12 * l);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float4 w = __ldg(src + q);
+            v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
+        }
+        rr = __ldg(R + 144 + l);
+    };
     if (live) {
         const int base = indptr[r] - s0 + part * nslots;
         const int32_t it1 = inc_ptr[r + 1];
         int32_t it = inc_ptr[r] + part;
-        int4 rcn = it < it1 ? rec_inc[it] : make_int4(0, 0, 0, 0);  // records one incidence ahead
-        for (; it < it1; it += P) {
-            const int4 rc = rcn;
-            if (it + P < it1) rcn = rec_inc[it + P];
-            const int32_t e = rc.x / 12;
-            const int l = rc.x - e * 12;
-            const int a = l / 3, i = l - 3 * (l / 3);
-            const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
-            int off[12];
+        if (it < it1) {
+            int4 rc = rec_inc[it];
+            int4 rcn = it + P < it1 ? rec_inc[it + P] : make_int4(0, 0, 0, 0);
+            float cur[12], crr;
+            load_row(rc.x, cur, crr);
+            bool first = true;
+            for (; it < it1; it += P) {
+                const bool has_next = it + P < it1;
+                float nxt[12], nrr = 0.f;
+                if (has_next) load_row(rcn.x, nxt, nrr);
+                const int4 rcnn = it + 2 * P < it1 ? rec_inc[it + 2 * P] : make_int4(0, 0, 0, 0);
+                const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
+                int off[12];
 #pragma unroll
-            for (int bb = 0; bb < 12; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-            if (!SUR || flags[e]) {
-                double val[12], rr;
-                nh_plain_row(recd + (int64_t)e * kNhRecD, a, i, val, rr);
-                if constexpr (SUR) {
-                    df64 acc[12];
+                for (int bb = 0; bb < 12; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
+                if (first) {
+                    // an element's columns are distinct slots: no add needed
 #pragma unroll
-                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
-#pragma unroll
-                    for (int bb = 0; bb < 12; ++bb) accf[off[bb]] = df_add(acc[bb], df_split(val[bb]));
-                    rf = df_add(rf, df_split(rr));
+                    for (int bb = 0; bb < 12; ++bb) acc[off[bb]] = cur[bb];
+                    first = false;
                 } else {
-                    double acc[12];
+                    float a[12];
 #pragma unroll
-                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accd[off[bb]];
+                    for (int bb = 0; bb < 12; ++bb) a[bb] = acc[off[bb]];
 #pragma unroll
-                    for (int bb = 0; bb < 12; ++bb) accd[off[bb]] = acc[bb] + val[bb];
-                    rd += rr;
+                    for (int bb = 0; bb < 12; ++bb) acc[off[bb]] = a[bb] + cur[bb];
                 }
-            } else {
-                float val[12], rr;
-                nh_surrogate_row(recf + (int64_t)e * kNhRecF, a, i, val, rr);
-                df64 acc[12];
-#pragma unroll
-                for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
-#pragma unroll
-                for (int bb = 0; bb < 12; ++bb) {
-                    const df64 sm = two_sum(acc[bb].hi, val[bb]);
-                    accf[off[bb]] = df64{sm.hi, acc[bb].lo + sm.lo};
-                }
-                const df64 sm = two_sum(rf.hi, rr);
+                const df64 sm = two_sum(rf.hi, crr);
                 rf = df64{sm.hi, rf.lo + sm.lo};
+                if (has_next) {
+                    rc = rcn;
+                    rcn = rcnn;
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) cur[bb] = nxt[bb];
+                    crr = nrr;
+                }
             }
         }
     }
     // residual: combine the P parts of each row (lane order), part 0 writes
     if constexpr (P == 2) {
-        if constexpr (SUR) {
-            const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
-            rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
-        } else {
-            rd += __shfl_down_sync(0xffffffffu, rd, 1);
-        }
+        const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
+        rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
     }
-    if (live && part == 0 && residual) {
-        if constexpr (SUR) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
-        else residual[r] = rd;
-    }
+    if (live && part == 0 && residual) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
     __syncwarp();
     if (values) {
         for (int j = lane; j < nslots; j += 32) {
-            if constexpr (SUR) {
-                // copies summed in double-float, converted by integer arithmetic (no FP64 pipe)
-                df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
+            float v = acc[j];
 #pragma unroll
-                for (int c = 1; c < P; ++c)
-                    v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
-                values[s0 + j] = df_to_double(v, 0);
-            } else {
-                double v = accd[j];
-#pragma unroll
-                for (int c = 1; c < P; ++c) v += accd[c * nslots + j];
-                values[s0 + j] = v;
-            }
+            for (int c = 1; c < P; ++c) v += acc[c * nslots + j];
+            values[s0 + j] = float_to_double_exact(v);
         }
     }
 }
 
+template <int SLOTS, int P>
+void launch_nh_rows_f32(int n_groups, const int2 *groups, const skg_pattern *pat, const float *recf,
+                        const unsigned long long *fallbacks, double *residual, double *values, cudaStream_t s) {
+    if (n_groups == 0) return;
+    const size_t smem = (size_t)kNhWarps * SLOTS * 4;
+    if (smem > 48 * 1024)
+        SKG_CUDA(cudaFuncSetAttribute(k_nh_rows_f32<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    const unsigned grid = (unsigned)((n_groups + kNhWarps - 1) / kNhWarps);
+    k_nh_rows_f32<SLOTS, P><<<grid, kNhWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
+                                                              pat->inc_ptr.get(), pat->rec.get(), recf, fallbacks,
+                                                              residual, values);
+    SKG_LAUNCH_CHECK("nh_rows_f32");
+}
+
+// With `fallbacks`: one wave of resident CTAs taking the groups grid-stride
+// (the launch is a no-op when no element fell back).
 template <bool SUR, int SLOTS, int P>
 void launch_nh_rows(int n_groups, const int2 *groups, const skg_pattern *pat, const double *recd, const float *recf,
-                    const unsigned char *flags, double *residual, double *values, cudaStream_t s) {
+                    const unsigned char *flags, const unsigned long long *fallbacks, double *residual,
+                    double *values, cudaStream_t s) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kNhWarps * SLOTS * 8;
     if (smem > 48 * 1024)
         SKG_CUDA(cudaFuncSetAttribute(k_nh_rows<SUR, SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    const unsigned grid = (unsigned)((n_groups + kNhWarps - 1) / kNhWarps);
+    unsigned grid = (unsigned)((n_groups + kNhWarps - 1) / kNhWarps);
+    if (fallbacks) {
+        static int resident = 0;  // CTAs per SM, per instantiation (same on every GB300)
+        if (!resident)
+            SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nh_rows<SUR, SLOTS, P>,
+                                                                   kNhWarps * 32, smem));
+        const unsigned wave = (unsigned)(resident > 0 ? resident : 1) * kSmCount;
+        if (grid > wave) grid = wave;
+    }
     k_nh_rows<SUR, SLOTS, P><<<grid, kNhWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
                                                               pat->inc_ptr.get(), pat->rec.get(), recd, recf, flags,
-                                                              residual, values);
+                                                              fallbacks, residual, values);
     SKG_LAUNCH_CHECK("nh_rows");
 }
 
@@ -343,9 +485,15 @@ __global__ void k_vector_gather(int64_t n_rows, const int32_t *__restrict__ inc_
 }  // namespace
 
 void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, const float *recf,
-             const unsigned char *flags, double *d_residual, double *d_values, cudaStream_t s) {
-    launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, d_residual, d_values, s);
-    launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, d_residual, d_values, s);
+             const unsigned char *flags, const unsigned long long *fallbacks, double *d_residual, double *d_values,
+             cudaStream_t s) {
+    // FP32 slots when no element fell back, double-float slots otherwise (each kernel reads the count)
+    launch_nh_rows_f32<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recf, fallbacks, d_residual, d_values, s);
+    launch_nh_rows_f32<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recf, fallbacks, d_residual, d_values, s);
+    launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, fallbacks, d_residual,
+                                              d_values, s);
+    launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, fallbacks, d_residual,
+                                              d_values, s);
 }
 
 // Whole-array copies of the results to the host (paths without row chunks).

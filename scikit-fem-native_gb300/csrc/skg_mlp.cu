@@ -1350,7 +1350,7 @@ void nh_assemble_surrogate(const skg_pattern *pat, const double *d_p, int64_t np
                 SKG_LAUNCH_CHECK("nh_surrogate_finish");
             },
             [&](const GroupSet &gs, cudaStream_t st) {
-                nh_rows(pat, gs, recd.get(), recf.get(), flags.get(), d_residual, d_values, st);
+                nh_rows(pat, gs, recd.get(), recf.get(), flags.get(), fb.get(), d_residual, d_values, st);
             },
             d_residual, h_residual);
     } else {

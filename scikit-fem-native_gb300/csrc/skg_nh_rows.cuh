@@ -39,8 +39,11 @@ __device__ __forceinline__ void write_plain_record(const NhGeom &g, const NhLaw 
     r[35] = lmbda * g.V;
 }
 
+// Surrogate row pass; `fallbacks` (device) counts the call's elements sent
+// to the plain law: FP32 slots when it is zero, double-float slots otherwise.
 void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, const float *recf,
-             const unsigned char *flags, double *d_residual, double *d_values, cudaStream_t s);
+             const unsigned char *flags, const unsigned long long *fallbacks, double *d_residual, double *d_values,
+             cudaStream_t s);
 
 // Residual and tangent from per-element arrays (patterns without row groups).
 void nh_gather(const skg_pattern *pat, const double *Ke, const double *re, double *d_residual, double *d_values,
