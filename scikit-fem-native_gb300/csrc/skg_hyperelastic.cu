@@ -201,18 +201,19 @@ __device__ __forceinline__ df64 df_split(double v) {
     return df64{h, (float)(v - (double)h)};
 }
 
-// Row groups as in the affine row pass: one warp per group of CSR rows, P
-// threads per row walking its incidences in element order, per-copy slot
-// sums in shared memory, summed in copy order and written coalesced.  SUR:
-// surrogate records (FP32 entries, double-float slot sums) with plain FP64
-// records for the elements flagged as fallback; otherwise plain records and
-// FP64 slot sums.
+// Surrogate row pass with fallbacks: row groups as in the affine row pass
+// (one warp per group of CSR rows, P threads per row walking its incidences
+// in element order, per-copy slot sums in shared memory, summed in copy order
+// and written coalesced); the FP32 surrogate rows and, for the elements
+// flagged as fallback, the FP64 plain rows from their records, summed in
+// double-float slots (a call in which every element falls back gives the
+// plain law's values to ~1e-14).
 //
 // With `fallbacks` (the call's count of elements sent to the plain law) the
 // kernel runs only when that count is nonzero, k_nh_rows_f32 otherwise; its
 // warps then take groups grid-stride, so that the launch that finds nothing
 // to do is a small grid.
-template <bool SUR, int SLOTS, int P>
+template <int SLOTS, int P>
 __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
     int n_groups, const int2 *__restrict__ groups, const int32_t *__restrict__ indptr,
     const int32_t *__restrict__ inc_ptr, const int4 *__restrict__ rec_inc, const double *__restrict__ recd,
@@ -221,21 +222,16 @@ __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
     if (fallbacks && *fallbacks == 0) return;
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double *accd = reinterpret_cast<double *>(smem + (size_t)warp * SLOTS * 8);
-    df64 *accf = reinterpret_cast<df64 *>(accd);
+    df64 *accf = reinterpret_cast<df64 *>(smem + (size_t)warp * SLOTS * 8);
     for (int gi = blockIdx.x * kNhWarps + warp; gi < n_groups; gi += gridDim.x * kNhWarps) {
         const int2 grp = groups[gi];
         const int32_t s0 = indptr[grp.x];
         const int nslots = indptr[grp.y] - s0;
-        for (int j = lane; j < P * nslots; j += 32) {
-            if constexpr (SUR) accf[j] = df64{0.f, 0.f};
-            else accd[j] = 0.0;
-        }
+        for (int j = lane; j < P * nslots; j += 32) accf[j] = df64{0.f, 0.f};
         __syncwarp();
         const int ridx = lane / P, part = lane - (lane / P) * P;
         const int32_t r = grp.x + ridx;
         const bool live = ridx < 32 / P && r < grp.y;
-        double rd = 0.0;
         df64 rf{0.f, 0.f};
         if (live) {
             const int base = indptr[r] - s0 + part * nslots;
@@ -250,33 +246,24 @@ __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
                 const int a = l / 3, i = l - 3 * (l / 3);
                 const unsigned ow[3] = {(unsigned)rc.y, (unsigned)rc.z, (unsigned)rc.w};
                 int off[12];
-    #pragma unroll
+#pragma unroll
                 for (int bb = 0; bb < 12; ++bb) off[bb] = base + (int)((ow[bb >> 2] >> (8 * (bb & 3))) & 0xffu);
-                if (!SUR || flags[e]) {
+                if (flags[e]) {
                     double val[12], rr;
                     nh_plain_row(recd + (int64_t)e * kNhRecD, a, i, val, rr);
-                    if constexpr (SUR) {
-                        df64 acc[12];
-    #pragma unroll
-                        for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
-    #pragma unroll
-                        for (int bb = 0; bb < 12; ++bb) accf[off[bb]] = df_add(acc[bb], df_split(val[bb]));
-                        rf = df_add(rf, df_split(rr));
-                    } else {
-                        double acc[12];
-    #pragma unroll
-                        for (int bb = 0; bb < 12; ++bb) acc[bb] = accd[off[bb]];
-    #pragma unroll
-                        for (int bb = 0; bb < 12; ++bb) accd[off[bb]] = acc[bb] + val[bb];
-                        rd += rr;
-                    }
+                    df64 acc[12];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
+#pragma unroll
+                    for (int bb = 0; bb < 12; ++bb) accf[off[bb]] = df_add(acc[bb], df_split(val[bb]));
+                    rf = df_add(rf, df_split(rr));
                 } else {
                     float val[12], rr;
                     nh_surrogate_row(recf + (int64_t)e * kNhRecF, a, i, val, rr);
                     df64 acc[12];
-    #pragma unroll
+#pragma unroll
                     for (int bb = 0; bb < 12; ++bb) acc[bb] = accf[off[bb]];
-    #pragma unroll
+#pragma unroll
                     for (int bb = 0; bb < 12; ++bb) {
                         const df64 sm = two_sum(acc[bb].hi, val[bb]);
                         accf[off[bb]] = df64{sm.hi, acc[bb].lo + sm.lo};
@@ -288,33 +275,18 @@ __global__ void __launch_bounds__(kNhWarps * 32) k_nh_rows(
         }
         // residual: combine the P parts of each row (lane order), part 0 writes
         if constexpr (P == 2) {
-            if constexpr (SUR) {
-                const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
-                rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
-            } else {
-                rd += __shfl_down_sync(0xffffffffu, rd, 1);
-            }
+            const float h = __shfl_down_sync(0xffffffffu, rf.hi, 1), lo = __shfl_down_sync(0xffffffffu, rf.lo, 1);
+            rf = df_add(fast_two_sum(rf.hi, rf.lo), fast_two_sum(h, lo));
         }
-        if (live && part == 0 && residual) {
-            if constexpr (SUR) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
-            else residual[r] = rd;
-        }
+        if (live && part == 0 && residual) residual[r] = df_to_double(fast_two_sum(rf.hi, rf.lo), 0);
         __syncwarp();
         if (values) {
             for (int j = lane; j < nslots; j += 32) {
-                if constexpr (SUR) {
-                    // copies summed in double-float, converted by integer arithmetic (no FP64 pipe)
-                    df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
-    #pragma unroll
-                    for (int c = 1; c < P; ++c)
-                        v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
-                    values[s0 + j] = df_to_double(v, 0);
-                } else {
-                    double v = accd[j];
-    #pragma unroll
-                    for (int c = 1; c < P; ++c) v += accd[c * nslots + j];
-                    values[s0 + j] = v;
-                }
+                // copies summed in double-float, converted by integer arithmetic (no FP64 pipe)
+                df64 v = fast_two_sum(accf[j].hi, accf[j].lo);
+#pragma unroll
+                for (int c = 1; c < P; ++c) v = df_add(v, fast_two_sum(accf[c * nslots + j].hi, accf[c * nslots + j].lo));
+                values[s0 + j] = df_to_double(v, 0);
             }
         }
         __syncwarp();  // the slots are zeroed again for the next group
@@ -447,25 +419,25 @@ void launch_nh_rows_f32(int n_groups, const int2 *groups, const skg_pattern *pat
 
 // With `fallbacks`: one wave of resident CTAs taking the groups grid-stride
 // (the launch is a no-op when no element fell back).
-template <bool SUR, int SLOTS, int P>
+template <int SLOTS, int P>
 void launch_nh_rows(int n_groups, const int2 *groups, const skg_pattern *pat, const double *recd, const float *recf,
                     const unsigned char *flags, const unsigned long long *fallbacks, double *residual,
                     double *values, cudaStream_t s) {
     if (n_groups == 0) return;
     const size_t smem = (size_t)kNhWarps * SLOTS * 8;
     if (smem > 48 * 1024)
-        SKG_CUDA(cudaFuncSetAttribute(k_nh_rows<SUR, SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SKG_CUDA(cudaFuncSetAttribute(k_nh_rows<SLOTS, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
     unsigned grid = (unsigned)((n_groups + kNhWarps - 1) / kNhWarps);
     if (fallbacks) {
         static int resident = 0;  // CTAs per SM, per instantiation (same on every GB300)
         if (!resident)
-            SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nh_rows<SUR, SLOTS, P>,
+            SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nh_rows<SLOTS, P>,
                                                                    kNhWarps * 32, smem));
         const unsigned wave = (unsigned)(resident > 0 ? resident : 1) * kSmCount;
         if (grid > wave) grid = wave;
     }
-    k_nh_rows<SUR, SLOTS, P><<<grid, kNhWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
+    k_nh_rows<SLOTS, P><<<grid, kNhWarps * 32, smem, s>>>(n_groups, groups, pat->indptr.get(),
                                                               pat->inc_ptr.get(), pat->rec.get(), recd, recf, flags,
                                                               fallbacks, residual, values);
     SKG_LAUNCH_CHECK("nh_rows");
@@ -490,9 +462,9 @@ void nh_rows(const skg_pattern *pat, const GroupSet &gs, const double *recd, con
     // FP32 slots when no element fell back, double-float slots otherwise (each kernel reads the count)
     launch_nh_rows_f32<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recf, fallbacks, d_residual, d_values, s);
     launch_nh_rows_f32<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recf, fallbacks, d_residual, d_values, s);
-    launch_nh_rows<true, kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, fallbacks, d_residual,
+    launch_nh_rows<kGroupSlotsSmall, 1>(gs.n_small, gs.small, pat, recd, recf, flags, fallbacks, d_residual,
                                               d_values, s);
-    launch_nh_rows<true, kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, fallbacks, d_residual,
+    launch_nh_rows<kGroupSlotsLarge, 2>(gs.n_large, gs.large, pat, recd, recf, flags, fallbacks, d_residual,
                                               d_values, s);
 }
 
