@@ -809,16 +809,17 @@ __device__ __forceinline__ double exact_entry_fp64(const double g[16]) {
 }
 
 // The 55 entries of a symmetric element matrix with fewer FP64 instructions
-// than one exact_entry_fp64 per entry (about 85 against 112).  With S_v(b) =
+// than one exact_entry_fp64 per entry (about 79 against 112).  With S_v(b) =
 // G_v,lo(b) + G_v,hi(b) (vertex v, edge b, 24 sums), the integer table gives
 //   vertex a, vertex b:      3 G_aa (a = b), -G_ab
 //   vertex a, edge b:        -S_a(b) (a not on b), 3 G_a,hi - G_a,lo (a = lo(b)), 3 G_a,lo - G_a,hi (a = hi(b))
-//   edge a = (i, j), edge b: 4 (S_i(b) + S_j(b) + X), X = G_ii + G_jj (a = b),
-//                            G_(other end of a),(other end of b) (one shared vertex), 0 (disjoint)
+//   edge a = (i, j), edge b: 4 (S_i(b) + S_j(b) + X), X = G_ii + G_jj (a = b; with G symmetric that is
+//                            8 (G_ii + G_jj + G_ij), two additions), X = G_(other end of a),(other end of b)
+//                            (one shared vertex), X = 0 (disjoint)
 // (t30 = 4 (1 + d) - 5 on vertex functions, 4 (1 + d) on edge pairs).  The
-// sign flips and the factor 4 act on the bits (integer instructions): exact,
-// provided every sum stays a normal number below the overflow threshold,
-// which shared_entries_ok checks on G first.
+// sign flips and the factors 4 and 8 act on the bits (integer instructions):
+// exact, provided every sum stays a normal number below the overflow
+// threshold, which shared_entries_ok checks on G first.
 __device__ __forceinline__ double neg_bits(double x) {
     return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
 }
@@ -826,10 +827,15 @@ __device__ __forceinline__ double times4_bits(double x) {  // zero stays zero
     const int hi = __double2hiint(x);
     return __hiloint2double(hi + ((hi & 0x7ff00000) ? 0x00200000 : 0), __double2loint(x));
 }
+__device__ __forceinline__ double times8_bits(double x) {  // zero stays zero
+    const int hi = __double2hiint(x);
+    return __hiloint2double(hi + ((hi & 0x7ff00000) ? 0x00300000 : 0), __double2loint(x));
+}
 
 // Every nonzero G entry with a biased exponent in [64, 2032]: then any sum of
 // up to six of them is zero or a normal number (a multiple of the smallest
-// entry's unit in the last place, above 2^-1022) and four times it is finite.
+// entry's unit in the last place, above 2^-1022) and four or eight times it
+// is finite.
 __device__ __forceinline__ bool shared_entries_ok(const double g[16]) {
     bool ok = true;
 #pragma unroll
@@ -853,10 +859,12 @@ __device__ __forceinline__ double shared_entry(const double g[16], const double 
         else return fma(3.0, g[A * 4 + lo], -g[A * 4 + hi]);
     } else {
         constexpr int i = sup_lo(A), j = sup_hi(A), lb = sup_lo(BB), hb = sup_hi(BB);
-        const double T = S[i][BB - 4] + S[j][BB - 4];
         if constexpr (A == BB) {
-            return times4_bits(T + (g[i * 4 + i] + g[j * 4 + j]));
-        } else if constexpr (i == lb || i == hb || j == lb || j == hb) {
+            // 4 (S_i + S_j + g_ii + g_jj) over edge (i, j) = 8 (g_ii + g_jj + g_ij): g is symmetric here
+            return times8_bits((g[i * 4 + i] + g[j * 4 + j]) + g[i * 4 + j]);
+        }
+        const double T = S[i][BB - 4] + S[j][BB - 4];
+        if constexpr (i == lb || i == hb || j == lb || j == hb) {
             constexpr int na = (i == lb || i == hb) ? j : i, nb = (lb == i || lb == j) ? hb : lb;
             return times4_bits(T + g[na * 4 + nb]);
         } else {
