@@ -809,23 +809,29 @@ __device__ __forceinline__ double exact_entry_fp64(const double g[16]) {
 }
 
 // The 55 entries of a symmetric element matrix with fewer FP64 instructions
-// than one exact_entry_fp64 per entry (about 79 against 112).  With S_v(b) =
+// than one exact_entry_fp64 per entry (about 55 against 112).  With S_v(b) =
 // G_v,lo(b) + G_v,hi(b) (vertex v, edge b, 24 sums), the integer table gives
 //   vertex a, vertex b:      3 G_aa (a = b), -G_ab
 //   vertex a, edge b:        -S_a(b) (a not on b), 3 G_a,hi - G_a,lo (a = lo(b)), 3 G_a,lo - G_a,hi (a = hi(b))
 //   edge a = (i, j), edge b: 4 (S_i(b) + S_j(b) + X), X = G_ii + G_jj (a = b; with G symmetric that is
 //                            8 (G_ii + G_jj + G_ij), two additions), X = G_(other end of a),(other end of b)
-//                            (one shared vertex), X = 0 (disjoint)
-// (t30 = 4 (1 + d) - 5 on vertex functions, 4 (1 + d) on edge pairs).  The
-// sign flips and the factors 4 and 8 act on the bits (integer instructions):
-// exact, provided every sum stays a normal number below the overflow
-// threshold, which shared_entries_ok checks on G first.
+//                            (one shared vertex s, other ends na, nb, fourth vertex n; with G's zero row
+//                            sums that is 4 (2 G_na,nb - G_s,n), one addition), X = 0 (disjoint)
+// (t30 = 4 (1 + d) - 5 on vertex functions, 4 (1 + d) on edge pairs), so only
+// the 12 sums S_v(b) with v off edge b are formed.  The sign flips and the
+// factors 2, 4 and 8 act on the bits (integer instructions): exact, provided
+// every sum stays a normal number below the overflow threshold, which
+// shared_entries_ok checks on G first.
 __device__ __forceinline__ double neg_bits(double x) {
     return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
 }
 __device__ __forceinline__ double times4_bits(double x) {  // zero stays zero
     const int hi = __double2hiint(x);
     return __hiloint2double(hi + ((hi & 0x7ff00000) ? 0x00200000 : 0), __double2loint(x));
+}
+__device__ __forceinline__ double times2_bits(double x) {  // zero stays zero
+    const int hi = __double2hiint(x);
+    return __hiloint2double(hi + ((hi & 0x7ff00000) ? 0x00100000 : 0), __double2loint(x));
 }
 __device__ __forceinline__ double times8_bits(double x) {  // zero stays zero
     const int hi = __double2hiint(x);
@@ -863,12 +869,14 @@ __device__ __forceinline__ double shared_entry(const double g[16], const double 
             // 4 (S_i + S_j + g_ii + g_jj) over edge (i, j) = 8 (g_ii + g_jj + g_ij): g is symmetric here
             return times8_bits((g[i * 4 + i] + g[j * 4 + j]) + g[i * 4 + j]);
         }
-        const double T = S[i][BB - 4] + S[j][BB - 4];
         if constexpr (i == lb || i == hb || j == lb || j == hb) {
-            constexpr int na = (i == lb || i == hb) ? j : i, nb = (lb == i || lb == j) ? hb : lb;
-            return times4_bits(T + g[na * 4 + nb]);
+            // shared vertex sv, other ends na (of a) and nb (of b), fourth vertex n: with the zero row sum
+            // G_sv,sv + G_sv,na + G_sv,nb + G_sv,n = 0 the entry is 4 (2 G_na,nb - G_sv,n)
+            constexpr int sv = (i == lb || i == hb) ? i : j;
+            constexpr int na = sv == i ? j : i, nb = (lb == sv) ? hb : lb, n = 6 - sv - na - nb;
+            return times4_bits(times2_bits(g[na * 4 + nb]) - g[sv * 4 + n]);
         } else {
-            return times4_bits(T);
+            return times4_bits(S[i][BB - 4] + S[j][BB - 4]);
         }
     }
 }
