@@ -273,7 +273,7 @@ def measured_peak():
 FP64_PROFILE = {
     "source": "ncu --metrics ... --clock-control none on python bench.py --cells 32 (instructions) / --cells 48 "
               "(DRAM) --steps 2 --warmup 3 --no-cpu-baseline --modes fp64, GB300",
-    "commit": "8274f2d",
+    "commit": "a327ee2",
     "ops_per_element": {"k_elem_ke_fp64_exact": 163.0, "k_rows_ke": 95.3},
     "dram_bytes_64": {"k_elem_ke_fp64_exact": 1261945000.0, "k_rows_ke": 2217479000.0},
 }
