@@ -793,6 +793,33 @@ __device__ __forceinline__ df64 exact_entry(const df64 g[16]) {
     return fast_two_sum(S, L);
 }
 
+// exact_entry for a symmetric G (the upper triangle, a <= b), with fewer
+// terms where G's symmetry and zero row sums allow (as shared_entry does in
+// FP64): an edge's diagonal entry as 8 (G_ii + G_jj + G_ij) (3 terms instead
+// of 4), an entry of two edges sharing a vertex s as 8 G_na,nb - 4 G_s,n (na,
+// nb their other ends, n the fourth vertex: 2 terms instead of 4).
+template <int A, int BB, int MODE>
+__device__ __forceinline__ df64 exact_entry_sym(const df64 g[16]) {
+    if constexpr (A >= 4 && BB >= 4) {
+        constexpr int i = sup_lo(A), j = sup_hi(A), lb = sup_lo(BB), hb = sup_hi(BB);
+        if constexpr (A == BB) {
+            float S = 0.f, L = 0.f;
+            sum_term<MODE>(S, L, df_mul_int<8>(g[i * 4 + i]));
+            sum_term<MODE>(S, L, df_mul_int<8>(g[j * 4 + j]));
+            sum_term<MODE>(S, L, df_mul_int<8>(g[i * 4 + j]));
+            return fast_two_sum(S, L);
+        } else if constexpr (i == lb || i == hb || j == lb || j == hb) {
+            constexpr int sv = (i == lb || i == hb) ? i : j;
+            constexpr int na = sv == i ? j : i, nb = (lb == sv) ? hb : lb, n = 6 - sv - na - nb;
+            float S = 0.f, L = 0.f;
+            sum_term<MODE>(S, L, df_mul_int<8>(g[na * 4 + nb]));
+            sum_term<MODE>(S, L, df_mul_int<-4>(g[sv * 4 + n]));
+            return fast_two_sum(S, L);
+        }
+    }
+    return exact_entry<A, BB, MODE>(g);
+}
+
 // FP64 entry K_ab = sum t30 G (G carrying the 1/30) with compile-time integer
 // factors: -1 terms become additions, a vertex-edge entry one FMA.
 template <int A, int BB>
@@ -810,7 +837,7 @@ __device__ __forceinline__ double exact_entry_fp64(const double g[16]) {
 
 // The 55 entries of a symmetric element matrix with fewer FP64 instructions
 // than one exact_entry_fp64 per entry (about 55 against 112).  With S_v(b) =
-// G_v,lo(b) + G_v,hi(b) (vertex v, edge b, 24 sums), the integer table gives
+// G_v,lo(b) + G_v,hi(b) (vertex v, edge b), the integer table gives
 //   vertex a, vertex b:      3 G_aa (a = b), -G_ab
 //   vertex a, edge b:        -S_a(b) (a not on b), 3 G_a,hi - G_a,lo (a = lo(b)), 3 G_a,lo - G_a,hi (a = hi(b))
 //   edge a = (i, j), edge b: 4 (S_i(b) + S_j(b) + X), X = G_ii + G_jj (a = b; with G symmetric that is
@@ -970,10 +997,10 @@ __device__ __forceinline__ void elem_ke_df64_tile(int64_t tile, int64_t ne, cons
         for (int k = 0; k < 16; ++k) g[k] = df64{0.f, 0.f};
     }
     df64 U[55];
-    if (sym) {
+    if (sym) {  // the same entries as k_elem_ke_df64_packed gives a symmetric element
         static_for<0, 100>([&](auto kk) {
             constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
-            if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry<A, BB, MODE>(g);
+            if constexpr (A <= BB) U[tri10(A, BB)] = exact_entry_sym<A, BB, MODE>(g);
         });
     }
     const int nvalid = (int)(ne - e0 < kKeBlock ? ne - e0 : kKeBlock);
@@ -1061,7 +1088,7 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_split(int64_t ne, const do
         static_for<0, 100>([&](auto kk) {
             constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
             if constexpr (A <= BB) {
-                const df64 v = exact_entry<A, BB, MODE_SPLIT>(g);
+                const df64 v = exact_entry_sym<A, BB, MODE_SPLIT>(g);
                 st[tri10(A, BB)] = v.hi + v.lo;
             }
         });
@@ -1131,7 +1158,7 @@ __global__ void __launch_bounds__(kKeBlock) k_elem_ke_df64_packed(int64_t ne, co
     static_for<0, 100>([&](auto kk) {
         constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
         if constexpr (A <= BB) {
-            const df64 v = exact_entry<A, BB, MODE_DF64>(g);
+            const df64 v = exact_entry_sym<A, BB, MODE_DF64>(g);
             st[tri10(A, BB)] = make_float2(v.hi, v.lo);
         }
     });
