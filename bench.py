@@ -407,8 +407,8 @@ def run_gpu(args, rank, world):
     bytes_rows = 24 * E + 8 * nnz
     head_mode = args.modes[0]
     # the workload's 4-point rule integrates quadratics exactly: the integer-factor element kernel runs
-    names = {"fp64": ("k_elem_ke_fp64_exact", "k_rows_ke"), "fp64_emulated": ("k_elem_ke_df64", "k_rows_ke_df"),
-             "split_fp32": ("k_elem_df64", "k_rows_group")}[head_mode]
+    names = {"fp64": ("k_elem_ke_fp64_exact", "k_rows_ke"), "fp64_emulated": ("k_elem_ke_df64_packed", "k_rows_ke_df"),
+             "split_fp32": ("k_elem_ke_split", "k_rows_ke_f32")}[head_mode]
     passes = [q for q in [(names[0], "element", bytes_elem, t_el), (names[1], "row", bytes_rows, t_rows)] if q[3] > 0]
     dominant = max(passes, key=lambda q: q[3])
     achieved = dominant[2] / (dominant[3] * 1e-3) / 1e9
