@@ -166,6 +166,8 @@ constexpr int kN1Block = 128;
 // Per-element coefficients, closed form: K_ac = s_a s_c (mu sum_uv G T + nu
 // (J c_a . J c_c) wsum / |det|) with G = b_k . b_l / |det|; the 21 entries of
 // the symmetric 6 x 6 matrix, stores staged through shared memory (FP64).
+// The curl term as c_a^T H c_c with H = 4 nu wsum J^T J / |det| (the
+// reference curls c_a have entries 0 and +-2): signed sums of H's entries.
 __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e_begin, int64_t e_end,
                                                             const double *__restrict__ p, int64_t npts,
                                                             const int32_t *__restrict__ t,
@@ -199,16 +201,16 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
             Gm[l][0] = Gm[0][l];
         }
         Gm[0][0] = -(Gm[0][1] + Gm[0][2] + Gm[0][3]);
-        double Jc[6][3];
+        // curl term nu (J c_a).(J c_c) = c_a^T (nu J^T J) c_c: with H = 4 nu J^T J (6 entries) and the
+        // reference curls' entries +-2, each entry is a signed sum of 1 to 4 entries of H
+        double H[3][3];
+        const double nu4 = 4.0 * nu;
 #pragma unroll
-        for (int a = 0; a < 6; ++a)
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                double v = 0.0;
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    if (ref_curl(a, r) != 0.0) v += J[i * 3 + r] * ref_curl(a, r);
-                Jc[a][i] = v;
+            for (int q = r; q < 3; ++q) {
+                H[r][q] = nu4 * (J[r] * J[q] + J[3 + r] * J[3 + q] + J[6 + r] * J[6 + q]);
+                H[q][r] = H[r][q];
             }
         // orientation signs (+1 / -1) applied as a sign-bit flip of the FP64 value
         uint32_t neg[6];
@@ -219,8 +221,17 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_fast(int64_t ne, int64_t e
         for (int a = 0; a < 6; ++a)
 #pragma unroll
             for (int c = a; c < 6; ++c) {
-                const double cc = Jc[a][0] * Jc[c][0] + Jc[a][1] * Jc[c][1] + Jc[a][2] * Jc[c][2];
-                double val = nu * cc;
+                double val = 0.0;
+                bool first = true;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        if (ref_curl(a, r) != 0.0 && ref_curl(c, q) != 0.0) {
+                            const double h = (ref_curl(a, r) > 0.0) == (ref_curl(c, q) > 0.0) ? H[r][q] : -H[r][q];
+                            val = first ? h : val + h;
+                            first = false;
+                        }
 #pragma unroll
                 for (int u = 0; u < 2; ++u)
 #pragma unroll
@@ -303,19 +314,16 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_df(int64_t ne, int64_t e_b
                 ok = ok && df_in_range(d);
                 G2[k][l] = G2[l][k] = make_float2(d.hi, d.lo);
             }
-        float2 C2[6][3];
+        // curl term (J c_a).(J c_c) = c_a^T (J^T J) c_c: H = 4 J^T J in double-float (6 entries; the
+        // reference curls' entries are +-2), each entry a signed sum of 1 to 4 of H's (hi, lo) pairs
+        float2 H2[3][3];
 #pragma unroll
-        for (int a = 0; a < 6; ++a)
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                df64 c{0.f, 0.f};
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    if (ref_curl(a, r) != 0.0) {
-                        const df64 x = df64{2.f * J[i * 3 + r].hi, 2.f * J[i * 3 + r].lo};  // |ref_curl| = 2
-                        c = ref_curl(a, r) > 0.0 ? df_add(c, x) : df_sub(c, x);
-                    }
-                C2[a][i] = make_float2(c.hi, c.lo);
+            for (int q = r; q < 3; ++q) {
+                const df64 h = df_add_fast(df_add_fast(df_mul(J[r], J[q]), df_mul(J[3 + r], J[3 + q])),
+                                           df_mul(J[6 + r], J[6 + q]));
+                H2[r][q] = H2[q][r] = make_float2(4.f * h.hi, 4.f * h.lo);
             }
         const df64 mu = inc_mass ? df_from_double(mass ? mass[e] : 1.0, 0, ok) : df64{0.f, 0.f};
         df64 nu{0.f, 0.f};
@@ -344,12 +352,19 @@ __global__ void __launch_bounds__(kN1Block) k_n1_elem_df(int64_t ne, int64_t e_b
                     }
                 float ch = 0.f, cl = 0.f;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const float2 x = C2[a][i], y = C2[c][i];
-                    const float ph = x.x * y.x;
-                    ch += ph;
-                    cl += fmaf(x.x, y.x, -ph) + fmaf(x.x, y.y, x.y * y.x);
-                }
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        if (ref_curl(a, r) != 0.0 && ref_curl(c, q) != 0.0) {
+                            const float2 h = H2[r][q];
+                            if ((ref_curl(a, r) > 0.0) == (ref_curl(c, q) > 0.0)) {
+                                ch += h.x;
+                                cl += h.y;
+                            } else {
+                                ch -= h.x;
+                                cl -= h.y;
+                            }
+                        }
                 const float m = mh + ml, cc = ch + cl;
                 // mass term (scale 2^-s) and curl term (scale 2^s) as (hi, lo) pairs
                 const float mth = mu.hi * m, ctl_h = nu.hi * cc;

@@ -350,6 +350,23 @@ def test_device_resident_csr_handoff():
     assert relerr(yn, Kn @ xn) < 1e-13
 
 
+def test_p2_exact_rule_entries_far_from_unit_scale():
+    """The FP64 exact-rule element pass forms most entries from shared sums
+    with the factors 2, 4 and 8 applied to the exponent bits; when a G entry's
+    exponent leaves the range where that is exact, the element takes one
+    table evaluation per entry instead.  A coefficient scaled by 2^-980 puts
+    G there (every value stays normal, and a power-of-two scaling is exact):
+    the result is the golden matrix scaled by 2^-980."""
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    scale = 2.0 ** -980
+    Apub = np.broadcast_to(np.moveaxis(g["A"] * scale, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    K = sk.asm(aniso, b, A=Apub)
+    same_pattern(K, g)
+    assert relerr(K.data / scale, g["data"]) < RTOL
+
+
 def _asymmetry_cases():
     """Per-element tensors around the symmetry tolerance |A_kl - A_lk| <=
     1e-14 (|A_00| + |A_11| + |A_22| + |A_01| + |A_02| + |A_12|)."""
