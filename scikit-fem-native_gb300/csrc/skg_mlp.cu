@@ -583,6 +583,14 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
             FiTr[c] = i == 0 ? FiT[c] : i == 1 ? FiT[3 + c] : FiT[6 + c];
             FFtr[c] = i == 0 ? FFt[c] : i == 1 ? FFt[3 + c] : FFt[6 + c];
         }
+        // sum_ml Wab[m][l] dI_m[iJ] dI_l[kL] = sum_l U[l][J] dI_l[kL] with U[l][J] = sum_m Wab[m][l] dI_m[iJ],
+        // formed once per row block
+        float U[3][3];
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+            for (int Jj = 0; Jj < 3; ++Jj)
+                U[l][Jj] = Wab[l] * dIr[0][Jj] + Wab[3 + l] * dIr[1][Jj] + Wab[6 + l] * dIr[2][Jj];
         float Ai[28];
 #pragma unroll
         for (int Jj = 0; Jj < 3; ++Jj)
@@ -591,11 +599,7 @@ __device__ __forceinline__ bool surrogate_finish(const SurState &st, const float
 #pragma unroll
                 for (int L = 0; L < 3; ++L) {
                     const int b = k * 3 + L;
-                    float v = 0.f;
-#pragma unroll
-                    for (int m = 0; m < 3; ++m)
-#pragma unroll
-                        for (int l = 0; l < 3; ++l) v += Wab[m * 3 + l] * dIr[m][Jj] * dI[l][b];
+                    float v = U[0][Jj] * dI[0][b] + U[1][Jj] * dI[1][b] + U[2][Jj] * dI[2][b];
                     const float dik = i == k ? 1.f : 0.f, dJL = Jj == L ? 1.f : 0.f;
                     v += Wa[0] * 2.f * dik * dJL;
                     v += Wa[1] * 2.f * (2.f * Fr[Jj] * F[b] + I1 * dik * dJL - dik * C[L * 3 + Jj] -
@@ -861,24 +865,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nh_surrogate_tc(int64_t e_beg
                                                                    const float4 *__restrict__ xin,
                                                                    float *__restrict__ net,
                                                                    unsigned long long *__restrict__ counters) {
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem_tc[];  // own name: the other kernels' dynamic arrays are 16-aligned
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int row = tid & (kTcRows - 1), half = tid / kTcRows, jb = half * kHalf;
-    float *Q = reinterpret_cast<float *>(smem + SM_Q);
-    float *part = reinterpret_cast<float *>(smem + SM_PART);  // [half][kPart][row]
-    unsigned char *opa_hi = smem + SM_OPA_HI, *opa_lo = smem + SM_OPA_LO;
-    unsigned char *opb_hi = smem + SM_OPB_HI, *opb_lo = smem + SM_OPB_LO;
-    const unsigned char *w2b_hi = smem + SM_W2B_HI, *w2b_lo = smem + SM_W2B_LO;
-    const unsigned char *w2t_hi = smem + SM_W2T_HI, *w2t_lo = smem + SM_W2T_LO;
+    float *Q = reinterpret_cast<float *>(smem_tc + SM_Q);
+    float *part = reinterpret_cast<float *>(smem_tc + SM_PART);  // [half][kPart][row]
+    unsigned char *opa_hi = smem_tc + SM_OPA_HI, *opa_lo = smem_tc + SM_OPA_LO;
+    unsigned char *opb_hi = smem_tc + SM_OPB_HI, *opb_lo = smem_tc + SM_OPB_LO;
+    const unsigned char *w2b_hi = smem_tc + SM_W2B_HI, *w2b_lo = smem_tc + SM_W2B_LO;
+    const unsigned char *w2t_hi = smem_tc + SM_W2T_HI, *w2t_lo = smem_tc + SM_W2T_LO;
     for (int k = tid; k < H * H; k += kTcThreads) {
         const int i = k / H, j = k - (k / H) * H;
         const float w = params[OW2 + k], hi = tc::to_tf32(w), lo = tc::to_tf32(w - hi);
-        *reinterpret_cast<float *>(smem + SM_W2B_HI + tc::operand_offset(H, i, j)) = hi;
-        *reinterpret_cast<float *>(smem + SM_W2B_LO + tc::operand_offset(H, i, j)) = lo;
-        *reinterpret_cast<float *>(smem + SM_W2T_HI + tc::operand_offset(H, j, i)) = hi;
-        *reinterpret_cast<float *>(smem + SM_W2T_LO + tc::operand_offset(H, j, i)) = lo;
+        *reinterpret_cast<float *>(smem_tc + SM_W2B_HI + tc::operand_offset(H, i, j)) = hi;
+        *reinterpret_cast<float *>(smem_tc + SM_W2B_LO + tc::operand_offset(H, i, j)) = lo;
+        *reinterpret_cast<float *>(smem_tc + SM_W2T_HI + tc::operand_offset(H, j, i)) = hi;
+        *reinterpret_cast<float *>(smem_tc + SM_W2T_LO + tc::operand_offset(H, j, i)) = lo;
     }
     for (int k = tid; k < QSIZE; k += kTcThreads) {
         float v = 0.f;
