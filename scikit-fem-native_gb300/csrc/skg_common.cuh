@@ -73,7 +73,7 @@ int guarded(F &&body) {
 // Stream-ordered scratch comes from the device's default memory pool.  Its
 // release threshold is raised once per device so that memory freed at the
 // end of one assembly stays reserved for the next (the default threshold
-// returns it to the driver at every synchronisation, and re-mapping
+// returns it to the CUDA driver at every synchronisation, and re-mapping
 // gigabytes of scratch per call costs milliseconds).  The pool belongs to
 // this process and ends with it.
 inline void retain_pool_memory() {
