@@ -909,10 +909,11 @@ __device__ __forceinline__ double shared_entry(const double g[16], const double 
 }
 
 __device__ __forceinline__ void shared_entries(const double g[16], double U[55]) {
-    double S[4][6];
+    double S[4][6];  // S_v(b) for vertex v off edge b only (the others are not used)
     static_for<0, 24>([&](auto kk) {
         constexpr int k = decltype(kk)::value, v = k / 6, e = k % 6;
-        S[v][e] = g[v * 4 + sup_lo(4 + e)] + g[v * 4 + sup_hi(4 + e)];
+        if constexpr (v != sup_lo(4 + e) && v != sup_hi(4 + e))
+            S[v][e] = g[v * 4 + sup_lo(4 + e)] + g[v * 4 + sup_hi(4 + e)];
     });
     static_for<0, 100>([&](auto kk) {
         constexpr int k = decltype(kk)::value, A = k / 10, BB = k % 10;
