@@ -3,8 +3,8 @@ the full workloads, not on fixture-sized meshes.
 
 * P2 anisotropic diffusion, 64^3 x 6 jittered cube (1,572,864 tets, 60.9 M
   nonzeros), the benchmark's seeded mesh and tensors: FP64, FP64-emulated and
-  split-FP32, through the device path and through the host-output path (16
-  row chunks copied while later chunks are computed).
+  split-FP32, each through the device path and through the host-output path
+  (16 row chunks copied while later chunks are computed).
 * Nedelec N1 Maxwell, 48^3 x 6 cube with seeded vertex relabelling, 27-point
   rule: FP64 and split-FP32.
 * Vector P1 neo-Hookean, 64^3 x 6 cube: plain law (FP64) and the learned
@@ -104,6 +104,19 @@ def test_p2_aniso_64_pattern_and_host_path(p2_case):
     K = form.assemble(c["A_pub"], copy=True)  # host arrays in, scipy CSR out (chunked copies)
     assert np.array_equal(K.indptr, c["indptr"]) and np.array_equal(K.indices, c["indices"])
     check_values("C2 fp64 host path", K.data, c["data"], FP64)
+
+
+@pytest.mark.parametrize("mode,bounds", [("fp64_emulated", FP64), ("split_fp32", SPLIT)])
+def test_p2_aniso_64_host_path_fp32_pair_modes(p2_case, mode, bounds):
+    """The FP32-pair modes through the host-facing call: element pass, range
+    check, then the row pass in chunks copied to the page-locked matrix."""
+    from skfemntv_gb300.assembly import NativeTensorForm
+
+    c = p2_case
+    form = NativeTensorForm(c["basis"])
+    K = form.assemble(c["A_pub"], precision=mode, copy=True)
+    assert np.array_equal(K.indptr, c["indptr"]) and np.array_equal(K.indices, c["indices"])
+    check_values(f"C2 {mode} host path", K.data, c["data"], bounds)
 
 
 @pytest.mark.parametrize("mode,bounds", [("fp64", FP64), ("fp64_emulated", FP64), ("split_fp32", SPLIT)])
