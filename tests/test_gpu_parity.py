@@ -350,17 +350,19 @@ def test_device_resident_csr_handoff():
     assert relerr(yn, Kn @ xn) < 1e-13
 
 
-def test_p2_exact_rule_entries_far_from_unit_scale():
+@pytest.mark.parametrize("exponent", [-980, 1000])
+def test_p2_exact_rule_entries_far_from_unit_scale(exponent):
     """The FP64 exact-rule element pass forms most entries from shared sums
     with the factors 2, 4 and 8 applied to the exponent bits; when a G entry's
     exponent leaves the range where that is exact, the element takes one
     table evaluation per entry instead.  A coefficient scaled by 2^-980 puts
-    G there (every value stays normal, and a power-of-two scaling is exact):
-    the result is the golden matrix scaled by 2^-980."""
+    G there; one scaled by 2^1000 keeps G just inside the range, near the top
+    (every value stays normal and finite, and a power-of-two scaling is
+    exact): the result is the golden matrix scaled the same way."""
     g = load_golden("p2_aniso")
     b = p2_basis(g, (g["X"], g["W"]))
     E, Q = b._coefficient_shape
-    scale = 2.0 ** -980
+    scale = 2.0 ** exponent
     Apub = np.broadcast_to(np.moveaxis(g["A"] * scale, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
     K = sk.asm(aniso, b, A=Apub)
     same_pattern(K, g)
