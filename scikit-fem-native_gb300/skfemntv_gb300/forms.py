@@ -445,10 +445,21 @@ def _terms(expr, term, total, message):
     raise UnsupportedNativeForm(message)
 
 
-def _evaluate(coefficient, kwargs, factor):
+def _evaluate(coefficient, kwargs, factor, squeeze=False):
+    """The term's coefficient times its factor (_coefficients.py:71-86).  A
+    factor of 1 keeps the caller's array, so a broadcast view stays a view.
+    ``squeeze`` drops the unit axes of an array of more than two dimensions,
+    as the reference does for the scalar coefficients of bilinear terms
+    (forms.py:302, 463): (E, Q, 1) or (1, E, Q) then reads as (E, Q).  Tensor
+    coefficients keep their axes: squeezed, a (3, 3, E, 1) tensor would lose
+    its point axis and fail the shape check."""
     if coefficient is None:
         return float(factor)
-    v = factor * np.asarray(_resolve(coefficient, kwargs), dtype=np.float64)
+    v = np.asarray(_resolve(coefficient, kwargs), dtype=np.float64)
+    if factor != 1.0:
+        v = factor * v
+    if squeeze and v.ndim > 2:
+        v = np.squeeze(v)
     return v
 
 
@@ -471,7 +482,7 @@ def _cross_assemble(form, trial_basis, test_basis, kwargs, memory_limit_bytes, m
     for t in terms:
         if t.kind not in ("value", "gradient", "row_divergence", "column_divergence"):
             raise UnsupportedNativeForm(f"unsupported cross-basis term kind {t.kind!r}")
-        m = native.assemble(t.kind, _evaluate(t.coefficient, kwargs, t.factor))
+        m = native.assemble(t.kind, _evaluate(t.coefficient, kwargs, t.factor, squeeze=True))
         result = m if result is None else result + m
     return result
 
@@ -511,7 +522,8 @@ def asm(form, *bases, num_threads=None, memory_limit_bytes=None, memory_safety_f
                        "native BilinearForm must reduce to dot(u, v), ddot(grad(u), grad(v)), "
                        "or a sum of those terms")
         return assemble_bilinear(
-            form, basis, [(t.kind, _evaluate(t.coefficient, kwargs, t.factor)) for t in terms],
+            form, basis, [(t.kind, _evaluate(t.coefficient, kwargs, t.factor, squeeze=t.kind != "gradient_tensor"))
+                          for t in terms],
             precision=precision, memory_limit_bytes=memory_limit_bytes,
             memory_safety_factor=memory_safety_factor)
     raise TypeError(

@@ -132,6 +132,54 @@ def test_p2_anisotropic_per_point_tabulated_path():
     assert relerr(K.data, data) < RTOL
 
 
+def test_p2_constant_tensor_combined_with_isotropic_term_and_rejections():
+    """The reference's anisotropic-form cases (tests/test_anisotropic_forms.py:41-125) on P2 tets: a
+    constant (3, 3) tensor gives a symmetric matrix equal to the oracle's; a nonsymmetric tensor summed
+    with an isotropic mass term equals the sum of the oracle's two assemblies; a tensor of the wrong
+    shape raises ValueError and a vector field UnsupportedNativeForm, with the reference's messages."""
+    g = load_golden("p2_aniso")
+    b = p2_basis(g, (g["X"], g["W"]))
+    E, Q = b._coefficient_shape
+    ob = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+
+    A = np.array([[2.0, 0.4, 0.1], [0.4, 0.8, -0.2], [0.1, -0.2, 1.3]])
+    K = sk.asm(aniso, b, A=A)
+    data, indptr, indices = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(A, (E, Q)))
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, data) < RTOL
+    assert abs(K - K.T).max() <= 2e-14 * np.max(np.abs(K.data))
+
+    @sk.BilinearForm
+    def aniso_mass(u, v, w):
+        return dot(mul(w.A, grad(u)), grad(v)) + 0.25 * dot(u, v)
+
+    An = np.array([[1.4, 0.2, 0.0], [-0.1, 0.7, 0.3], [0.05, 0.0, 1.1]])
+    Kc = sk.asm(aniso_mass, b, A=An)
+    td, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(An, (E, Q)))
+    md, _, _ = O.bilinear_assemble(ob, value=0.25)
+    Kc.sort_indices()
+    assert np.array_equal(Kc.indptr, indptr) and np.array_equal(Kc.indices, indices)
+    assert relerr(Kc.data, td + md) < RTOL
+    assert abs(Kc - Kc.T).max() > 1e-3 * np.max(np.abs(Kc.data))
+
+    # a scalar coefficient with a unit axis reads as (E, Q), as in the reference (_coefficients.py:84)
+    @sk.BilinearForm
+    def kmass(u, v, w):
+        return w.k * dot(u, v)
+
+    k = 1.0 + np.arange(E * Q, dtype=float).reshape(E, Q) / (E * Q)
+    kd, _, _ = O.bilinear_assemble(ob, value=k)
+    for raw in (k, k[..., None], k[None]):
+        assert relerr(sk.asm(kmass, b, k=raw).data, kd) < RTOL
+
+    with pytest.raises(ValueError, match="recommended scikit-fem shape"):
+        sk.asm(aniso, b, A=np.eye(2))
+    vb = sk.Basis(sk.MeshTet2(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP2(), dim=3),
+                  quadrature=(g["X"], g["W"]))
+    with pytest.raises(sk.UnsupportedNativeForm, match="scalar field"):
+        sk.asm(aniso, vb, A=np.eye(3))
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp64_emulated"])
 def test_p2_fp64_class_paths(precision):
     """Native FP64 and the double-float (FP32-pair) path both meet the FP64 bar."""

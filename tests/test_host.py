@@ -243,3 +243,50 @@ def test_coefficient_classification_routes_fused_and_tabulated_paths():
         per_element(np.ones((E + 1, Q)), E, Q, "value")
     with pytest.raises(ValueError):
         per_point(np.ones((E, Q + 1)), E, Q, "value")
+
+
+def test_coefficient_evaluation_factor_and_squeeze():
+    """A term's coefficient times its factor (_coefficients.py:71-86): a factor of 1 leaves a broadcast
+    view uncopied; squeezing, as bilinear scalar terms do, reads (E, Q, 1) and (1, E, Q) as (E, Q)."""
+    from skfemntv_gb300.forms import Coefficient, _evaluate
+
+    E, Q = 6, 4
+    kappa = np.arange(E * Q, dtype=float).reshape(E, Q)
+    A = np.broadcast_to(np.eye(3)[..., None, None], (3, 3, E, Q))
+    got = _evaluate(Coefficient("A"), {"A": A}, 1.0)
+    assert got.shape == (3, 3, E, Q) and got.strides[2:] == (0, 0)
+    assert np.array_equal(_evaluate(Coefficient("A"), {"A": A}, 2.0), 2.0 * A)
+    assert _evaluate(None, {}, 0.25) == 0.25
+    for raw in (kappa[..., None], kappa[None]):
+        assert np.array_equal(_evaluate(Coefficient("k"), {"k": raw}, 1.0, squeeze=True), kappa)
+        assert _evaluate(Coefficient("k"), {"k": raw}, 1.0).shape == raw.shape
+    assert _evaluate(Coefficient("k"), {"k": kappa[:, :1]}, 3.0, squeeze=True).shape == (E, 1)
+
+
+def test_anisotropic_tensor_layouts_and_shape_error():
+    """The three tensor layouts the reference accepts (forms.py:377-404) give one (E, Q, 3, 3) view, a
+    tensor constant over each element's points goes to the fused per-element path in its own layout, and
+    any other shape raises the reference's ValueError naming the recommended shape."""
+    from skfemntv_gb300.assembly import anisotropic_tensor, tensor_per_element
+
+    E, Q = 4, 5
+    rng = np.random.default_rng(2)
+    Aq = rng.random((E, Q, 3, 3))
+    public = np.ascontiguousarray(np.moveaxis(Aq, (2, 3), (0, 1)))
+    assert np.array_equal(anisotropic_tensor(public, E, Q), Aq)
+    assert np.array_equal(anisotropic_tensor(Aq, E, Q), Aq)
+    A = rng.random((3, 3))
+    assert np.array_equal(anisotropic_tensor(A, E, Q), np.broadcast_to(A, (E, Q, 3, 3)))
+    assert tensor_per_element(Aq, E, Q) is None and tensor_per_element(public, E, Q) is None
+    arr, kind = tensor_per_element(A, E, Q)
+    assert kind == 1 and np.array_equal(arr, np.broadcast_to(A, (E, 3, 3)))
+    Ae = rng.random((E, 3, 3))
+    arr, kind = tensor_per_element(np.broadcast_to(Ae[:, None], (E, Q, 3, 3)), E, Q)
+    assert kind == 1 and np.array_equal(arr, Ae)
+    arr, kind = tensor_per_element(np.repeat(np.moveaxis(Ae, 0, -1)[..., None], Q, axis=3), E, Q)
+    assert kind == 2 and np.array_equal(arr, np.moveaxis(Ae, 0, -1))
+    for bad in (np.eye(2), np.ones((3, 3, E, Q + 1)), np.ones((E, Q, 3))):
+        with pytest.raises(ValueError, match="recommended scikit-fem shape"):
+            tensor_per_element(bad, E, Q)
+        with pytest.raises(ValueError, match="recommended scikit-fem shape"):
+            anisotropic_tensor(bad, E, Q)
