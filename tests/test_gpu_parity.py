@@ -289,6 +289,50 @@ def test_n1_mass_and_curl_separately():
     assert relerr(Km.data, dm) < RTOL and relerr(Kc.data, dc) < RTOL
 
 
+def test_n1_pointwise_coefficients_reused_matrix_and_contract():
+    """The reference's TetN1Assembler cases (tests/test_hcurl_tet_assembler.py:51-95): a coefficient that
+    varies over the quadrature points (the pointwise kernel) against the oracle, mass and curl-curl
+    overwriting one matrix object, the memory estimate and budget, the basis type and coefficient shape
+    errors, and thread limits that leave the values unchanged."""
+    g = load_golden("n1_maxwell")
+    nb = O.make_n1_basis(g["p"], g["t"])
+    gb = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]))
+    a = sk.TetN1Assembler(gb)
+    assert gb.dx.shape == nb.dx.shape
+    coef = np.linspace(0.5, 1.5, gb.dx.size).reshape(gb.dx.shape)
+    Km = a.assemble_mass(coef)
+    ident = (id(Km), id(Km.data), id(Km.indices), id(Km.indptr))
+    dm, indptr, indices = O.n1_assemble_maxwell(nb, coef, 0.0)
+    assert np.array_equal(Km.indptr, indptr) and np.array_equal(Km.indices, indices)
+    assert relerr(Km.data, dm) < RTOL
+    Kc = a.assemble_curl_curl(coef)
+    assert (id(Kc), id(Kc.data), id(Kc.indices), id(Kc.indptr)) == ident
+    dc, _, _ = O.n1_assemble_maxwell(nb, 0.0, coef)
+    assert relerr(Kc.data, dc) < RTOL
+    Kmx = a.assemble_maxwell(mass_coefficient=coef, curl_coefficient=coef[::-1])
+    dmx, _, _ = O.n1_assemble_maxwell(nb, coef, coef[::-1])
+    assert relerr(Kmx.data, dmx) < RTOL
+
+    est = sk.estimate_tet_n1_assembly_memory(gb)
+    assert est.kind == "hcurl_tet_n1" and est.row_local_dofs == est.column_local_dofs == 6
+    with pytest.raises(TypeError, match="AffineTetN1Basis"):
+        sk.TetN1Assembler(sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1)))
+    with pytest.raises(sk.AssemblyMemoryBudgetError):
+        sk.TetN1Assembler(gb, memory_limit_bytes=1)
+    with pytest.raises(ValueError, match="mass coefficient"):
+        a.assemble_mass(np.zeros((2, 2, 2)))
+    with pytest.raises(ValueError, match="curl coefficient"):
+        a.assemble_curl_curl(np.zeros(gb.dx.shape[0] + 1))
+
+    with sk.thread_limit(1):
+        serial = a.assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2).data.copy()
+    with sk.thread_limit(4):
+        parallel = a.assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2).data.copy()
+    assert np.array_equal(serial, parallel)
+    d13, _, _ = O.n1_assemble_maxwell(nb, 1.3, 0.2)
+    assert relerr(serial, d13) < RTOL
+
+
 def test_vector_p1_elasticity_terms():
     g = load_golden("vp1_elasticity")
     b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))
@@ -359,6 +403,53 @@ def test_geometry_errors_match_reference():
     bad = sk.MeshTet(np.eye(3, 4), np.array([[0], [1], [1], [2]]))
     with pytest.raises(ValueError, match="repeats a corner"):
         sk.AffineTetN1Basis(bad)
+
+
+def test_geometry_validation_cases_match_reference():
+    """The reference's tetrahedral geometry checks (tests/test_geometry_validation.py:22-137, its tet cases
+    and the tet analogue of its triangle condition-number case): the diagnostics of a valid mesh, one
+    uniformly inverted tet accepted and reported, a 1e-50-scaled tet accepted with its determinant, an
+    edge node that inverts a quadratic tet inside rejected at the first quadrature point where the
+    determinant turns negative, and the Frobenius condition number of a flat but valid tet."""
+    scalar = sk.ElementVector(sk.ElementTetP1(), dim=1)
+    mesh = sk.MeshTet()
+    b = sk.Basis(mesh, scalar)
+    d = b.geometry_diagnostics
+    Q = b.X.shape[1]
+    assert isinstance(d, sk.GeometryDiagnostics)
+    assert d.element_count == mesh.nelements and d.quadrature_points_per_element == Q
+    assert d.minimum_determinant > 0 and d.maximum_determinant >= d.minimum_determinant
+    assert d.minimum_scaled_determinant > 0 and d.determinant_tolerance > 0
+    assert 0 <= d.worst_element < mesh.nelements and 0 <= d.worst_quadrature_point < Q
+    assert d.maximum_condition_number >= 3
+    assert 0 <= d.worst_condition_element < mesh.nelements and 0 <= d.worst_condition_quadrature_point < Q
+
+    inverted = sk.MeshTet(np.array([[0., 0., 1., 0.], [0., 1., 0., 0.], [0., 0., 0., 1.]]),
+                          np.array([[0], [1], [2], [3]]))
+    b = sk.Basis(inverted, scalar)
+    assert b.geometry_diagnostics.maximum_determinant < 0
+    assert b.geometry_diagnostics.minimum_scaled_determinant == pytest.approx(1.0)
+    assert b.geometry_diagnostics.negative_orientation_elements == 1
+    assert np.all(b.dx > 0)
+
+    scale = 1e-50
+    b = sk.Basis(sk.MeshTet(scale * sk.MeshTet().p, sk.MeshTet().t), scalar)
+    np.testing.assert_allclose(b.geometry_diagnostics.minimum_determinant, scale ** 3, rtol=2e-15)
+    assert b.geometry_diagnostics.minimum_scaled_determinant == pytest.approx(1.0)
+
+    m2 = sk.MeshTet2.from_mesh(sk.MeshTet())
+    points = m2.p.copy()
+    points[:, 4] = -2.0
+    corner = points[:, m2.t[:4, 0]]
+    assert np.linalg.det(corner[:, 1:] - corner[:, :1]) > 0
+    with pytest.raises(ValueError, match=r"cell=0, quadrature_point=2, determinant=-.*reason=orientation_change"):
+        sk.Basis(sk.MeshTet2(points, m2.t), sk.ElementVector(sk.ElementTetP2(), dim=1), intorder=4)
+
+    flat = sk.MeshTet(np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 1e-8]]),
+                      np.array([[0], [1], [2], [3]]))
+    d = sk.Basis(flat, scalar).geometry_diagnostics
+    assert d.maximum_condition_number == pytest.approx(np.sqrt((2 + 1e-16) * (2 + 1e16)))
+    assert d.worst_condition_element == 0 and d.worst_condition_quadrature_point == 0
 
 
 def test_full_size_p1_laplace_vs_oracle():
