@@ -531,12 +531,13 @@ class NativeCrossBilinearForm:
     tensors.  Each call returns a new matrix, as the reference's."""
 
     def __init__(self, test_basis, trial_basis, *, memory_limit_bytes=None, memory_safety_factor=1.25):
+        # the budget first: reading dx below makes the bases' device tabulation
+        self.memory_estimate = estimate_bilinear_memory(test_basis, trial_basis)
+        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
         if test_basis.dx.shape != trial_basis.dx.shape:
             raise ValueError("trial and test quadrature shapes must match")
         if not np.allclose(test_basis.dx, trial_basis.dx):
             raise ValueError("trial and test quadrature weights must match")
-        self.memory_estimate = estimate_bilinear_memory(test_basis, trial_basis)
-        enforce_memory_budget(self.memory_estimate, memory_limit_bytes, safety_factor=memory_safety_factor)
         if not np.allclose(test_basis.global_coordinates, trial_basis.global_coordinates):
             raise ValueError("trial and test quadrature coordinates must match")
         self.test_basis, self.trial_basis = test_basis, trial_basis

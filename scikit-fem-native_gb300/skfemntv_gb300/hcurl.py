@@ -18,7 +18,7 @@ from . import quadrature as quad
 from ._native import SKG_FP64, call
 from .assembly import Pattern, _MatrixTarget, _precision, per_element, per_point
 from .mesh import oriented_edges
-from .preflight import AssemblyMemoryEstimate, enforce_memory_budget
+from .preflight import enforce_memory_budget, estimate_n1_memory
 
 
 @dataclass(frozen=True)
@@ -138,14 +138,7 @@ class AffineTetN1Basis:
 def estimate_tet_n1_assembly_memory(basis):
     if not isinstance(basis, AffineTetN1Basis):
         raise TypeError("basis must be AffineTetN1Basis")
-    E, N = basis.mesh.nelements, basis.N
-    nnz = min(N * N, E * 36)
-    return AssemblyMemoryEstimate(
-        kind="hcurl_tet_n1", rows=N, columns=N, entity_count=E, quadrature_points_per_entity=len(basis.W),
-        row_local_dofs=6, column_local_dofs=6, nnz_upper_bound=nnz,
-        device_pattern_bytes=4 * (12 * E + 2 * (N + 1) + 6 * E + nnz), device_values_bytes=8 * nnz,
-        device_scratch_bytes=8 * 36 * E, host_csr_bytes=12 * nnz + 8 * (N + 1),
-        pattern_temporary_bytes_upper_bound=8 * (N + 1) + 16 * E * 6)
+    return estimate_n1_memory(basis, basis.mesh.nelements, len(basis.W), int(basis.N))
 
 
 class TetN1Assembler:

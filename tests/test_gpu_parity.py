@@ -333,6 +333,59 @@ def test_n1_pointwise_coefficients_reused_matrix_and_contract():
     assert relerr(serial, d13) < RTOL
 
 
+def test_named_coefficient_components_use_the_first_axis():
+    """The reference's coefficient-component cases (tests/test_coefficient_components.py:25-138, on
+    scalar P1 tets; composite elements are outside this path): components of a keyword array are taken
+    along its first axis in bilinear and linear forms, beside an anisotropic tensor term; a missing
+    parameter, an out-of-range component and a non-integer index raise the reference's messages."""
+    m = sk.MeshTet.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4), np.linspace(0, 1, 3))
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1))
+    E, Q = b.dx.shape
+    x = np.moveaxis(b.global_coordinates, -1, 0)
+    material = np.empty((2, E, Q))
+    material[0] = 0.7 + 0.2 * x[0]
+    material[1] = 1.1 + 0.3 * x[1]
+    diffusion = np.array([[1.4, 0.2, 0.0], [-0.1, 0.8, 0.1], [0.0, 0.3, 1.2]])
+
+    @sk.BilinearForm
+    def form(u, v, w):
+        return (w.material[0] * dot(u, v) + w.material[1] * ddot(grad(u), grad(v))
+                + dot(mul(w.diffusion, grad(u)), grad(v)))
+
+    K = sk.asm(form, b, material=material, diffusion=diffusion)
+    ob = O.make_basis(m.p, m.t, False, quadrature=(b.X, b.W))
+    pd, indptr, indices = O.bilinear_assemble(ob, value=material[0], gradient=material[1])
+    td, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(diffusion, (E, Q)))
+    K.sort_indices()
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, pd + td) < RTOL
+
+    loads = np.empty((2, E, Q))
+    loads[0] = 0.5
+    loads[1] = 1.0 + x[0]
+
+    @sk.LinearForm
+    def load(v, w):
+        return dot(w.loads[1], v)
+
+    assert relerr(sk.asm(load, b, loads=loads), O.linear_assemble(ob, value=loads[1][..., None])) < RTOL
+
+    @sk.BilinearForm
+    def indexed(u, v, w):
+        return w.material[2] * dot(u, v)
+
+    @sk.BilinearForm
+    def noninteger(u, v, w):
+        return w.material["stiffness"] * dot(u, v)
+
+    with pytest.raises(ValueError, match="missing form parameter 'material'"):
+        sk.asm(indexed, b)
+    with pytest.raises(ValueError, match="has no component 2"):
+        sk.asm(indexed, b, material=np.ones((2, E, Q)))
+    with pytest.raises(ValueError, match="component index must be an integer"):
+        sk.asm(noninteger, b)
+
+
 def test_vector_p1_elasticity_terms():
     g = load_golden("vp1_elasticity")
     b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X1, W1))

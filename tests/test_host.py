@@ -182,14 +182,91 @@ def test_runtime_controls():
     assert sk.get_num_threads() == before
 
 
+class _SizesMesh:
+    def __init__(self, E):
+        self.nelements = E
+
+
+class _SizesBasis:
+    """Stand-in with the sizes a memory estimate reads (no device arrays)."""
+
+    def __init__(self, E, Q, nodes, comp, N):
+        self.mesh = _SizesMesh(E)
+        self.W = np.full(Q, 1.0 / Q)
+        self._nodes, self._comp, self.N = nodes, comp, N
+        self.element_dofs = np.zeros((nodes * comp, E), dtype=np.int64)
+        self._tab = None
+
+
 def test_memory_budget_error():
-    est = sk.AssemblyMemoryEstimate("bilinear", 10, 10, 4, 1, 4, 4, 64, 1000, 512, 0, 768, 100)
-    with pytest.raises(sk.AssemblyMemoryBudgetError, match="budget exceeded"):
+    est = sk.estimate_bilinear_memory(_SizesBasis(40, 4, 4, 1, 30))
+    with pytest.raises(sk.AssemblyMemoryBudgetError, match="budget exceeded") as captured:
         sk.enforce_memory_budget(est, 100)
+    assert captured.value.estimate == est and captured.value.required_bytes > 100
+    assert captured.value.largest_allocation in str(captured.value) and "local_dofs=4x4" in str(captured.value)
     sk.enforce_memory_budget(est, 10 ** 9)
-    with pytest.raises(ValueError):
-        sk.enforce_memory_budget(est, -1)
+    sk.enforce_memory_budget(est, None)
+    with pytest.raises(ValueError, match="positive"):
+        sk.enforce_memory_budget(est, 0)
+    with pytest.raises(TypeError, match="integer or None"):
+        sk.enforce_memory_budget(est, 1.5e9)
+    with pytest.raises(TypeError, match="integer or None"):
+        sk.enforce_memory_budget(est, True)
+    with pytest.raises(ValueError, match="memory_safety_factor"):  # checked even without a budget
+        sk.enforce_memory_budget(est, None, safety_factor=0.5)
     assert issubclass(sk.AssemblyMemoryBudgetError, MemoryError)
+
+
+def test_memory_estimate_counts_this_backends_allocations():
+    """The reference's preflight contract (tests/test_memory_preflight.py:21-86) restated for the GPU
+    backend: the fields keep their names and count the int32 device DOF maps and CSR, the float64 element
+    matrices (E x Lr x Lc, as the reference's scatter map), the page-locked host matrix and one copy, the
+    row incidence, and per-call staging.  A vector space scales the element matrices by 9; a cross
+    estimate has its own kind and local sizes; what the basis already holds moves from the incremental
+    bytes to basis_bytes, leaving the total unchanged."""
+    E, Q, N = 96, 4, 60
+    b = _SizesBasis(E, Q, 4, 1, N)
+    est = sk.estimate_bilinear_memory(b)
+    L = 4
+    nnz = min(N * N, E * L * L)
+    assert est.kind == "bilinear" and est.rows == est.columns == N
+    assert est.nnz_upper_bound == nnz
+    assert est.scatter_bytes == E * L * L * 8
+    assert est.dof_map_bytes == E * L * 4 * 3  # the basis's device map and the pattern's two copies
+    assert est.native_tabulation_bytes == E * Q * (4 * 4 + 7) * 8
+    assert est.csr_bytes_upper_bound == 4 * (N + 1) + 12 * nnz + 2 * (12 * nnz + 8 * (N + 1))
+    assert est.staging_bytes_upper_bound == 16 * 8 * E + 2 * 9 * E * Q * 8
+    assert est.basis_bytes == b.element_dofs.nbytes + b.W.nbytes
+    assert est.construction_peak_total_bytes_upper_bound > est.basis_bytes
+    assert est.construction_peak_incremental_bytes_upper_bound > est.persistent_incremental_bytes_upper_bound
+    assert "MiB" in sk.format_bytes(2 ** 20)
+
+    vec = sk.estimate_bilinear_memory(_SizesBasis(E, Q, 4, 3, 3 * N))
+    assert vec.row_local_dofs == 3 * est.row_local_dofs and vec.scatter_bytes == 9 * est.scatter_bytes
+    assert vec.construction_peak_incremental_bytes_upper_bound > est.construction_peak_incremental_bytes_upper_bound
+
+    cross = sk.estimate_bilinear_memory(_SizesBasis(E, Q, 4, 3, 3 * N), b)
+    assert cross.kind == "cross-bilinear" and (cross.row_local_dofs, cross.column_local_dofs) == (12, 4)
+    assert cross.scatter_bytes == E * 12 * 4 * 8
+    with pytest.raises(ValueError, match="quadrature shapes must match"):
+        sk.estimate_bilinear_memory(b, _SizesBasis(E, Q + 1, 4, 1, N))
+    with pytest.raises(TypeError):
+        sk.estimate_bilinear_memory(object())
+
+    # once the basis holds its device map and tabulation they count as basis bytes
+    b._dofs_dev = np.zeros((E, L), dtype=np.int32)
+    b._tab = {"shape": np.zeros((E, Q, 4)), "grad": np.zeros((E, Q, 4, 3)), "dx": np.zeros((E, Q)),
+              "x": np.zeros((E, Q, 3)), "det": np.zeros((E, Q)), "tol": np.zeros((E, Q)),
+              "cond": np.zeros((E, Q))}
+    held = sk.estimate_bilinear_memory(b)
+    assert held.native_tabulation_bytes == 0 and held.dof_map_bytes == E * L * 4 * 2
+    assert held.basis_bytes > est.basis_bytes
+    assert held.construction_peak_total_bytes_upper_bound == est.construction_peak_total_bytes_upper_bound
+
+    peak = est.construction_peak_total_bytes_upper_bound
+    assert est.fits_in(peak, safety_factor=1.0) and not est.fits_in(peak, safety_factor=1.01)
+    with pytest.raises(ValueError, match="at least 1"):
+        est.fits_in(peak, safety_factor=0.9)
 
 
 def test_no_product_module_imports_oracle():
@@ -243,6 +320,26 @@ def test_coefficient_classification_routes_fused_and_tabulated_paths():
         per_element(np.ones((E + 1, Q)), E, Q, "value")
     with pytest.raises(ValueError):
         per_point(np.ones((E, Q + 1)), E, Q, "value")
+
+
+def test_component_access_errors_raise_before_assembly():
+    """A missing parameter, an out-of-range component and a non-integer component index raise the
+    reference's ValueErrors (tests/test_coefficient_components.py:122-138) while the form is traced or
+    its coefficients evaluated, before anything reaches a basis or the device."""
+    @sk.BilinearForm
+    def indexed(u, v, w):
+        return w.material[2] * dot(u, v)
+
+    @sk.BilinearForm
+    def noninteger(u, v, w):
+        return w.material["stiffness"] * dot(u, v)
+
+    with pytest.raises(ValueError, match="missing form parameter 'material'"):
+        sk.asm(indexed, None)
+    with pytest.raises(ValueError, match="has no component 2"):
+        sk.asm(indexed, None, material=np.ones((2, 3, 4)))
+    with pytest.raises(ValueError, match="component index must be an integer"):
+        sk.asm(noninteger, None)
 
 
 def test_coefficient_evaluation_factor_and_squeeze():
