@@ -353,6 +353,45 @@ int skg_n1_vector_load(const skg_pattern *pattern, const double *d_p, int64_t np
                        int32_t nq, const double *h_X, const double *h_W,
                        const double *d_f, double *d_out, void *stream);
 
+/* N1 element matrices d_out (E, 6, 6), row = test edge, FP64: the
+ * assembly's element pass written to the caller's buffer.  Replaces
+ * integrate_tet_n1 (cpp/src/assembly/edge_topology.cpp:156-233, bound in
+ * cpp/src/bindings.cpp) and AffineTetN1Basis.element_mass_matrices /
+ * element_curl_curl_matrices (python/skfemntv/hcurl_basis.py:376-386).
+ * d_mass / d_curl: NULL for 1, else per element (E) for coef_per_point 0
+ * or per point (E, Q) for 1; include flags select the terms. */
+int skg_n1_element_matrices(const double *d_p, int64_t npts, const int32_t *d_t,
+                            const int8_t *d_signs, int64_t n_elements, int32_t nq,
+                            const double *h_X, const double *h_W, const double *d_mass,
+                            const double *d_curl, int32_t coef_per_point,
+                            int32_t include_mass, int32_t include_curl, double *d_out,
+                            void *stream);
+
+/* A global edge field u (n_edges) at the rule's points h_X (3, Q), written
+ * component-first to d_out (3, E, Q): values (curl 0) or vector curls
+ * (curl 1) of the mapped, oriented basis.  Replaces AffineTetN1Basis
+ * .evaluate / .evaluate_curl (python/skfemntv/hcurl_basis.py:418-432).
+ * d_elem_edges (6, E) int32, d_signs (6, E) int8. */
+int skg_n1_evaluate(const double *d_p, int64_t npts, const int32_t *d_t,
+                    const int32_t *d_elem_edges, const int8_t *d_signs,
+                    int64_t n_elements, int64_t n_edges, int32_t nq, const double *h_X,
+                    const double *d_coefficients, int32_t curl, double *d_out,
+                    void *stream);
+
+/* Edge-moment interpolation, AffineTetN1Basis.interpolate_edge_moments
+ * (python/skfemntv/hcurl_basis.py:388-416), in two device passes around the
+ * caller's field: skg_n1_edge_points writes x = p_a + (p_b - p_a) t_q for
+ * each global edge (a, b) of d_edges (2, n_edges) int32 and parameter h_param
+ * (Q) to d_out (3, n_edges * Q), edge-major; skg_n1_edge_moments sums
+ * m = sum_q w_q f(x_q) . (p_b - p_a) over the field values d_values
+ * (3, n_edges * Q) into d_out (n_edges). */
+int skg_n1_edge_points(const double *d_p, int64_t npts, const int32_t *d_edges,
+                       int64_t n_edges, int32_t nq, const double *h_param, double *d_out,
+                       void *stream);
+int skg_n1_edge_moments(const double *d_p, int64_t npts, const int32_t *d_edges,
+                        int64_t n_edges, int32_t nq, const double *h_weights,
+                        const double *d_values, double *d_out, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Linear forms.  Replaces LinearFormAssembler.assemble                 */
 /* (cpp/src/assembly/linear_form_assembler.cpp:41-154):                 */

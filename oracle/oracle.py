@@ -500,6 +500,47 @@ def n1_assemble_maxwell(b: OracleN1Basis, mass_coefficient=None, curl_coefficien
     return data, indptr, indices
 
 
+def n1_element_matrices(b: OracleN1Basis, mass_coefficient=None, curl_coefficient=None, include_mass=True,
+                        include_curl=True):
+    """integrate_tet_n1 (edge_topology.cpp:156-233), the (E, 6, 6) element
+    matrices; with one term included these are
+    AffineTetN1Basis.element_mass_matrices / element_curl_curl_matrices
+    (hcurl_basis.py:376-386)."""
+    E, Q = b.dx.shape
+    mass = np.ascontiguousarray(np.broadcast_to(
+        np.asarray(1.0 if mass_coefficient is None else mass_coefficient, dtype=np.float64), (E, Q)))
+    curl = np.ascontiguousarray(np.broadcast_to(
+        np.asarray(1.0 if curl_coefficient is None else curl_coefficient, dtype=np.float64), (E, Q)))
+    el = np.empty((E, 6, 6))
+    lib().fo_integrate_tet_n1(b.values, b.curls, np.ascontiguousarray(b.dx), mass, curl, E, Q,
+                              int(include_mass), int(include_curl), 1, el)
+    return el
+
+
+def n1_evaluate(b: OracleN1Basis, coefficients, curl=False):
+    """AffineTetN1Basis.evaluate / evaluate_curl (hcurl_basis.py:418-432):
+    the global edge field at the rule's points, (3, E, Q)."""
+    local = np.asarray(coefficients, dtype=np.float64)[b.element_dofs].T
+    return np.einsum("eb,ebiq->ieq", local, b.curls if curl else b.values)
+
+
+def n1_interpolate_edge_moments(p, edges, field, quadrature_order=4):
+    """AffineTetN1Basis.interpolate_edge_moments (hcurl_basis.py:388-416):
+    Gauss-Legendre tangential moments along each ascending global edge, the
+    field called once per edge."""
+    nodes, weights = np.polynomial.legendre.leggauss(int(quadrature_order))
+    param = 0.5 * (nodes + 1.0)
+    weights = 0.5 * weights
+    out = np.empty(edges.shape[1])
+    for k, (a, b) in enumerate(edges.T):
+        first = p[:, a]
+        tangent = p[:, b] - first
+        pts = first[:, None] + tangent[:, None] * param[None, :]
+        vals = np.broadcast_to(np.asarray(field(pts), dtype=np.float64), pts.shape)
+        out[k] = np.einsum("iq,i,q->", vals, tangent, weights)
+    return out
+
+
 def n1_vector_load(b: OracleN1Basis, f):
     """TetN1LinearAssembler.assemble_vector_load (hcurl_assembler.py:218-246):
     local_eb = sum_iq phi_ebiq f_ieq dx_eq, summed into the edge DOFs in

@@ -703,3 +703,165 @@ extern "C" int skg_n1_vector_load(const skg_pattern *pat, const double *d_p, int
         gather_element_vectors(pat, le.get(), d_out, s);
     });
 }
+
+// ------------------------------------------------------------------ basis evaluation
+
+// A global edge field at the rule's points, component-first (3, E, Q):
+// values sum_a u[dof(e, a)] s_a (lam_i b_j - lam_j b_i) / det J (covariant
+// Piola of the Whitney functions, b_k = det J grad lam_k), curls
+// sum_a u[dof(e, a)] s_a J c_a / det J.  One thread per (element, point).
+__global__ void k_n1_evaluate(int64_t ne, const double *__restrict__ p, int64_t npts, const int32_t *__restrict__ t,
+                              const int32_t *__restrict__ elem_edges, const int8_t *__restrict__ signs,
+                              int64_t n_edges, int nq, const double *__restrict__ Xq,
+                              const double *__restrict__ coef, int want_curl, double *__restrict__ out) {
+    const int64_t total = ne * nq;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int64_t e = i / nq;
+    const int q = (int)(i - e * nq);
+    double J[9], b[4][3], det;
+    n1_geometry(p, npts, t, ne, e, J, b, det);
+    double u[6];
+    for (int a = 0; a < 6; ++a) {
+        const int32_t d = elem_edges[a * ne + e];
+        // an edge id outside [0, n_edges) never reaches memory: the point becomes NaN
+        u[a] = d >= 0 && d < n_edges ? coef[d] * (double)signs[a * ne + e] : __longlong_as_double(0x7ff8000000000000LL);
+    }
+    double v[3] = {0.0, 0.0, 0.0};
+    if (want_curl) {
+        for (int a = 0; a < 6; ++a)
+            for (int r = 0; r < 3; ++r)
+                v[r] += u[a] * (J[r * 3 + 0] * kRefCurl[a][0] + J[r * 3 + 1] * kRefCurl[a][1] +
+                                J[r * 3 + 2] * kRefCurl[a][2]) / det;
+    } else {
+        const double x = Xq[q], y = Xq[nq + q], z = Xq[2 * nq + q];
+        const double lam[4] = {1.0 - x - y - z, x, y, z};
+        for (int a = 0; a < 6; ++a) {
+            const int k = kEdge[a][0], l = kEdge[a][1];
+            for (int r = 0; r < 3; ++r) v[r] += u[a] * (lam[k] * b[l][r] - lam[l] * b[k][r]) / det;
+        }
+    }
+    out[i] = v[0];
+    out[total + i] = v[1];
+    out[2 * total + i] = v[2];
+}
+
+// Points along each global edge, x = p_first + (p_second - p_first) t_q,
+// component-first (3, n_edges * nq), edge-major.  Rounded as the product
+// then the sum (no fused multiply-add), as the same expression on the host.
+__global__ void k_edge_points(int64_t n_edges, int nq, const double *__restrict__ p, int64_t npts,
+                              const int32_t *__restrict__ edges, const double *__restrict__ param,
+                              double *__restrict__ out) {
+    const int64_t total = n_edges * nq;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int64_t k = i / nq;
+    const int q = (int)(i - k * nq);
+    const int32_t a = edges[k], b = edges[n_edges + k];
+    const bool ok = a >= 0 && a < npts && b >= 0 && b < npts;
+    for (int r = 0; r < 3; ++r) {
+        const double first = ok ? p[r * npts + a] : __longlong_as_double(0x7ff8000000000000LL);
+        const double tangent = ok ? __dsub_rn(p[r * npts + b], first) : first;
+        out[r * total + i] = __dadd_rn(first, __dmul_rn(tangent, param[q]));
+    }
+}
+
+// Tangential moments m_k = sum_q w_q f(x_q) . (p_second - p_first) of a
+// field sampled at k_edge_points' points, one thread per edge.
+__global__ void k_edge_moments(int64_t n_edges, int nq, const double *__restrict__ p, int64_t npts,
+                               const int32_t *__restrict__ edges, const double *__restrict__ weights,
+                               const double *__restrict__ f, double *__restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_edges) return;
+    const int32_t a = edges[k], b = edges[n_edges + k];
+    if (!(a >= 0 && a < npts && b >= 0 && b < npts)) {
+        out[k] = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
+    const int64_t total = n_edges * nq;
+    double tangent[3];
+    for (int r = 0; r < 3; ++r) tangent[r] = p[r * npts + b] - p[r * npts + a];
+    double m = 0.0;
+    for (int q = 0; q < nq; ++q) {
+        const int64_t i = k * nq + q;
+        m += weights[q] * (f[i] * tangent[0] + f[total + i] * tangent[1] + f[2 * total + i] * tangent[2]);
+    }
+    out[k] = m;
+}
+
+extern "C" int skg_n1_element_matrices(const double *d_p, int64_t npts, const int32_t *d_t, const int8_t *d_signs,
+                                       int64_t ne, int32_t nq, const double *h_X, const double *h_W,
+                                       const double *d_mass, const double *d_curl, int32_t coef_per_point,
+                                       int32_t include_mass, int32_t include_curl, double *d_out, void *stream) {
+    return guarded([&] {
+        require(ne >= 0 && nq > 0 && h_X && h_W, "quadrature rule is empty");
+        require(coef_per_point == 0 || coef_per_point == 1, "coefficient layout must be 0 (per element) or 1 (per point)");
+        require(ne == 0 || (d_p && d_t && d_signs && d_out), "mesh or output arrays are NULL");
+        if (ne == 0) return;
+        cudaStream_t s = as_stream(stream);
+        N1Table tab;
+        n1_table(nq, h_X, h_W, tab);
+        if (!coef_per_point) {
+            k_n1_elem_fast<<<grid_for(ne, kN1Block), kN1Block, 0, s>>>(ne, 0, ne, d_p, npts, d_t, d_signs, tab,
+                                                                      d_mass, d_curl, include_mass, include_curl,
+                                                                      d_out);
+            SKG_LAUNCH_CHECK("n1_element_matrices");
+            return;
+        }
+        std::vector<double> xw(4 * (size_t)nq);
+        for (int i = 0; i < 3 * nq; ++i) xw[i] = h_X[i];
+        for (int q = 0; q < nq; ++q) xw[3 * nq + q] = h_W[q];
+        DevBuf<double> dxw(xw.size(), s);
+        SKG_CUDA(cudaMemcpyAsync(dxw.get(), xw.data(), xw.size() * 8, cudaMemcpyHostToDevice, s));
+        k_n1_element<<<grid_for(ne, 128), 128, 0, s>>>(ne, d_p, npts, d_t, d_signs, nq, dxw.get(), dxw.get() + 3 * nq,
+                                                       tab, d_mass, d_curl, 1, include_mass, include_curl, d_out);
+        SKG_LAUNCH_CHECK("n1_element_matrices_pointwise");
+    });
+}
+
+extern "C" int skg_n1_evaluate(const double *d_p, int64_t npts, const int32_t *d_t, const int32_t *d_elem_edges,
+                               const int8_t *d_signs, int64_t ne, int64_t n_edges, int32_t nq, const double *h_X,
+                               const double *d_coefficients, int32_t curl, double *d_out, void *stream) {
+    return guarded([&] {
+        require(ne >= 0 && n_edges >= 0 && nq > 0 && h_X, "quadrature rule is empty");
+        require(ne == 0 || (d_p && d_t && d_elem_edges && d_signs && d_coefficients && d_out),
+                "mesh, coefficient or output arrays are NULL");
+        if (ne == 0) return;
+        cudaStream_t s = as_stream(stream);
+        DevBuf<double> dX(3 * (size_t)nq, s);
+        SKG_CUDA(cudaMemcpyAsync(dX.get(), h_X, 3 * (size_t)nq * 8, cudaMemcpyHostToDevice, s));
+        k_n1_evaluate<<<grid_for(ne * nq, 256), 256, 0, s>>>(ne, d_p, npts, d_t, d_elem_edges, d_signs, n_edges, nq,
+                                                            dX.get(), d_coefficients, curl != 0, d_out);
+        SKG_LAUNCH_CHECK("n1_evaluate");
+    });
+}
+
+extern "C" int skg_n1_edge_points(const double *d_p, int64_t npts, const int32_t *d_edges, int64_t n_edges,
+                                  int32_t nq, const double *h_param, double *d_out, void *stream) {
+    return guarded([&] {
+        require(n_edges >= 0 && nq > 0 && h_param, "edge rule is empty");
+        require(n_edges == 0 || (d_p && d_edges && d_out), "mesh, edge or output arrays are NULL");
+        if (n_edges == 0) return;
+        cudaStream_t s = as_stream(stream);
+        DevBuf<double> dt((size_t)nq, s);
+        SKG_CUDA(cudaMemcpyAsync(dt.get(), h_param, (size_t)nq * 8, cudaMemcpyHostToDevice, s));
+        k_edge_points<<<grid_for(n_edges * nq, 256), 256, 0, s>>>(n_edges, nq, d_p, npts, d_edges, dt.get(), d_out);
+        SKG_LAUNCH_CHECK("edge_points");
+    });
+}
+
+extern "C" int skg_n1_edge_moments(const double *d_p, int64_t npts, const int32_t *d_edges, int64_t n_edges,
+                                   int32_t nq, const double *h_weights, const double *d_values, double *d_out,
+                                   void *stream) {
+    return guarded([&] {
+        require(n_edges >= 0 && nq > 0 && h_weights, "edge rule is empty");
+        require(n_edges == 0 || (d_p && d_edges && d_values && d_out), "mesh, edge, field or output arrays are NULL");
+        if (n_edges == 0) return;
+        cudaStream_t s = as_stream(stream);
+        DevBuf<double> dw((size_t)nq, s);
+        SKG_CUDA(cudaMemcpyAsync(dw.get(), h_weights, (size_t)nq * 8, cudaMemcpyHostToDevice, s));
+        k_edge_moments<<<grid_for(n_edges, 256), 256, 0, s>>>(n_edges, nq, d_p, npts, d_edges, dw.get(), d_values,
+                                                             d_out);
+        SKG_LAUNCH_CHECK("edge_moments");
+    });
+}

@@ -80,6 +80,11 @@ SIGNATURES = {
     "skg_cross_assemble_tabulated": [_vp, _i64, _i32, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp,
                                      _vp, _vp, _vp],
     "skg_n1_vector_load": [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp],
+    "skg_n1_element_matrices": [_vp, _i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp,
+                                _vp],
+    "skg_n1_evaluate": [_vp, _i64, _vp, _vp, _vp, _i64, _i64, _i32, _vp, _vp, _i32, _vp, _vp],
+    "skg_n1_edge_points": [_vp, _i64, _vp, _i64, _i32, _vp, _vp, _vp],
+    "skg_n1_edge_moments": [_vp, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _vp],
     "skg_pattern_row_groups": [_vp, ctypes.POINTER(ctypes.c_int32)],
     "skg_nh_assemble_surrogate": [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _vp, _vp, ctypes.c_float, _vp, _vp, _i64p, _vp],

@@ -134,6 +134,85 @@ class AffineTetN1Basis:
     def curls(self):
         return self._mapped()[1].transpose(1, 2, 0, 3)
 
+    # ------------------------------------------------------------ device evaluation
+    def _element_matrices(self, include_mass, include_curl):
+        E, Q = self.dx.shape
+        out = dev.empty((E, 6, 6), np.float64)
+        call("skg_n1_element_matrices", dev.ptr(self.mesh._dev("p")), self.mesh.p.shape[1], dev.ptr(self._t4),
+             dev.ptr(self._signs_dev), E, Q, dev.hptr(self.X), dev.hptr(self.W), None, None, 0,
+             int(include_mass), int(include_curl), dev.ptr(out), dev.stream_ptr())
+        return out.cpu().numpy()
+
+    def element_mass_matrices(self):
+        """(E, 6, 6) element mass matrices sum_q dx v_a . v_c
+        (hcurl_basis.py:376-380), computed on the device."""
+        return self._element_matrices(True, False)
+
+    def element_curl_curl_matrices(self):
+        """(E, 6, 6) element curl-curl matrices sum_q dx c_a . c_c
+        (hcurl_basis.py:382-386), computed on the device."""
+        return self._element_matrices(False, True)
+
+    def _edges_device(self):
+        if not hasattr(self, "_edges_dev"):
+            self._edges_dev = dev.to_device(self.dof_map.topology.edges, np.int32)  # (2, n_edges)
+        return self._edges_dev
+
+    def interpolate_edge_moments(self, field, *, quadrature_order=4):
+        """Interpolate a vector field by tangential moments along the
+        ascending global edges (hcurl_basis.py:388-416): for edge (a, b),
+        m = sum_q w_q field(x_q) . (p_b - p_a) on the Gauss-Legendre rule of
+        ``quadrature_order`` points mapped to the edge.  The points are made
+        and the moments summed on the device; ``field`` is called once, with
+        the points of every edge as one (3, n_edges * order) array, edge-major
+        (the reference calls it once per edge with (3, order))."""
+        if not callable(field):
+            raise TypeError("field must be callable")
+        if (isinstance(quadrature_order, bool) or not isinstance(quadrature_order, (int, np.integer))
+                or quadrature_order < 1):
+            raise ValueError("quadrature_order must be a positive integer")
+        nodes, weights = np.polynomial.legendre.leggauss(int(quadrature_order))
+        param = np.ascontiguousarray(0.5 * (nodes + 1.0))
+        weights = np.ascontiguousarray(0.5 * weights)
+        n_edges, nq = self.N, len(param)
+        p, npts = dev.ptr(self.mesh._dev("p")), self.mesh.p.shape[1]
+        edges = dev.ptr(self._edges_device()) if n_edges else None
+        points = dev.empty((3, n_edges * nq), np.float64)
+        call("skg_n1_edge_points", p, npts, edges, n_edges, nq, dev.hptr(param), dev.ptr(points), dev.stream_ptr())
+        x = points.cpu().numpy()
+        values = np.asarray(field(x), dtype=np.float64)
+        try:
+            values = np.broadcast_to(values, x.shape)
+        except ValueError as error:
+            raise ValueError("field must return vectors broadcastable to (3, points)") from error
+        d_values = dev.to_device(values, np.float64)
+        out = dev.empty(max(1, n_edges), np.float64)
+        call("skg_n1_edge_moments", p, npts, edges, n_edges, nq, dev.hptr(weights), dev.ptr(d_values),
+             dev.ptr(out), dev.stream_ptr())
+        return out[:n_edges].cpu().numpy()
+
+    def _evaluate(self, coefficients, curl):
+        u = np.asarray(coefficients, dtype=np.float64)
+        if u.shape != (self.N,):
+            raise ValueError(f"coefficients must have shape ({self.N},)")
+        E, Q = self.dx.shape
+        out = dev.empty((3, E, Q), np.float64)
+        d_u = dev.to_device(u, np.float64)
+        call("skg_n1_evaluate", dev.ptr(self.mesh._dev("p")), self.mesh.p.shape[1], dev.ptr(self._t4),
+             dev.ptr(self._ee_dev), dev.ptr(self._signs_dev), E, self.N, Q, dev.hptr(self.X), dev.ptr(d_u),
+             int(curl), dev.ptr(out), dev.stream_ptr())
+        return out.cpu().numpy()
+
+    def evaluate(self, coefficients):
+        """A global edge field at the rule's points, (component, cell, point)
+        (hcurl_basis.py:424-427), computed on the device."""
+        return self._evaluate(coefficients, False)
+
+    def evaluate_curl(self, coefficients):
+        """Its vector curl, (component, cell, point) (hcurl_basis.py:429-432),
+        computed on the device."""
+        return self._evaluate(coefficients, True)
+
 
 def estimate_tet_n1_assembly_memory(basis):
     if not isinstance(basis, AffineTetN1Basis):
