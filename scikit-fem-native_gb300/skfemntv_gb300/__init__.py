@@ -16,7 +16,8 @@ from .element import ElementTetP1, ElementTetP2, ElementVector
 from .errors import UnsupportedNativeForm
 from .forms import BilinearForm, LinearForm, asm, ddot, div, dot, grad, inner, mul, sym_grad
 from .hyperelastic import EnergySurrogate, NeoHookean
-from .hcurl import (AffineTetN1Basis, HcurlTetGeometryDiagnostics, TetN1Assembler, TetN1LinearAssembler,
+from .hcurl import (AffineTetN1Basis, HcurlTetGeometryDiagnostics, OrientedEdgeDofMap, OrientedEdgeTopology,
+                    TetN1Assembler, TetN1LinearAssembler, build_oriented_edge_dof_map, build_oriented_edge_topology,
                     estimate_tet_n1_assembly_memory)
 from .mesh import MeshTet, MeshTet2
 from .preflight import (AssemblyMemoryBudgetError, AssemblyMemoryEstimate, enforce_memory_budget,
@@ -30,7 +31,8 @@ __all__ = [
     "AssemblyGraph", "NativeBilinearForm", "NativeCrossBilinearForm", "NativeLinearForm",
     "AffineTetN1Basis", "AssemblyMemoryBudgetError", "AssemblyMemoryEstimate", "BACKEND", "Basis",
     "BilinearForm", "CAPABILITIES", "ElementTetP1", "ElementTetP2", "ElementVector", "GeometryDiagnostics",
-    "HcurlTetGeometryDiagnostics", "LinearForm", "EnergySurrogate", "MeshTet", "MeshTet2", "NeoHookean", "P1Energy", "TetN1Assembler", "TetN1LinearAssembler",
+    "HcurlTetGeometryDiagnostics", "LinearForm", "OrientedEdgeDofMap", "OrientedEdgeTopology",
+    "build_oriented_edge_dof_map", "build_oriented_edge_topology", "EnergySurrogate", "MeshTet", "MeshTet2", "NeoHookean", "P1Energy", "TetN1Assembler", "TetN1LinearAssembler",
     "UnsupportedNativeForm", "asm", "available_num_threads", "ddot", "div", "dot", "enforce_memory_budget",
     "estimate_bilinear_memory", "estimate_tet_n1_assembly_memory", "format_bytes", "get_num_threads",
     "grad", "has_capability", "inner", "mul", "set_num_threads", "sym_grad", "thread_limit",

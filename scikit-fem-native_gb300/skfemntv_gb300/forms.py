@@ -528,4 +528,4 @@ def asm(form, *bases, num_threads=None, memory_limit_bytes=None, memory_safety_f
             memory_safety_factor=memory_safety_factor)
     raise TypeError(
         "skfemntv_gb300.asm accepts forms created by skfemntv_gb300.LinearForm or "
-        "skfemntv_gb300.BilinearForm")
+        "skfemntv_gb300.BilinearForm; use skfem.asm explicitly for scikit-fem forms")

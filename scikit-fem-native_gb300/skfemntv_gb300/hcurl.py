@@ -45,6 +45,45 @@ class OrientedEdgeDofMap:
     def basis_signs(self):
         return self.topology.element_edge_signs
 
+    def local_coefficients(self, global_coefficients):
+        """Global edge moments (n_edges,) to coefficients of the oriented local
+        bases, (6, E) (edge_dof_map.py:34-41)."""
+        values = np.asarray(global_coefficients)
+        if values.ndim != 1 or values.shape[0] != self.ndofs:
+            raise ValueError(f"global edge coefficients must have shape ({self.ndofs},)")
+        return self.basis_signs * values[self.element_dofs]
+
+    def global_moments_from_local(self, local_coefficients):
+        """Per-cell global-oriented moments from local coefficients (6, E),
+        cells not merged (edge_dof_map.py:43-51)."""
+        values = np.asarray(local_coefficients)
+        if values.shape != self.element_dofs.shape:
+            raise ValueError(f"local edge coefficients must have shape {self.element_dofs.shape}")
+        return self.basis_signs * values
+
+
+def build_oriented_edge_topology(mesh):
+    """Global edges of a tetrahedral mesh's corners, numbered first-seen in
+    cell-major, local-edge-major order with ascending vertex pairs, and the
+    sign of each directed local edge against its global one
+    (edge_topology.py:33-63), computed on the device.  Edge nodes of a
+    quadratic mesh do not change edge identity."""
+    if int(mesh.dim()) != 3:
+        raise NotImplementedError("oriented edge topology supports tetrahedra")
+    if mesh.t.shape[0] < 4:
+        raise ValueError("mesh connectivity does not contain all corner vertices")
+    if hasattr(mesh, "_dev"):
+        t4 = mesh._dev("t")[:4].contiguous()
+    else:  # any object with a connectivity ``t`` and ``dim()``
+        t4 = dev.to_device(np.asarray(mesh.t)[:4], np.int32)
+    edges, ee, sg = oriented_edges(t4, int(t4.shape[1]))
+    return OrientedEdgeTopology(edges, ee.cpu().numpy().astype(np.int64), sg.cpu().numpy(), quad.TET_EDGES)
+
+
+def build_oriented_edge_dof_map(mesh):
+    """One scalar DOF per global edge (edge_dof_map.py:54-55)."""
+    return OrientedEdgeDofMap(build_oriented_edge_topology(mesh))
+
 
 @dataclass(frozen=True)
 class HcurlTetGeometryDiagnostics:

@@ -1,7 +1,8 @@
 """The Nedelec basis beyond assembly, on the GPU: element matrices, evaluation of edge fields and their
-curls, and edge-moment interpolation, against the oracle (same seeded inputs) and with the reference's
-own cases (tests/test_hcurl_tet_basis.py, test_hcurl_tet_interpolation.py,
-test_hcurl_tet_robustness.py)."""
+curls, edge-moment interpolation, the oriented edge topology and the edge DOF map, against the oracle
+(same seeded inputs) and with the reference's own cases (tests/test_hcurl_tet_basis.py,
+test_hcurl_tet_interpolation.py, test_hcurl_tet_robustness.py, test_edge_topology.py,
+test_edge_dof_map.py)."""
 import numpy as np
 import pytest
 from scipy.sparse import coo_matrix
@@ -188,3 +189,67 @@ def test_mixed_orientation_preserves_interpolant_and_error_norms():
         ce = b.evaluate_curl(c) - exact_curl(b.global_coordinates)
         norms.append((np.einsum("ieq,ieq,eq->", ve, ve, b.dx), np.einsum("ieq,ieq,eq->", ce, ce, b.dx)))
     np.testing.assert_allclose(norms[0], norms[1], atol=3e-14)
+
+
+def _assert_local_orientation(t, topo):
+    """Each directed local edge is its global edge, reversed where its sign is -1
+    (tests/test_edge_topology.py:11-18)."""
+    for cell in range(t.shape[1]):
+        for local, (start, end) in enumerate(topo.local_edges):
+            directed = (int(t[start, cell]), int(t[end, cell]))
+            edge = tuple(int(v) for v in topo.edges[:, topo.element_edges[local, cell]])
+            assert directed == (edge if topo.element_edge_signs[local, cell] == 1 else edge[::-1])
+
+
+def test_edge_topology_and_dof_map_contracts():
+    """tests/test_edge_topology.py:21-79 and test_edge_dof_map.py:14-76 on tetrahedra: unique ascending
+    global edges, local orientation signs, numbering equal to the oracle's first-seen one, vertex
+    reordering keeping the edge set, local/global coefficient round trips (a shared edge gives every cell
+    the same moment), and the shape and repeated-corner errors."""
+    from skfemntv_gb300.edge_dof_map import build_oriented_edge_dof_map
+    from skfemntv_gb300.edge_topology import build_oriented_edge_topology
+
+    one = sk.MeshTet()
+    topo = build_oriented_edge_topology(one)
+    assert topo.element_edges.shape == (6, 1)
+    assert len(set(map(tuple, topo.edges.T))) == topo.edges.shape[1] == 6
+    _assert_local_orientation(one.t, topo)
+
+    cube = _cube(2)
+    reordered = sk.MeshTet(cube.p, cube.t[[1, 0, 2, 3]])
+    tops = [build_oriented_edge_topology(m) for m in (cube, reordered)]
+    for m, t in zip((cube, reordered), tops):
+        assert set(np.unique(t.element_edge_signs)) <= {-1, 1}
+        assert np.all(t.edges[0] < t.edges[1])
+        _assert_local_orientation(m.t, t)
+        edges, ee, sg = O.edge_topology(m.t)
+        assert np.array_equal(t.edges, edges) and np.array_equal(t.element_edges, ee)
+        assert np.array_equal(t.element_edge_signs, sg)
+    assert set(map(tuple, tops[0].edges.T)) == set(map(tuple, tops[1].edges.T))
+
+    for m in (cube, reordered):
+        dofs = build_oriented_edge_dof_map(m)
+        assert dofs.ndofs == dofs.topology.edges.shape[1]
+        values = np.array([10.0 * a + b for a, b in dofs.topology.edges.T])
+        recovered = dofs.global_moments_from_local(dofs.local_coefficients(values))
+        np.testing.assert_array_equal(recovered, values[dofs.element_dofs])
+    counts = np.bincount(dofs.element_dofs.ravel(), minlength=dofs.ndofs)
+    shared = int(np.flatnonzero(counts >= 2)[0])
+    ordinal = np.arange(1.0, dofs.ndofs + 1.0)
+    recovered = dofs.global_moments_from_local(dofs.local_coefficients(ordinal))
+    for local, cell in np.argwhere(dofs.element_dofs == shared):
+        assert recovered[local, cell] == ordinal[shared]
+    with pytest.raises(ValueError, match="global edge coefficients"):
+        dofs.local_coefficients(np.zeros((dofs.ndofs, 1)))
+    with pytest.raises(ValueError, match="local edge coefficients"):
+        dofs.global_moments_from_local(np.zeros(dofs.ndofs))
+
+    class _RepeatedCorner:
+        t = np.array([[0], [0], [1], [2]], dtype=np.int64)
+
+        @staticmethod
+        def dim():
+            return 3
+
+    with pytest.raises(ValueError, match="cell 0 repeats a corner vertex"):
+        build_oriented_edge_topology(_RepeatedCorner())
