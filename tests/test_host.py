@@ -109,6 +109,28 @@ def test_unsupported_forms_raise():
         dot(mul(np.eye(3), grad(u)), grad(u))
 
 
+def test_public_api_contract():
+    """tests/test_public_api_contract.py:11-64: exports unique and resolvable, no solver policy exported, an
+    unsupported form raises UnsupportedNativeForm with no fallback, and the reference's module paths for
+    the edge topology and DOF map resolve."""
+    assert len(sk.__all__) == len(set(sk.__all__))
+    for name in sk.__all__:
+        assert hasattr(sk, name), name
+    assert not hasattr(sk, "solve") and not hasattr(sk, "condense")
+
+    @sk.BilinearForm
+    def unsupported(u, v, w):
+        return u
+
+    with pytest.raises(sk.UnsupportedNativeForm):
+        sk.asm(unsupported, None)
+    from skfemntv_gb300.edge_dof_map import build_oriented_edge_dof_map
+    from skfemntv_gb300.edge_topology import build_oriented_edge_topology
+
+    assert build_oriented_edge_topology is sk.build_oriented_edge_topology
+    assert build_oriented_edge_dof_map is sk.build_oriented_edge_dof_map
+
+
 def test_asm_rejects_foreign_forms():
     with pytest.raises(TypeError):
         sk.asm(object(), None)
