@@ -253,3 +253,15 @@ def test_edge_topology_and_dof_map_contracts():
 
     with pytest.raises(ValueError, match="cell 0 repeats a corner vertex"):
         build_oriented_edge_topology(_RepeatedCorner())
+
+
+def test_n1_on_a_quadratic_mesh_uses_its_corners():
+    """A ten-node mesh gives the same edges and matrices as its corner mesh (hcurl_basis.py:295-306: the
+    basis reads the four corner rows only)."""
+    cube = _cube(2)
+    b4 = sk.AffineTetN1Basis(cube)
+    b10 = sk.AffineTetN1Basis(sk.MeshTet2.from_mesh(cube))
+    assert np.array_equal(b4.dof_map.topology.edges, b10.dof_map.topology.edges)
+    K4 = sk.TetN1Assembler(b4).assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2).copy()
+    K10 = sk.TetN1Assembler(b10).assemble_maxwell(mass_coefficient=1.3, curl_coefficient=0.2)
+    assert np.array_equal(K4.indices, K10.indices) and np.array_equal(K4.data, K10.data)

@@ -132,6 +132,68 @@ def test_p2_anisotropic_per_point_tabulated_path():
     assert relerr(K.data, data) < RTOL
 
 
+def test_curved_p2_geometry_takes_the_tabulated_path():
+    """Edge nodes moved off their edges' midpoints make the quadratic map curved (isoparametric, all ten
+    nodes: basis.py:2194-2294): the basis is not affine and every form runs the tabulated kernels.
+    Geometry bit for bit with the oracle; Laplace, anisotropic tensor, mass and load on scalar P2,
+    elasticity on vector P2, and P1 on the ten-node mesh (which keeps the quadratic geometry map,
+    basis.py:2274-2283) against the oracle."""
+    g = load_golden("p2_aniso")
+    t = g["t"]
+    p = g["p"].copy()
+    edge_nodes = np.unique(t[4:])
+    p[:, edge_nodes] += 0.02 * np.random.default_rng(9).uniform(-1.0, 1.0, (3, len(edge_nodes)))
+    m = sk.MeshTet2(p, t)
+    XW = (g["X"], g["W"])
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=XW)
+    assert not b.is_affine
+    ob = O.make_basis(p, t, True, quadrature=XW)
+    assert np.array_equal(b.dx, ob.dx) and np.array_equal(b.tabulated_gradients, ob.grad)
+    assert np.array_equal(b.global_coordinates, ob.x)
+    E, Q = b._coefficient_shape
+
+    K = sk.asm(lap, b)
+    d, indptr, indices = O.bilinear_assemble(ob, gradient=1.0)
+    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
+    assert relerr(K.data, d) < RTOL
+    A = g["A"]  # per element (E, 3, 3)
+    Apub = np.broadcast_to(np.moveaxis(A, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    want, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(Apub, (E, Q)))
+    assert relerr(sk.asm(aniso, b, A=Apub).data, want) < RTOL
+
+    @sk.BilinearForm
+    def mass(u, v, w):
+        return dot(u, v)
+
+    @sk.LinearForm
+    def load(v, w):
+        return dot(w.f, v)
+
+    assert relerr(sk.asm(mass, b).data, O.bilinear_assemble(ob, value=1.0)[0]) < RTOL
+    f = 1.0 + np.sin(3.0 * ob.x[..., 0]) * ob.x[..., 1]
+    assert relerr(sk.asm(load, b, f=f), O.linear_assemble(ob, value=f[..., None])) < RTOL
+
+    @sk.BilinearForm
+    def elasticity(u, v, w):
+        return 2.0 * ddot(sym_grad(u), sym_grad(v)) + 10.0 * div(u) * div(v)
+
+    bv = sk.Basis(m, sk.ElementVector(sk.ElementTetP2(), dim=3), quadrature=XW)
+    obv = O.make_basis(p, t, True, comp=3, quadrature=XW)
+    Kv = sk.asm(elasticity, bv)
+    dv, indptr_v, indices_v = O.bilinear_assemble(obv, symmetric_gradient=2.0, divergence=10.0)
+    assert np.array_equal(Kv.indptr, indptr_v) and np.array_equal(Kv.indices, indices_v)
+    assert relerr(Kv.data, dv) < RTOL
+
+    b1 = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=XW)
+    assert not b1.is_affine
+    ob1 = O.make_basis(p, t, False, quadrature=XW)
+    assert np.array_equal(b1.dx, ob1.dx)
+    K1 = sk.asm(lap, b1)
+    d1, indptr1, indices1 = O.bilinear_assemble(ob1, gradient=1.0)
+    assert np.array_equal(K1.indptr, indptr1) and np.array_equal(K1.indices, indices1)
+    assert relerr(K1.data, d1) < RTOL
+
+
 def test_p2_constant_tensor_combined_with_isotropic_term_and_rejections():
     """The reference's anisotropic-form cases (tests/test_anisotropic_forms.py:41-125) on P2 tets: a
     constant (3, 3) tensor gives a symmetric matrix equal to the oracle's; a nonsymmetric tensor summed
