@@ -732,18 +732,19 @@ __global__ void k_n1_evaluate(int64_t ne, const double *__restrict__ p, int64_t 
         for (int a = 0; a < 6; ++a)
             for (int r = 0; r < 3; ++r)
                 v[r] += u[a] * (J[r * 3 + 0] * kRefCurl[a][0] + J[r * 3 + 1] * kRefCurl[a][1] +
-                                J[r * 3 + 2] * kRefCurl[a][2]) / det;
+                                J[r * 3 + 2] * kRefCurl[a][2]);
     } else {
         const double x = Xq[q], y = Xq[nq + q], z = Xq[2 * nq + q];
         const double lam[4] = {1.0 - x - y - z, x, y, z};
         for (int a = 0; a < 6; ++a) {
             const int k = kEdge[a][0], l = kEdge[a][1];
-            for (int r = 0; r < 3; ++r) v[r] += u[a] * (lam[k] * b[l][r] - lam[l] * b[k][r]) / det;
+            for (int r = 0; r < 3; ++r) v[r] += u[a] * (lam[k] * b[l][r] - lam[l] * b[k][r]);
         }
     }
-    out[i] = v[0];
-    out[total + i] = v[1];
-    out[2 * total + i] = v[2];
+    const double inv = 1.0 / det;  // both sums carry the factor 1 / det J
+    out[i] = v[0] * inv;
+    out[total + i] = v[1] * inv;
+    out[2 * total + i] = v[2] * inv;
 }
 
 // Points along each global edge, x = p_first + (p_second - p_first) t_q,
