@@ -96,6 +96,31 @@ def test_n1_maxwell():
     assert rel(data, g["data"]) < 1e-14
 
 
+def test_n1_element_matrices_evaluation_and_interpolation():
+    """The oracle's N1 element matrices summed over the edge DOFs give the reference's Maxwell matrix;
+    edge-moment interpolation of a constant field gives the moments of its tangents, and evaluating them
+    gives the field back with zero curl (the reference's own interpolation test,
+    tests/test_hcurl_tet_interpolation.py:12-29)."""
+    g = load_golden("n1_maxwell")
+    nb = O.make_n1_basis(g["p"], g["t"])
+    el = O.n1_element_matrices(nb, 1.0, (1.0 / g["mu"])[:, None])
+    dofs = nb.element_dofs.T
+    K = np.zeros((nb.N, nb.N))
+    np.add.at(K, (np.repeat(dofs, 6, axis=1).ravel(), np.tile(dofs, (1, 6)).ravel()), el.ravel())
+    rows = np.repeat(np.arange(nb.N), np.diff(g["indptr"]))
+    assert rel(K[rows, g["indices"]], g["data"]) < 1e-14
+    mass = O.n1_element_matrices(nb, include_curl=False)
+    curl = O.n1_element_matrices(nb, include_mass=False)
+    assert rel(mass + curl, O.n1_element_matrices(nb)) < 1e-15
+    constant = np.array((1.25, -0.5, 0.75))
+    m = O.n1_interpolate_edge_moments(g["p"], nb.edges, lambda x: constant[:, None] + 0.0 * x)
+    tangents = g["p"][:, nb.edges[1]] - g["p"][:, nb.edges[0]]
+    np.testing.assert_allclose(m, constant @ tangents, atol=2e-15)
+    np.testing.assert_allclose(O.n1_evaluate(nb, m), np.broadcast_to(constant[:, None, None], (3,) + nb.dx.shape),
+                               atol=2e-14)
+    np.testing.assert_allclose(O.n1_evaluate(nb, m, curl=True), 0.0, atol=2e-14)
+
+
 def test_n1_vector_load():
     g = load_golden("n1_load")
     b = O.make_n1_basis(g["p"], g["t"])
