@@ -146,6 +146,17 @@ def main():
         lambda x: np.stack([np.sin(3.0 * x[0]), x[1] * x[2], np.cos(2.0 * x[2]) - x[0]])).copy()
     out["n1_load"] = dict(p=p_r, t=t_r, f=fq, load=load_arr, load_callable=load_fun, xq=nb.global_coordinates)
 
+    # --- Nedelec N1 basis on the same mesh, 3rd-order rule: element matrices, a seeded edge
+    #     field evaluated with its curl, edge-moment interpolation of a smooth field ---
+    nb3 = sk.AffineTetN1Basis(mr, intorder=3)
+    u_edges = np.random.default_rng(np.random.SeedSequence(37)).standard_normal(nb3.N)
+    moments = nb3.interpolate_edge_moments(
+        lambda x: np.stack([np.sin(3.0 * x[0]) + x[1], x[0] * x[2], np.cos(2.0 * x[2]) - x[0] * x[1]]),
+        quadrature_order=4)
+    out["n1_basis"] = dict(p=p_r, t=t_r, X=nb3.X, W=nb3.W, mass=nb3.element_mass_matrices(),
+                           curl_curl=nb3.element_curl_curl_matrices(), u=u_edges, values=nb3.evaluate(u_edges),
+                           curls=nb3.evaluate_curl(u_edges), moments=moments)
+
     # --- cross-basis assembly: P2 vector test x P1 scalar trial (Stokes coupling),
     #     P2 x P1 scalar mass, and a full gradient tensor on vector P1 ---
     rng_c = np.random.default_rng(np.random.SeedSequence(41))

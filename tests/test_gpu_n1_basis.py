@@ -52,6 +52,21 @@ def test_n1_element_matrices_match_oracle_and_assembly():
     assert relerr(_scatter(gb, Mc).toarray(), Kc.toarray()) < 1e-13
 
 
+def test_n1_basis_against_the_reference():
+    """Fixture n1_basis, produced by the reference: element matrices, evaluation of a seeded edge field
+    and its curl, and edge-moment interpolation of a smooth field (3rd-order rule)."""
+    g = load_golden("n1_basis")
+    b = sk.AffineTetN1Basis(sk.MeshTet(g["p"], g["t"]), intorder=3)
+    # the rule comes from numpy's Gauss-Legendre nodes and weights, as the reference's does; numpy's weights
+    # on an Arm host differ from the x86 values in the fixture in the last bits
+    assert relerr(b.X, g["X"]) < 1e-15 and relerr(b.W, g["W"]) < 1e-15
+    assert relerr(b.element_mass_matrices(), g["mass"]) < RTOL
+    assert relerr(b.element_curl_curl_matrices(), g["curl_curl"]) < RTOL
+    assert relerr(b.evaluate(g["u"]), g["values"]) < RTOL
+    assert relerr(b.evaluate_curl(g["u"]), g["curls"]) < RTOL
+    assert relerr(b.interpolate_edge_moments(_field, quadrature_order=4), g["moments"]) < 1e-14
+
+
 def test_n1_element_matrices_per_point_coefficients_through_the_c_abi():
     """coef_per_point = 1: per-point mass and curl coefficients through the explicit quadrature loop."""
     from skfemntv_gb300 import _device as dev

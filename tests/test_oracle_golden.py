@@ -121,6 +121,23 @@ def test_n1_element_matrices_evaluation_and_interpolation():
     np.testing.assert_allclose(O.n1_evaluate(nb, m, curl=True), 0.0, atol=2e-14)
 
 
+def _n1_field(x):
+    return np.stack([np.sin(3.0 * x[0]) + x[1], x[0] * x[2], np.cos(2.0 * x[2]) - x[0] * x[1]])
+
+
+def test_n1_basis_against_the_reference():
+    """The reference's element matrices, evaluation of a seeded edge field and its curl, and edge-moment
+    interpolation (fixture n1_basis, 3rd-order rule) against the oracle."""
+    g = load_golden("n1_basis")
+    nb = O.make_n1_basis(g["p"], g["t"], intorder=3)
+    assert np.array_equal(nb.X, g["X"]) and np.array_equal(nb.W, g["W"])
+    assert rel(O.n1_element_matrices(nb, include_curl=False), g["mass"]) < 1e-14
+    assert rel(O.n1_element_matrices(nb, include_mass=False), g["curl_curl"]) < 1e-14
+    assert rel(O.n1_evaluate(nb, g["u"]), g["values"]) < 1e-14
+    assert rel(O.n1_evaluate(nb, g["u"], curl=True), g["curls"]) < 1e-14
+    assert rel(O.n1_interpolate_edge_moments(g["p"], nb.edges, _n1_field, 4), g["moments"]) < 1e-15
+
+
 def test_n1_vector_load():
     g = load_golden("n1_load")
     b = O.make_n1_basis(g["p"], g["t"])
