@@ -120,6 +120,19 @@ def main():
     K2d = sk.asm(lap, b2d)
     out["p2_laplace_default"] = dict(p=m2.p, t=m2.t, X=b2d.X, W=b2d.W, **csr_parts(K2d))
 
+    # --- curved (isoparametric) P2: the same mesh with its edge nodes moved off the edges'
+    #     midpoints (own seed), 4-point rule: geometry, anisotropic diffusion and Laplace ---
+    rng_c = np.random.default_rng(np.random.SeedSequence(41))
+    pc = m2.p.copy()
+    edge_nodes = np.unique(m2.t[4:])
+    pc[:, edge_nodes] += 0.02 * rng_c.uniform(-1.0, 1.0, (3, len(edge_nodes)))
+    bc = sk.Basis(sk.MeshTet2(pc, m2.t), sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=(X4, W4))
+    Kc = sk.asm(aniso, bc, A=np.ascontiguousarray(Apub))
+    Kcl = sk.asm(lap, bc)
+    lap_parts = {f"lap_{k}": v for k, v in csr_parts(Kcl).items()}
+    out["p2_curved"] = dict(p=pc, t=m2.t, X=X4, W=W4, A=A, **csr_parts(Kc), **lap_parts, dx=bc.dx,
+                            grads=bc.tabulated_gradients, det=bc._geometry_determinants, xq=bc.global_coordinates)
+
     # --- Nedelec N1 Maxwell, relabelled 3^3 x 6 cube, 27-point Duffy rule ---
     rng = np.random.default_rng(np.random.SeedSequence(3))
     perm = rng.permutation(m0.p.shape[1])

@@ -135,31 +135,27 @@ def test_p2_anisotropic_per_point_tabulated_path():
 def test_curved_p2_geometry_takes_the_tabulated_path():
     """Edge nodes moved off their edges' midpoints make the quadratic map curved (isoparametric, all ten
     nodes: basis.py:2194-2294): the basis is not affine and every form runs the tabulated kernels.
-    Geometry bit for bit with the oracle; Laplace, anisotropic tensor, mass and load on scalar P2,
-    elasticity on vector P2, and P1 on the ten-node mesh (which keeps the quadratic geometry map,
-    basis.py:2274-2283) against the oracle."""
-    g = load_golden("p2_aniso")
-    t = g["t"]
-    p = g["p"].copy()
-    edge_nodes = np.unique(t[4:])
-    p[:, edge_nodes] += 0.02 * np.random.default_rng(9).uniform(-1.0, 1.0, (3, len(edge_nodes)))
+    Geometry bit for bit, Laplace and anisotropic diffusion against the reference's own outputs (fixture
+    p2_curved); mass and load on scalar P2, elasticity on vector P2 and P1 on the ten-node mesh (which
+    keeps the quadratic geometry map, basis.py:2274-2283) against the oracle."""
+    g = load_golden("p2_curved")
+    p, t = g["p"], g["t"]
     m = sk.MeshTet2(p, t)
     XW = (g["X"], g["W"])
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP2(), dim=1), quadrature=XW)
     assert not b.is_affine
+    assert np.array_equal(b.dx, g["dx"]) and np.array_equal(b.tabulated_gradients, g["grads"])
+    assert np.array_equal(b._geometry_determinants, g["det"]) and np.array_equal(b.global_coordinates, g["xq"])
     ob = O.make_basis(p, t, True, quadrature=XW)
-    assert np.array_equal(b.dx, ob.dx) and np.array_equal(b.tabulated_gradients, ob.grad)
-    assert np.array_equal(b.global_coordinates, ob.x)
     E, Q = b._coefficient_shape
 
     K = sk.asm(lap, b)
-    d, indptr, indices = O.bilinear_assemble(ob, gradient=1.0)
-    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
-    assert relerr(K.data, d) < RTOL
-    A = g["A"]  # per element (E, 3, 3)
-    Apub = np.broadcast_to(np.moveaxis(A, (1, 2), (0, 1))[..., None], (3, 3, E, Q))
-    want, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(Apub, (E, Q)))
-    assert relerr(sk.asm(aniso, b, A=Apub).data, want) < RTOL
+    assert np.array_equal(K.indptr, g["lap_indptr"]) and np.array_equal(K.indices, g["lap_indices"])
+    assert relerr(K.data, g["lap_data"]) < RTOL
+    Apub = np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q))
+    Ka = sk.asm(aniso, b, A=Apub)
+    same_pattern(Ka, g)
+    assert relerr(Ka.data, g["data"]) < RTOL
 
     @sk.BilinearForm
     def mass(u, v, w):

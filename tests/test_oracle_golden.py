@@ -66,6 +66,23 @@ def test_p2_aniso_cross_tensor():
     assert np.array_equal(dn, g["ns_data"])
 
 
+def test_p2_curved_isoparametric():
+    """Edge nodes off the edges' midpoints (fixture p2_curved): the ten-node geometry map bit for bit, the
+    anisotropic tensor and Laplace matrices in the reference's summation order."""
+    g = load_golden("p2_curved")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    assert np.array_equal(b.dx, g["dx"]) and np.array_equal(b.grad, g["grads"])
+    assert np.array_equal(b.det, g["det"]) and np.array_equal(b.x, g["xq"])
+    E, Q = b.dx.shape
+    T = O.anisotropic_tensor(np.broadcast_to(np.moveaxis(g["A"], (1, 2), (0, 1))[..., None], (3, 3, E, Q)), (E, Q))
+    data, indptr, indices = O.cross_gradient_tensor_assemble(b, T)
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert np.array_equal(data, g["data"])
+    ld, lip, lind = O.bilinear_assemble(b, gradient=1.0)
+    assert np.array_equal(lip, g["lap_indptr"]) and np.array_equal(lind, g["lap_indices"])
+    assert np.array_equal(ld, g["lap_data"])
+
+
 def test_p2_threaded_colored_close():
     g = load_golden("p2_aniso")
     b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
