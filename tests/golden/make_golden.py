@@ -247,6 +247,105 @@ def main():
     rhs = sk.asm(load, b2, f=fq)
     out["p2_load"] = dict(p=m2.p, t=m2.t, X=X4, W=W4, f=fq, rhs=np.asarray(rhs).copy())
 
+    # --- volume forms from the reference's compatible-forms cases on vector P1 (default rule):
+    #     constant, gradient and coordinate loads; mass, elasticity, coordinate and parameter
+    #     coefficients ---
+    from skfemntv.helpers import div, sym_grad  # type: ignore
+
+    mf = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 3),) * 3)
+    bf = sk.Basis(mf, sk.ElementVector(sk.ElementTetP1(), dim=3), intorder=2)
+
+    @sk.LinearForm
+    def force_load(v, w):
+        return dot(w.force, v)
+
+    @sk.LinearForm
+    def tensor_load(v, w):
+        return ddot(w.tensor, grad(v))
+
+    @sk.LinearForm
+    def coordinate_load(v, w):
+        x = w.x
+        return dot(np.stack((1.0 + x[0], x[1] ** 2, -0.5 * x[2]), axis=0), v)
+
+    @sk.BilinearForm
+    def vmass(u, v, w):
+        return dot(u, v)
+
+    @sk.BilinearForm
+    def elasticity(u, v, w):
+        return 2.0 * 0.7 * ddot(sym_grad(u), sym_grad(v)) + 2.3 * div(u) * div(v)
+
+    @sk.BilinearForm
+    def weighted_mass(u, v, w):
+        return (1.0 + w.x[0] ** 2) * dot(u, v)
+
+    @sk.BilinearForm
+    def scaled_mass(u, v, w):
+        return w.scale * (1.0 + w.x[0]) * dot(u, v)
+
+    @sk.BilinearForm
+    def reaction_diffusion(u, v, w):
+        return (w.reaction * (1.0 + w.x[0] ** 2) * dot(u, v)
+                + w.diffusivity * np.exp(-w.x[1]) * ddot(grad(u), grad(v)))
+
+    tensor = np.arange(9, dtype=float).reshape(3, 3, 1, 1) / 10
+    Kf = sk.asm(vmass, bf)
+    out["forms_vp1"] = dict(
+        p=mf.p, t=mf.t, X=bf.X, W=bf.W, force=np.array([1.2, -0.7, 2.1]), tensor=tensor,
+        r_force=np.asarray(sk.asm(force_load, bf, force=np.array([1.2, -0.7, 2.1])[:, None, None])).copy(),
+        r_tensor=np.asarray(sk.asm(tensor_load, bf, tensor=tensor)).copy(),
+        r_coordinate=np.asarray(sk.asm(coordinate_load, bf)).copy(), **csr_parts(Kf),
+        elasticity=np.asarray(sk.asm(elasticity, bf).data).copy(),
+        weighted_mass=np.asarray(sk.asm(weighted_mass, bf).data).copy(),
+        scaled_mass=np.asarray(sk.asm(scaled_mass, bf, scale=1.8).data).copy(),
+        reaction_diffusion=np.asarray(sk.asm(reaction_diffusion, bf, reaction=1.3, diffusivity=0.4).data).copy())
+
+    # --- first-axis coefficient components (scalar P1, default rule) beside a tensor term, and a
+    #     component of a linear-form coefficient ---
+    mk = sk.MeshTet.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4), np.linspace(0, 1, 3))
+    bk = sk.Basis(mk, sk.ElementVector(sk.ElementTetP1(), dim=1))
+    xk = np.moveaxis(bk.global_coordinates, -1, 0)
+    material = np.stack((0.7 + 0.2 * xk[0], 1.1 + 0.3 * xk[1]))
+    diffusion = np.array([[1.4, 0.2, 0.0], [-0.1, 0.8, 0.1], [0.0, 0.3, 1.2]])
+    loads = np.stack((np.full(xk[0].shape, 0.5), 1.0 + xk[0]))
+
+    @sk.BilinearForm
+    def components(u, v, w):
+        return (w.material[0] * dot(u, v) + w.material[1] * ddot(grad(u), grad(v))
+                + dot(mul(w.diffusion, grad(u)), grad(v)))
+
+    @sk.LinearForm
+    def component_load(v, w):
+        return dot(w.loads[1], v)
+
+    Kk = sk.asm(components, bk, material=material, diffusion=diffusion)
+    out["components_p1"] = dict(p=mk.p, t=mk.t, X=bk.X, W=bk.W, material=material, diffusion=diffusion,
+                                loads=loads, **csr_parts(Kk),
+                                r=np.asarray(sk.asm(component_load, bk, loads=loads)).copy())
+
+    # --- anisotropic forms on the P2 mesh, 4-point rule: a constant (3, 3) tensor, a nonsymmetric
+    #     constant tensor with an isotropic mass term, and a scalar coefficient with a unit axis ---
+    @sk.BilinearForm
+    def aniso_mass(u, v, w):
+        return dot(mul(w.A, grad(u)), grad(v)) + 0.25 * dot(u, v)
+
+    @sk.BilinearForm
+    def kmass(u, v, w):
+        return w.k * dot(u, v)
+
+    Ac = np.array([[2.0, 0.4, 0.1], [0.4, 0.8, -0.2], [0.1, -0.2, 1.3]])
+    An = np.array([[1.4, 0.2, 0.0], [-0.1, 0.7, 0.3], [0.05, 0.0, 1.1]])
+    E2, Q2 = b2.dx.shape
+    kq = 1.0 + np.arange(E2 * Q2, dtype=float).reshape(E2, Q2) / (E2 * Q2)
+    Kac = sk.asm(aniso, b2, A=Ac)
+    Kam = sk.asm(aniso_mass, b2, A=An)
+    out["aniso_forms_p2"] = dict(p=m2.p, t=m2.t, X=X4, W=W4, A_const=Ac, A_nonsym=An, k=kq, **csr_parts(Kac),
+                                 combined_indptr=np.asarray(Kam.tocsr().indptr, np.int64),
+                                 combined_indices=np.asarray(Kam.tocsr().indices, np.int64),
+                                 combined=np.asarray(Kam.tocsr().data).copy(),
+                                 kmass=np.asarray(sk.asm(kmass, b2, k=kq[..., None]).data).copy())
+
     os.makedirs(HERE, exist_ok=True)
     only = set(sys.argv[1:])  # fixture names to (re)write; all when empty
     for name, arrays in out.items():

@@ -1,11 +1,12 @@
 """Form front end on the GPU with the reference's compatible-forms cases (tests/test_compatible_forms.py,
-volume forms on a vector P1 basis with the default rule) against the oracle: constant and coordinate
-dependent loads, a gradient load through ``LinearForm.assemble``, mass and elasticity forms, coordinate
-and parameter dependent coefficients, several terms with subtraction, and the error for a foreign form."""
+volume forms on a vector P1 basis with the default rule) against the reference's own outputs (fixture
+forms_vp1): constant, gradient and coordinate-dependent loads, a gradient load through
+``LinearForm.assemble``, mass and elasticity forms, coordinate and parameter dependent coefficients,
+several terms with subtraction, and the error for a foreign form."""
 import numpy as np
 import pytest
 
-import oracle as O
+from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 sk = pytest.importorskip("skfemntv_gb300")
@@ -19,77 +20,64 @@ def relerr(a, b):
 
 
 @pytest.fixture(scope="module")
-def bases():
-    m = sk.MeshTet.init_tensor(*(np.linspace(0.0, 1.0, 3),) * 3)
-    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), intorder=2)
-    ob = O.make_basis(m.p, m.t, False, comp=3, quadrature=(b.X, b.W))
-    return b, ob
+def case():
+    g = load_golden("forms_vp1")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=3), intorder=2)
+    assert np.array_equal(b.X, g["X"]) and np.array_equal(b.W, g["W"])
+    return g, b
 
 
-def test_linear_forms(bases):
-    b, ob = bases
+def test_linear_forms(case):
+    g, b = case
 
     @sk.LinearForm
     def load(v, w):
         return dot(w.force, v)
 
-    force = np.array([1.2, -0.7, 2.1])
-    assert relerr(sk.asm(load, b, force=force[:, None, None]), O.linear_assemble(ob, value=force)) < RTOL
+    assert relerr(sk.asm(load, b, force=g["force"][:, None, None]), g["r_force"]) < RTOL
 
     @sk.LinearForm
     def gradient_load(v, w):
         return ddot(w.tensor, grad(v))
 
-    tensor = np.arange(9, dtype=float).reshape(3, 3) / 10
-    got = gradient_load.assemble(b, tensor=tensor[:, :, None, None])
-    assert relerr(got, O.linear_assemble(ob, gradient=tensor)) < RTOL
-
-    def field(x):
-        return np.stack((1.0 + x[0], x[1] ** 2, -0.5 * x[2]), axis=0)
+    assert relerr(gradient_load.assemble(b, tensor=g["tensor"]), g["r_tensor"]) < RTOL
 
     @sk.LinearForm
     def coordinate_load(v, w):
-        return dot(field(w.x), v)
+        x = w.x
+        return dot(np.stack((1.0 + x[0], x[1] ** 2, -0.5 * x[2]), axis=0), v)
 
-    x = np.moveaxis(b.global_coordinates, -1, 0)
-    want = O.linear_assemble(ob, value=np.moveaxis(field(x), 0, -1))
-    assert relerr(sk.asm(coordinate_load, b), want) < RTOL
+    assert relerr(sk.asm(coordinate_load, b), g["r_coordinate"]) < RTOL
 
 
-def test_bilinear_forms(bases):
-    b, ob = bases
-    x = np.moveaxis(b.global_coordinates, -1, 0)
+def test_bilinear_forms(case):
+    g, b = case
 
     @sk.BilinearForm
     def mass(u, v, w):
         return dot(u, v)
 
     K = sk.asm(mass, b)
-    d, indptr, indices = O.bilinear_assemble(ob, value=1.0)
-    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
-    assert relerr(K.data, d) < RTOL
-
-    lam, mu = 2.3, 0.7
+    assert np.array_equal(K.indptr, g["indptr"]) and np.array_equal(K.indices, g["indices"])
+    assert relerr(K.data, g["data"]) < RTOL
 
     @sk.BilinearForm
     def elasticity(u, v, w):
-        return 2.0 * mu * ddot(sym_grad(u), sym_grad(v)) + lam * div(u) * div(v)
+        return 2.0 * 0.7 * ddot(sym_grad(u), sym_grad(v)) + 2.3 * div(u) * div(v)
 
-    assert relerr(sk.asm(elasticity, b).data,
-                  O.bilinear_assemble(ob, symmetric_gradient=2.0 * mu, divergence=lam)[0]) < RTOL
+    assert relerr(sk.asm(elasticity, b).data, g["elasticity"]) < RTOL
 
     @sk.BilinearForm
     def weighted_mass(u, v, w):
         return (1.0 + w.x[0] ** 2) * dot(u, v)
 
-    assert relerr(sk.asm(weighted_mass, b).data, O.bilinear_assemble(ob, value=1.0 + x[0] ** 2)[0]) < RTOL
+    assert relerr(sk.asm(weighted_mass, b).data, g["weighted_mass"]) < RTOL
 
     @sk.BilinearForm
     def scaled_mass(u, v, w):
         return w.scale * (1.0 + w.x[0]) * dot(u, v)
 
-    assert relerr(sk.asm(scaled_mass, b, scale=1.8).data,
-                  O.bilinear_assemble(ob, value=1.8 * (1.0 + x[0]))[0]) < RTOL
+    assert relerr(sk.asm(scaled_mass, b, scale=1.8).data, g["scaled_mass"]) < RTOL
 
     @sk.BilinearForm
     def reaction_diffusion(u, v, w):
@@ -97,8 +85,7 @@ def test_bilinear_forms(bases):
                 + w.diffusivity * np.exp(-w.x[1]) * ddot(grad(u), grad(v)))
 
     got = sk.asm(reaction_diffusion, b, reaction=1.3, diffusivity=0.4).data
-    want = O.bilinear_assemble(ob, value=1.3 * (1.0 + x[0] ** 2), gradient=0.4 * np.exp(-x[1]))[0]
-    assert relerr(got, want) < RTOL
+    assert relerr(got, g["reaction_diffusion"]) < RTOL
 
     @sk.BilinearForm
     def with_subtraction(u, v, w):

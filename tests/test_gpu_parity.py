@@ -191,44 +191,37 @@ def test_curved_p2_geometry_takes_the_tabulated_path():
 
 
 def test_p2_constant_tensor_combined_with_isotropic_term_and_rejections():
-    """The reference's anisotropic-form cases (tests/test_anisotropic_forms.py:41-125) on P2 tets: a
-    constant (3, 3) tensor gives a symmetric matrix equal to the oracle's; a nonsymmetric tensor summed
-    with an isotropic mass term equals the sum of the oracle's two assemblies; a tensor of the wrong
-    shape raises ValueError and a vector field UnsupportedNativeForm, with the reference's messages."""
-    g = load_golden("p2_aniso")
+    """The reference's anisotropic-form cases (tests/test_anisotropic_forms.py:41-125) on P2 tets against
+    its own outputs (fixture aniso_forms_p2): a constant (3, 3) tensor gives a symmetric matrix; a
+    nonsymmetric tensor summed with an isotropic mass term; a scalar coefficient with a unit axis reads as
+    (E, Q) (_coefficients.py:84); a tensor of the wrong shape raises ValueError and a vector field
+    UnsupportedNativeForm, with the reference's messages."""
+    g = load_golden("aniso_forms_p2")
     b = p2_basis(g, (g["X"], g["W"]))
     E, Q = b._coefficient_shape
-    ob = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
 
-    A = np.array([[2.0, 0.4, 0.1], [0.4, 0.8, -0.2], [0.1, -0.2, 1.3]])
-    K = sk.asm(aniso, b, A=A)
-    data, indptr, indices = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(A, (E, Q)))
-    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
-    assert relerr(K.data, data) < RTOL
+    K = sk.asm(aniso, b, A=g["A_const"])
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
     assert abs(K - K.T).max() <= 2e-14 * np.max(np.abs(K.data))
 
     @sk.BilinearForm
     def aniso_mass(u, v, w):
         return dot(mul(w.A, grad(u)), grad(v)) + 0.25 * dot(u, v)
 
-    An = np.array([[1.4, 0.2, 0.0], [-0.1, 0.7, 0.3], [0.05, 0.0, 1.1]])
-    Kc = sk.asm(aniso_mass, b, A=An)
-    td, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(An, (E, Q)))
-    md, _, _ = O.bilinear_assemble(ob, value=0.25)
+    Kc = sk.asm(aniso_mass, b, A=g["A_nonsym"])
     Kc.sort_indices()
-    assert np.array_equal(Kc.indptr, indptr) and np.array_equal(Kc.indices, indices)
-    assert relerr(Kc.data, td + md) < RTOL
+    assert np.array_equal(Kc.indptr, g["combined_indptr"]) and np.array_equal(Kc.indices, g["combined_indices"])
+    assert relerr(Kc.data, g["combined"]) < RTOL
     assert abs(Kc - Kc.T).max() > 1e-3 * np.max(np.abs(Kc.data))
 
-    # a scalar coefficient with a unit axis reads as (E, Q), as in the reference (_coefficients.py:84)
     @sk.BilinearForm
     def kmass(u, v, w):
         return w.k * dot(u, v)
 
-    k = 1.0 + np.arange(E * Q, dtype=float).reshape(E, Q) / (E * Q)
-    kd, _, _ = O.bilinear_assemble(ob, value=k)
+    k = g["k"]
     for raw in (k, k[..., None], k[None]):
-        assert relerr(sk.asm(kmass, b, k=raw).data, kd) < RTOL
+        assert relerr(sk.asm(kmass, b, k=raw).data, g["kmass"]) < RTOL
 
     with pytest.raises(ValueError, match="recommended scikit-fem shape"):
         sk.asm(aniso, b, A=np.eye(2))
@@ -393,40 +386,30 @@ def test_n1_pointwise_coefficients_reused_matrix_and_contract():
 
 def test_named_coefficient_components_use_the_first_axis():
     """The reference's coefficient-component cases (tests/test_coefficient_components.py:25-138, on
-    scalar P1 tets; composite elements are outside this path): components of a keyword array are taken
-    along its first axis in bilinear and linear forms, beside an anisotropic tensor term; a missing
-    parameter, an out-of-range component and a non-integer index raise the reference's messages."""
-    m = sk.MeshTet.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4), np.linspace(0, 1, 3))
-    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1))
+    scalar P1 tets; composite elements are outside this path) against its own outputs (fixture
+    components_p1): components of a keyword array are taken along its first axis in bilinear and linear
+    forms, beside an anisotropic tensor term; a missing parameter, an out-of-range component and a
+    non-integer index raise the reference's messages."""
+    g = load_golden("components_p1")
+    b = sk.Basis(sk.MeshTet(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP1(), dim=1))
+    assert np.array_equal(b.X, g["X"]) and np.array_equal(b.W, g["W"])
     E, Q = b.dx.shape
-    x = np.moveaxis(b.global_coordinates, -1, 0)
-    material = np.empty((2, E, Q))
-    material[0] = 0.7 + 0.2 * x[0]
-    material[1] = 1.1 + 0.3 * x[1]
-    diffusion = np.array([[1.4, 0.2, 0.0], [-0.1, 0.8, 0.1], [0.0, 0.3, 1.2]])
 
     @sk.BilinearForm
     def form(u, v, w):
         return (w.material[0] * dot(u, v) + w.material[1] * ddot(grad(u), grad(v))
                 + dot(mul(w.diffusion, grad(u)), grad(v)))
 
-    K = sk.asm(form, b, material=material, diffusion=diffusion)
-    ob = O.make_basis(m.p, m.t, False, quadrature=(b.X, b.W))
-    pd, indptr, indices = O.bilinear_assemble(ob, value=material[0], gradient=material[1])
-    td, _, _ = O.cross_gradient_tensor_assemble(ob, O.anisotropic_tensor(diffusion, (E, Q)))
+    K = sk.asm(form, b, material=g["material"], diffusion=g["diffusion"])
     K.sort_indices()
-    assert np.array_equal(K.indptr, indptr) and np.array_equal(K.indices, indices)
-    assert relerr(K.data, pd + td) < RTOL
-
-    loads = np.empty((2, E, Q))
-    loads[0] = 0.5
-    loads[1] = 1.0 + x[0]
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
 
     @sk.LinearForm
     def load(v, w):
         return dot(w.loads[1], v)
 
-    assert relerr(sk.asm(load, b, loads=loads), O.linear_assemble(ob, value=loads[1][..., None])) < RTOL
+    assert relerr(sk.asm(load, b, loads=g["loads"]), g["r"]) < RTOL
 
     @sk.BilinearForm
     def indexed(u, v, w):

@@ -210,3 +210,49 @@ def test_geometry_validation_messages():
     ps = np.array([[0., 1., 0., 0.], [0., 0., 1., 0.], [0., 0., 0., 1.]]) * 1e-50
     b = O.make_basis(ps, t, False)
     assert b.det[0, 0] > 0
+
+
+def test_compatible_volume_forms():
+    """Fixture forms_vp1 (the reference's compatible-forms cases on vector P1): loads and bilinear forms
+    with constant, coordinate and parameter coefficients."""
+    g = load_golden("forms_vp1")
+    b = O.make_basis(g["p"], g["t"], False, comp=3, quadrature=(g["X"], g["W"]))
+    x = np.moveaxis(b.x, -1, 0)
+    assert rel(O.linear_assemble(b, value=g["force"]), g["r_force"]) < 1e-14
+    assert rel(O.linear_assemble(b, gradient=g["tensor"][:, :, 0, 0]), g["r_tensor"]) < 1e-14
+    field = np.stack((1.0 + x[0], x[1] ** 2, -0.5 * x[2]), axis=0)
+    assert rel(O.linear_assemble(b, value=np.moveaxis(field, 0, -1)), g["r_coordinate"]) < 1e-14
+    data, indptr, indices = O.bilinear_assemble(b, value=1.0)
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert rel(data, g["data"]) < 1e-14
+    assert rel(O.bilinear_assemble(b, symmetric_gradient=2.0 * 0.7, divergence=2.3)[0], g["elasticity"]) < 1e-14
+    assert rel(O.bilinear_assemble(b, value=1.0 + x[0] ** 2)[0], g["weighted_mass"]) < 1e-14
+    assert rel(O.bilinear_assemble(b, value=1.8 * (1.0 + x[0]))[0], g["scaled_mass"]) < 1e-14
+    rd = O.bilinear_assemble(b, value=1.3 * (1.0 + x[0] ** 2), gradient=0.4 * np.exp(-x[1]))[0]
+    assert rel(rd, g["reaction_diffusion"]) < 1e-14
+
+
+def test_coefficient_components_and_anisotropic_forms():
+    """Fixtures components_p1 (first-axis components beside a tensor term, a linear-form component) and
+    aniso_forms_p2 (a constant tensor, a nonsymmetric one plus an isotropic mass term, a scalar
+    coefficient with a unit axis)."""
+    g = load_golden("components_p1")
+    b = O.make_basis(g["p"], g["t"], False, quadrature=(g["X"], g["W"]))
+    E, Q = b.dx.shape
+    pd, indptr, indices = O.bilinear_assemble(b, value=g["material"][0], gradient=g["material"][1])
+    td, _, _ = O.cross_gradient_tensor_assemble(b, O.anisotropic_tensor(g["diffusion"], (E, Q)))
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert rel(pd + td, g["data"]) < 1e-14
+    assert rel(O.linear_assemble(b, value=g["loads"][1][..., None]), g["r"]) < 1e-14
+
+    g = load_golden("aniso_forms_p2")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X"], g["W"]))
+    E, Q = b.dx.shape
+    d, indptr, indices = O.cross_gradient_tensor_assemble(b, O.anisotropic_tensor(g["A_const"], (E, Q)))
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert rel(d, g["data"]) < 1e-14
+    tn, _, _ = O.cross_gradient_tensor_assemble(b, O.anisotropic_tensor(g["A_nonsym"], (E, Q)))
+    md, _, _ = O.bilinear_assemble(b, value=0.25)
+    assert np.array_equal(indptr, g["combined_indptr"]) and np.array_equal(indices, g["combined_indices"])
+    assert rel(tn + md, g["combined"]) < 1e-14
+    assert rel(O.bilinear_assemble(b, value=g["k"])[0], g["kmass"]) < 1e-14
