@@ -2,6 +2,7 @@
 symbol declared in include/skfem_gb300.h, and the host logic of the drop-in
 (form tracing, quadrature tables, mesh generation, DOF numbering, runtime
 controls, memory preflight) matches the reference's behaviour."""
+import ctypes
 import os
 import re
 
@@ -49,6 +50,40 @@ def test_ctypes_signatures_match_header_parameter_counts():
     assert set(counts) == set(header_symbols())
     for name, n in counts.items():
         assert len(_native.SIGNATURES[name]) == n, (name, len(_native.SIGNATURES[name]), n)
+
+
+def test_n1_basis_entry_points_check_arguments_before_device_work():
+    """The N1 basis entry points reject empty rules, bad layouts and missing arrays with SKG_EINVAL and a
+    message before any device call, and return at once for an empty mesh."""
+    from skfemntv_gb300._native import call
+
+    X = np.full((3, 1), 0.25)
+    W = np.array([1.0 / 6.0])
+    t = np.array([0.5])
+    hX, hW, ht = (a.ctypes.data_as(ctypes.c_void_p) for a in (X, W, t))
+    cases = [
+        ("skg_n1_element_matrices", (None, 0, None, None, 1, 0, hX, hW, None, None, 0, 1, 1, None, None),
+         "quadrature rule is empty"),
+        ("skg_n1_element_matrices", (None, 0, None, None, 1, 1, hX, hW, None, None, 2, 1, 1, None, None),
+         "coefficient layout"),
+        ("skg_n1_element_matrices", (None, 0, None, None, 1, 1, hX, hW, None, None, 0, 1, 1, None, None),
+         "mesh or output arrays are NULL"),
+        ("skg_n1_evaluate", (None, 0, None, None, None, 1, 1, 0, hX, None, 0, None, None), "quadrature rule is empty"),
+        ("skg_n1_evaluate", (None, 0, None, None, None, 1, 1, 1, hX, None, 0, None, None),
+         "mesh, coefficient or output arrays are NULL"),
+        ("skg_n1_edge_points", (None, 0, None, 1, 0, ht, None, None), "edge rule is empty"),
+        ("skg_n1_edge_points", (None, 0, None, 1, 1, ht, None, None), "mesh, edge or output arrays are NULL"),
+        ("skg_n1_edge_moments", (None, 0, None, 1, 1, None, None, None, None), "edge rule is empty"),
+        ("skg_n1_edge_moments", (None, 0, None, 1, 1, hW, None, None, None),
+         "mesh, edge, field or output arrays are NULL"),
+    ]
+    for name, args, message in cases:
+        with pytest.raises(ValueError, match=message):
+            call(name, *args)
+    call("skg_n1_element_matrices", None, 0, None, None, 0, 1, hX, hW, None, None, 0, 1, 1, None, None)
+    call("skg_n1_evaluate", None, 0, None, None, None, 0, 0, 1, hX, None, 0, None, None)
+    call("skg_n1_edge_points", None, 0, None, 0, 1, ht, None, None)
+    call("skg_n1_edge_moments", None, 0, None, 0, 1, hW, None, None, None)
 
 
 def test_nvcc_targets_sm103a_only():
