@@ -192,10 +192,23 @@ def test_quadrature_tables_match_reference_rules():
 
 
 def test_quadrature_validation():
+    """The reference's invalid custom rules (tests/test_quadrature.py:184-199, for tetrahedra): points of the
+    wrong dimension, weights of the wrong length, and non-finite points or weights raise ValueError; a
+    valid rule comes back contiguous and unchanged."""
     with pytest.raises(ValueError, match="shape"):
         quadrature.validate((np.zeros((2, 3)), np.zeros(3)))
+    with pytest.raises(ValueError, match="shape"):
+        quadrature.validate((np.zeros((1, 2)), np.ones(2)))
+    with pytest.raises(ValueError, match="weights must have shape"):
+        quadrature.validate((np.zeros((3, 2)), np.ones(3)))
     with pytest.raises(ValueError, match="finite"):
         quadrature.validate((np.full((3, 1), np.nan), np.ones(1)))
+    with pytest.raises(ValueError, match="finite"):
+        quadrature.validate((np.zeros((3, 1)), np.array([np.inf])))
+    X = np.asfortranarray(np.array([[0.25, 0.1], [0.25, 0.2], [0.25, 0.3]]))
+    W = np.array([0.1, 0.05])
+    Xv, Wv = quadrature.validate((X, W))
+    assert Xv.flags.c_contiguous and np.array_equal(Xv, X) and np.array_equal(Wv, W)
 
 
 def test_mesh_init_tensor_matches_reference():
