@@ -22,6 +22,12 @@ from ._native import call
 from .element import ElementTetP1, ElementTetP2, ElementVector
 
 
+# The geometry kernel keeps the rule's reference tables (values and gradients
+# of the element and geometry nodes, weights) in one block's shared memory,
+# at most 227 KB on sm_103a: up to 343 points for P2 (order 11 and below).
+_GEOMETRY_TABLE_BYTES = 227 * 1024
+
+
 @dataclass(frozen=True)
 class GeometryDiagnostics:
     element_count: int
@@ -74,7 +80,7 @@ class Basis:
         if quadrature is not None:
             self.X, self.W = quad.validate(quadrature, 3)
         elif intorder > 4:
-            raise NotImplementedError("simplex rules above order 4 are not provided by the GPU backend")
+            self.X, self.W = quad.simplex_rule(intorder)
         elif self._quadratic or intorder >= 4:
             self.X, self.W = quad.tet_rule_p2()
         else:
@@ -83,6 +89,13 @@ class Basis:
         G = mesh.t.shape[0]
         if G < self._nodes:
             raise ValueError("mesh geometry nodes are incompatible with the element")
+        table_bytes = 8 * len(self.W) * (4 * self._nodes + 4 * G + 1)
+        if table_bytes > _GEOMETRY_TABLE_BYTES:
+            from .errors import UnsupportedNativeForm
+
+            raise UnsupportedNativeForm(
+                f"a rule of {len(self.W)} points needs {table_bytes} bytes of reference tables; the geometry "
+                f"kernel holds at most {_GEOMETRY_TABLE_BYTES} in shared memory")
         conn = mesh.t[: self._nodes]
         E = mesh.nelements
         C = self._comp

@@ -2,8 +2,9 @@
 
 The default rules are the reference's (python/skfemntv/basis.py:1716-1734:
 the symmetric 4-point rule for P1 and the 11-point Keast rule, with its
-negative centroid weight, for P2), and the Duffy product rule used by the
-H(curl) basis (python/skfemntv/hcurl_basis.py:37-56).  The point and weight
+negative centroid weight, for P2), the Duffy product rule used by the
+H(curl) basis (python/skfemntv/hcurl_basis.py:37-56) and the collapsed
+Gauss-Legendre rule the H1 basis takes above order 4 (basis.py:1580-1598).  The point and weight
 values must be the same numbers for results to agree, so they are restated
 here as data.
 """
@@ -47,6 +48,28 @@ def duffy_rule(order):
                 X.append((x, y, z))
                 W.append((1.0 - x) ** 2 * (1.0 - g[j]) * gw[i] * gw[j] * gw[k])
     return np.ascontiguousarray(np.asarray(X).T), np.asarray(W)
+
+
+def simplex_rule(order):
+    """The H1 basis's rule above order 4 on the unit tetrahedron
+    (basis.py:1580-1598): Gauss-Legendre points t on [0, 1],
+    (order + 4) // 2 per axis, collapsed as x = t0, y = (1 - t0) t1,
+    z = ((1 - t0)(1 - t1)) t2 with weight (1 - t0)^2 (1 - t1) times
+    (w0 w1) w2, the last axis fastest.  The products are grouped as there so
+    that the rule is the same numbers (its weights group the 1-D weights
+    differently from ``duffy_rule``)."""
+    count = max(1, (int(order) + 4) // 2)
+    g, gw = np.polynomial.legendre.leggauss(count)
+    g = (g + 1.0) / 2.0
+    gw = gw / 2.0
+    i0, i1, i2 = (a.ravel() for a in np.indices((count, count, count)))
+    rest = 1.0 - g
+    # the square through the C library's pow, as a scalar power is taken there
+    # (an array's ** 2 would multiply, which can round differently)
+    rest_sq = np.array([float(r) ** 2 for r in rest])
+    X = np.stack((g[i0], rest[i0] * g[i1], (rest[i0] * rest[i1]) * g[i2]))
+    W = (rest_sq[i0] * rest[i1]) * ((gw[i0] * gw[i1]) * gw[i2])
+    return np.ascontiguousarray(X), W
 
 
 def validate(quadrature, dimension=3):

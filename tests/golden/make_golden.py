@@ -120,6 +120,14 @@ def main():
     K2d = sk.asm(lap, b2d)
     out["p2_laplace_default"] = dict(p=m2.p, t=m2.t, X=b2d.X, W=b2d.W, **csr_parts(K2d))
 
+    # --- the basis rules above order 4 (collapsed Gauss-Legendre), and P2 Laplace with order 6 ---
+    rules = {}
+    for order in (5, 6, 7, 8):
+        bo = sk.Basis(sk.MeshTet(), sk.ElementVector(sk.ElementTetP1(), dim=1), intorder=order)
+        rules[f"X{order}"], rules[f"W{order}"] = bo.X, bo.W
+    b6 = sk.Basis(m2, sk.ElementVector(sk.ElementTetP2(), dim=1), intorder=6)
+    out["simplex_rules"] = dict(p=m2.p, t=m2.t, **rules, **csr_parts(sk.asm(lap, b6)))
+
     # --- curved (isoparametric) P2: the same mesh with its edge nodes moved off the edges'
     #     midpoints (own seed), 4-point rule: geometry, anisotropic diffusion and Laplace ---
     rng_c = np.random.default_rng(np.random.SeedSequence(41))

@@ -132,6 +132,20 @@ def test_p2_anisotropic_per_point_tabulated_path():
     assert relerr(K.data, data) < RTOL
 
 
+def test_p2_laplace_with_an_order_6_rule():
+    """intorder above 4 selects the collapsed Gauss-Legendre rule (basis.py:1580-1598): 125 points for order
+    6; P2 Laplace with it against the reference's own output (fixture simplex_rules).  The rule is compared
+    to 1e-15: numpy's Gauss-Legendre weights on an Arm host differ from the fixture's x86 values in the
+    last bits."""
+    g = load_golden("simplex_rules")
+    b = sk.Basis(sk.MeshTet2(g["p"], g["t"]), sk.ElementVector(sk.ElementTetP2(), dim=1), intorder=6)
+    assert b.X.shape == (3, 125)
+    assert relerr(b.X, g["X6"]) < 1e-15 and relerr(b.W, g["W6"]) < 1e-15
+    K = sk.asm(lap, b)
+    same_pattern(K, g)
+    assert relerr(K.data, g["data"]) < RTOL
+
+
 def test_curved_p2_geometry_takes_the_tabulated_path():
     """Edge nodes moved off their edges' midpoints make the quadratic map curved (isoparametric, all ten
     nodes: basis.py:2194-2294): the basis is not affine and every form runs the tabulated kernels.

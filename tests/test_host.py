@@ -211,6 +211,34 @@ def test_quadrature_validation():
     assert Xv.flags.c_contiguous and np.array_equal(Xv, X) and np.array_equal(Wv, W)
 
 
+def test_high_order_rules_match_the_reference_and_integrate_monomials():
+    """Above order 4 the basis takes the collapsed Gauss-Legendre rule (basis.py:1580-1598): the same numbers
+    as the reference's (fixture simplex_rules), and exact for every monomial x^a y^b z^c with a + b + c up
+    to the order (tests/test_quadrature.py:44-65), whose integral over the unit tetrahedron is
+    a! b! c! / (a + b + c + 3)!."""
+    from math import factorial
+
+    g = load_golden("simplex_rules")
+    for order in (5, 6, 7, 8):
+        X, W = quadrature.simplex_rule(order)
+        assert np.array_equal(X, g[f"X{order}"]) and np.array_equal(W, g[f"W{order}"]), order
+        for a in range(order + 1):
+            for b in range(order + 1 - a):
+                for c in range(order + 1 - a - b):
+                    exact = factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 3)
+                    got = float(np.sum(W * X[0] ** a * X[1] ** b * X[2] ** c))
+                    assert abs(got - exact) <= 1e-14 * max(exact, 1e-3), (order, a, b, c)
+
+
+def test_rules_too_large_for_the_geometry_kernel_are_rejected_before_device_work():
+    """A P2 rule of order 12 (512 points) needs more reference tables than one block's shared memory holds:
+    UnsupportedNativeForm before anything reaches the device; order 11 (343 points) fits."""
+    with pytest.raises(sk.UnsupportedNativeForm, match="512 points"):
+        sk.Basis(sk.MeshTet2(), sk.ElementVector(sk.ElementTetP2(), dim=1), intorder=12)
+    X, W = quadrature.simplex_rule(11)
+    assert 8 * len(W) * (4 * 10 + 4 * 10 + 1) <= 227 * 1024
+
+
 def test_mesh_init_tensor_matches_reference():
     g = load_golden("p1_laplace")
     m = sk.MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3)

@@ -256,3 +256,12 @@ def test_coefficient_components_and_anisotropic_forms():
     assert np.array_equal(indptr, g["combined_indptr"]) and np.array_equal(indices, g["combined_indices"])
     assert rel(tn + md, g["combined"]) < 1e-14
     assert rel(O.bilinear_assemble(b, value=g["k"])[0], g["kmass"]) < 1e-14
+
+
+def test_p2_laplace_with_an_order_6_rule():
+    """Fixture simplex_rules: P2 Laplace with the reference's order-6 collapsed rule."""
+    g = load_golden("simplex_rules")
+    b = O.make_basis(g["p"], g["t"], True, quadrature=(g["X6"], g["W6"]))
+    data, indptr, indices = O.bilinear_assemble(b, gradient=1.0)
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    assert rel(data, g["data"]) < 1e-14
