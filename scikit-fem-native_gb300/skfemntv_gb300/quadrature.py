@@ -2,11 +2,11 @@
 
 The default rules are the reference's (python/skfemntv/basis.py:1716-1734:
 the symmetric 4-point rule for P1 and the 11-point Keast rule, with its
-negative centroid weight, for P2), the Duffy product rule used by the
-H(curl) basis (python/skfemntv/hcurl_basis.py:37-56) and the collapsed
-Gauss-Legendre rule the H1 basis takes above order 4 (basis.py:1580-1598).  The point and weight
-values must be the same numbers for results to agree, so they are restated
-here as data.
+negative centroid weight, for P2), restated as data; the Duffy product rule
+of the H(curl) basis (python/skfemntv/hcurl_basis.py:37-56) and the
+collapsed Gauss-Legendre rule the H1 basis takes above order 4
+(basis.py:1580-1598) are computed with the reference's arithmetic.  The
+points and weights must be the same numbers for results to agree.
 """
 from __future__ import annotations
 
