@@ -10,7 +10,8 @@ CUDA kernels for sm_103a reached through the C ABI in
 ``include/skfem_gb300.h``.
 """
 from .adjoint import P1Energy
-from .assembly import AssemblyGraph, NativeBilinearForm, NativeCrossBilinearForm, NativeLinearForm
+from .assembly import (AssemblyGraph, LinearFormDiagnostics, NativeBilinearForm, NativeCrossBilinearForm,
+                       NativeLinearForm)
 from .basis import Basis, GeometryDiagnostics
 from .element import ElementTetP1, ElementTetP2, ElementVector
 from .errors import UnsupportedNativeForm
@@ -28,7 +29,7 @@ from .runtime import (BACKEND, CAPABILITIES, available_num_threads, get_num_thre
 __version__ = "0.1.0"
 
 __all__ = [
-    "AssemblyGraph", "NativeBilinearForm", "NativeCrossBilinearForm", "NativeLinearForm",
+    "AssemblyGraph", "LinearFormDiagnostics", "NativeBilinearForm", "NativeCrossBilinearForm", "NativeLinearForm",
     "AffineTetN1Basis", "AssemblyMemoryBudgetError", "AssemblyMemoryEstimate", "BACKEND", "Basis",
     "BilinearForm", "CAPABILITIES", "ElementTetP1", "ElementTetP2", "ElementVector", "GeometryDiagnostics",
     "HcurlTetGeometryDiagnostics", "LinearForm", "OrientedEdgeDofMap", "OrientedEdgeTopology",

@@ -16,6 +16,8 @@ geometry tabulation, element matrices, the same fixed-order gather).
 from __future__ import annotations
 
 import ctypes
+import time
+from dataclasses import dataclass
 
 import numpy as np
 from scipy.sparse import csr_matrix
@@ -612,38 +614,69 @@ class NativeCrossBilinearForm:
         return self.target.copy_matrix()
 
 
+@dataclass(frozen=True)
+class LinearFormDiagnostics:
+    """What ``NativeLinearForm.assemble`` reports beside the vector
+    (linear_form.py:10-14): elements, points per element, and the wall time of
+    the call (coefficient upload, kernels, copy of the result)."""
+
+    entity_count: int
+    quadrature_point_count: int
+    assembly_seconds: float
+
+
 class NativeLinearForm:
-    """f.v + G:grad v on one basis (linear_form.py:17-107)."""
+    """f.v + G:grad v on one basis (linear_form.py:17-107).  ``assemble``
+    returns (vector, LinearFormDiagnostics) as the reference's does."""
 
     def __init__(self, basis):
         self.basis = basis
         E, L = basis.mesh.nelements, basis._nodes * basis._comp
+        Q = len(basis.W)
+        self._shape = (E, Q, basis._comp)
+        self._gradient_shape = (E, Q, basis._comp, 3)
         self.pattern = Pattern(basis._dev_dofs(), None, E, L, 0, basis.N, 0)
         self.d_out = dev.empty(max(1, basis.N), np.float64)
 
-    def assemble(self, *, value=None, gradient=None):
+    @property
+    def ndofs(self):
+        return self.basis.N
+
+    @staticmethod
+    def _coefficient(name, coefficient, shape):
+        """None, a constant of shape ``shape[2:]``, or an array broadcast to
+        ``shape``; float64 only (linear_form.py:91-107)."""
+        if coefficient is None:
+            return None
+        coefficient = np.asarray(coefficient)
+        if coefficient.dtype != np.float64:
+            raise TypeError(f"{name} coefficient must have dtype float64")
+        if coefficient.shape == shape[2:]:
+            return np.ascontiguousarray(coefficient)
+        try:
+            return np.broadcast_to(coefficient, shape)
+        except ValueError as error:
+            raise ValueError(f"{name} coefficient must broadcast to {shape}") from error
+
+    def assemble(self, *, value=None, gradient=None, num_threads=0):
+        start = time.perf_counter()
         b = self.basis
-        E, Q = b._coefficient_shape
-        C = b._comp
+        E, Q, C = self._shape
+        value = self._coefficient("value", value, self._shape)
+        gradient = self._coefficient("gradient", gradient, self._gradient_shape)
         if value is None and gradient is None:
             raise ValueError("at least one coefficient is required")
         dv = dg = None
         if value is not None:
-            v = np.asarray(value, dtype=np.float64)
-            v = np.broadcast_to(v, (E, Q, C)) if v.shape != (C,) else np.broadcast_to(v, (E, Q, C))
-            dv = dev.to_device(np.ascontiguousarray(v), np.float64)
+            dv = dev.to_device(np.ascontiguousarray(np.broadcast_to(value, self._shape)), np.float64)
         if gradient is not None:
-            g = np.asarray(gradient, dtype=np.float64)
-            try:
-                g = np.broadcast_to(g, (E, Q, C, 3))
-            except ValueError as error:
-                raise ValueError(f"gradient coefficient must broadcast to {(E, Q, C, 3)}") from error
-            dg = dev.to_device(np.ascontiguousarray(g), np.float64)
+            dg = dev.to_device(np.ascontiguousarray(np.broadcast_to(gradient, self._gradient_shape)), np.float64)
         tab = b._device_tabulation()
         call("skg_linear_assemble_tabulated", self.pattern.h, dev.ptr(b._dev_dofs()), E, b._nodes, C, Q,
              dev.ptr(tab["shape"]), dev.ptr(tab["grad"]), dev.ptr(tab["dx"]), dev.ptr(dv), dev.ptr(dg),
              dev.ptr(self.d_out), dev.stream_ptr())
-        return self.d_out[: b.N].cpu().numpy()
+        result = self.d_out[: b.N].cpu().numpy()
+        return result, LinearFormDiagnostics(E, Q, time.perf_counter() - start)
 
 
 def assemble_bilinear(form, basis, terms, *, precision="fp64", memory_limit_bytes=None,
@@ -703,4 +736,5 @@ def assemble_linear(form, basis, terms):
             gradient = c if gradient is None else gradient + c
         else:
             raise UnsupportedNativeForm
-    return native.assemble(value=value, gradient=gradient)
+    result, _ = native.assemble(value=value, gradient=gradient)
+    return result

@@ -35,6 +35,10 @@ def test_linear_forms(case):
         return dot(w.force, v)
 
     assert relerr(sk.asm(load, b, force=g["force"][:, None, None]), g["r_force"]) < RTOL
+    # the assembler itself returns (vector, diagnostics) as the reference's (linear_form.py:62-89)
+    r, diag = sk.NativeLinearForm(b).assemble(value=g["force"])
+    assert relerr(r, g["r_force"]) < RTOL
+    assert (diag.entity_count, diag.quadrature_point_count) == b.dx.shape and diag.assembly_seconds > 0
 
     @sk.LinearForm
     def gradient_load(v, w):

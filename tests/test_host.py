@@ -440,6 +440,22 @@ def test_component_access_errors_raise_before_assembly():
         sk.asm(noninteger, None)
 
 
+def test_native_linear_form_coefficient_rules():
+    """NativeLinearForm._coefficient (linear_form.py:91-107, tests/test_compatible_forms.py:14-24): a
+    constant keeps its shape, anything else is broadcast to (E, Q, C[, 3]); only float64 is accepted
+    (TypeError), and a shape that does not broadcast raises ValueError naming the target shape."""
+    f = sk.NativeLinearForm._coefficient
+    assert f("value", np.array([2.0]), (100, 3, 1)).shape == (1,)
+    assert f("gradient", np.array([[3.0, 4.0, 5.0]]), (100, 3, 1, 3)).shape == (1, 3)
+    assert f("value", np.ones((100, 3, 1)), (100, 3, 1)).shape == (100, 3, 1)
+    assert f("value", np.ones((100, 1, 1)), (100, 3, 1)).shape == (100, 3, 1)
+    assert f("value", None, (100, 3, 1)) is None
+    with pytest.raises(TypeError, match="dtype float64"):
+        f("value", np.array([2], dtype=np.int64), (100, 3, 1))
+    with pytest.raises(ValueError, match=r"gradient coefficient must broadcast to \(100, 3, 1, 3\)"):
+        f("gradient", np.ones((7, 3)), (100, 3, 1, 3))
+
+
 def test_coefficient_evaluation_factor_and_squeeze():
     """A term's coefficient times its factor (_coefficients.py:71-86): a factor of 1 leaves a broadcast
     view uncopied; squeezing, as bilinear scalar terms do, reads (E, Q, 1) and (1, E, Q) as (E, Q)."""
