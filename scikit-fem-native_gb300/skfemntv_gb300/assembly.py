@@ -588,6 +588,38 @@ class NativeCrossBilinearForm:
         full = scalar[(...,) + (None,) * tensor.ndim] * tensor
         return self.assemble_tensor(row_kind, column_kind, full)
 
+    def assemble_kinds(self, row_kind, column_kind, coefficient=1.0, *, num_threads=0):
+        """Value / gradient contractions with a scalar coefficient c
+        (bilinear_form.py:244-334) on volume bases, component by component:
+        value-value c; a gradient against a value pairs each derivative
+        direction with the value, c for every direction; gradient-gradient c
+        for equal directions.  ``normal_gradient`` needs facet normals, which
+        volume bases do not have (ValueError, as the reference's)."""
+        valid = {"value", "gradient", "normal_gradient"}
+        if row_kind not in valid or column_kind not in valid:
+            raise ValueError("cross kind must be value, gradient, or normal_gradient")
+        if self.test_components != self.trial_components:
+            raise ValueError("cross contractions require matching components")
+        scalar = np.broadcast_to(np.asarray(coefficient, dtype=np.float64), self.coefficient_shape)
+        if row_kind == "normal_gradient":
+            raise ValueError("row normal_gradient requires test-basis normals")
+        if column_kind == "normal_gradient":
+            raise ValueError("column normal_gradient requires trial-basis normals")
+        C, d = self.test_components, self.dimension
+        if row_kind == "value" and column_kind == "value":
+            pattern = np.eye(C)
+        elif column_kind == "value":
+            pattern = np.einsum("rc,i->ric", np.eye(C), np.ones(d))
+        elif row_kind == "value":
+            pattern = np.einsum("rc,j->rcj", np.eye(C), np.ones(d))
+        else:
+            pattern = np.einsum("rc,ij->ricj", np.eye(C), np.eye(d))
+        # the coefficient placed into zeros (exact zeros elsewhere, whatever its sign)
+        tensor = np.zeros(self.coefficient_shape + pattern.shape)
+        for index in zip(*np.nonzero(pattern)):
+            tensor[(Ellipsis,) + index] = scalar
+        return self.assemble_tensor(row_kind, column_kind, tensor, num_threads=num_threads)
+
     def assemble_tensor(self, row_kind, column_kind, coefficient, *, num_threads=0):
         """Assemble a caller-supplied value / gradient contraction tensor
         (cell, point) + row axes + column axes."""

@@ -255,6 +255,17 @@ def main():
     rhs = sk.asm(load, b2, f=fq)
     out["p2_load"] = dict(p=m2.p, t=m2.t, X=X4, W=W4, f=fq, rhs=np.asarray(rhs).copy())
 
+    # --- NativeCrossBilinearForm.assemble_kinds on vector P1 (4-point rule): the four value /
+    #     gradient pairings with a per-point coefficient of both signs ---
+    bkp = sk.Basis(mc, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(X4, W4))
+    ck = np.random.default_rng(np.random.SeedSequence(43)).uniform(-1.0, 2.0, bkp.dx.shape)
+    kinds = {}
+    for row_kind in ("value", "gradient"):
+        for column_kind in ("value", "gradient"):
+            Kk = sk.NativeCrossBilinearForm(bkp, bkp).assemble_kinds(row_kind, column_kind, ck)
+            kinds.update({f"{row_kind}_{column_kind}_{k}": v for k, v in csr_parts(Kk).items()})
+    out["cross_kinds"] = dict(p=mc.p, t=mc.t, X=X4, W=W4, c=ck, **kinds)
+
     # --- volume forms from the reference's compatible-forms cases on vector P1 (default rule):
     #     constant, gradient and coordinate loads; mass, elasticity, coordinate and parameter
     #     coefficients ---

@@ -708,6 +708,30 @@ def test_n1_orientation_invariance():
     np.testing.assert_allclose(lo, lm, atol=4e-14)
 
 
+def test_cross_assemble_kinds_matches_reference():
+    """NativeCrossBilinearForm.assemble_kinds (bilinear_form.py:244-334) on vector P1: the four value /
+    gradient pairings with a per-point coefficient of both signs against the reference's own outputs
+    (fixture cross_kinds); an unknown kind, normal_gradient without facet normals and mismatched
+    component counts raise ValueError."""
+    g = load_golden("cross_kinds")
+    m = sk.MeshTet(g["p"], g["t"])
+    b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(g["X"], g["W"]))
+    form = sk.NativeCrossBilinearForm(b, b)
+    for row in ("value", "gradient"):
+        for column in ("value", "gradient"):
+            K = form.assemble_kinds(row, column, g["c"])
+            key = f"{row}_{column}_"
+            assert np.array_equal(K.indptr, g[key + "indptr"]) and np.array_equal(K.indices, g[key + "indices"])
+            assert relerr(K.data, g[key + "data"]) < RTOL, (row, column)
+    with pytest.raises(ValueError, match="cross kind must be"):
+        form.assemble_kinds("curl", "value")
+    with pytest.raises(ValueError, match="requires test-basis normals"):
+        form.assemble_kinds("normal_gradient", "value")
+    bs = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=1), quadrature=(g["X"], g["W"]))
+    with pytest.raises(ValueError, match="matching components"):
+        sk.NativeCrossBilinearForm(b, bs).assemble_kinds("value", "value")
+
+
 def test_cross_basis_assembly_matches_reference():
     """Two-basis asm (Stokes-type coupling div(v) u, a weighted P2 x P1 mass) and
     NativeCrossBilinearForm.assemble_tensor (gradient and value tensors on vector
