@@ -173,6 +173,12 @@ class Basis:
         return self._host("x")
 
     @property
+    def nelems(self):
+        """Number of elements (basis.py:1804-1806), from the mesh: reading dx
+        would make the device tabulation."""
+        return int(self.mesh.nelements)
+
+    @property
     def _coefficient_shape(self):
         return (self.mesh.nelements, len(self.W))
 

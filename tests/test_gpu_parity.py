@@ -716,6 +716,7 @@ def test_cross_assemble_kinds_matches_reference():
     g = load_golden("cross_kinds")
     m = sk.MeshTet(g["p"], g["t"])
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(g["X"], g["W"]))
+    assert b.nelems == m.nelements == b.dx.shape[0]
     form = sk.NativeCrossBilinearForm(b, b)
     for row in ("value", "gradient"):
         for column in ("value", "gradient"):
