@@ -553,6 +553,9 @@ class NativeCrossBilinearForm:
         self.test_components = test_basis._comp
         self.trial_components = trial_basis._comp
         self.dimension = 3
+        # facet normals of the bases (bilinear_form.py:177-178): None for volume bases
+        self.test_normals = getattr(test_basis, "normals", None)
+        self.trial_normals = getattr(trial_basis, "normals", None)
 
     def assemble(self, kind, coefficient):
         """kind: "value", "gradient", "row_divergence" (vector test, scalar
@@ -601,10 +604,12 @@ class NativeCrossBilinearForm:
         if self.test_components != self.trial_components:
             raise ValueError("cross contractions require matching components")
         scalar = np.broadcast_to(np.asarray(coefficient, dtype=np.float64), self.coefficient_shape)
-        if row_kind == "normal_gradient":
+        if row_kind == "normal_gradient" and self.test_normals is None:
             raise ValueError("row normal_gradient requires test-basis normals")
-        if column_kind == "normal_gradient":
+        if column_kind == "normal_gradient" and self.trial_normals is None:
             raise ValueError("column normal_gradient requires trial-basis normals")
+        if "normal_gradient" in (row_kind, column_kind):
+            raise UnsupportedNativeForm("normal_gradient contractions need facet bases")
         C, d = self.test_components, self.dimension
         if row_kind == "value" and column_kind == "value":
             pattern = np.eye(C)

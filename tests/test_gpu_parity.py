@@ -718,6 +718,7 @@ def test_cross_assemble_kinds_matches_reference():
     b = sk.Basis(m, sk.ElementVector(sk.ElementTetP1(), dim=3), quadrature=(g["X"], g["W"]))
     assert b.nelems == m.nelements == b.dx.shape[0]
     form = sk.NativeCrossBilinearForm(b, b)
+    assert form.test_normals is None and form.trial_normals is None
     for row in ("value", "gradient"):
         for column in ("value", "gradient"):
             K = form.assemble_kinds(row, column, g["c"])
