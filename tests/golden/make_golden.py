@@ -120,6 +120,13 @@ def main():
     K2d = sk.asm(lap, b2d)
     out["p2_laplace_default"] = dict(p=m2.p, t=m2.t, X=b2d.X, W=b2d.W, **csr_parts(K2d))
 
+    # --- the Duffy product rules of the N1 basis, orders 1 to 8 ---
+    n1_rules = {}
+    for order in range(1, 9):
+        bo = sk.AffineTetN1Basis(sk.MeshTet(), intorder=order)
+        n1_rules[f"X{order}"], n1_rules[f"W{order}"] = bo.X, bo.W
+    out["n1_rules"] = n1_rules
+
     # --- the basis rules above order 4 (collapsed Gauss-Legendre), and P2 Laplace with order 6 ---
     rules = {}
     for order in (5, 6, 7, 8):

@@ -230,6 +230,17 @@ def test_high_order_rules_match_the_reference_and_integrate_monomials():
                     assert abs(got - exact) <= 1e-14 * max(exact, 1e-3), (order, a, b, c)
 
 
+def test_n1_duffy_rules_match_the_reference():
+    """The N1 basis's Duffy product rules (hcurl_basis.py:37-56), orders 1 to 8, are the reference's numbers
+    (fixture n1_rules), and the oracle's restatement agrees."""
+    g = load_golden("n1_rules")
+    for order in range(1, 9):
+        X, W = quadrature.duffy_rule(order)
+        assert np.array_equal(X, g[f"X{order}"]) and np.array_equal(W, g[f"W{order}"]), order
+        Xo, Wo = O.duffy_quadrature(order)
+        assert np.array_equal(Xo, X) and np.array_equal(Wo, W), order
+
+
 def test_rules_too_large_for_the_geometry_kernel_are_rejected_before_device_work():
     """A P2 rule of order 12 (512 points) needs more reference tables than one block's shared memory holds:
     UnsupportedNativeForm before anything reaches the device; order 11 (343 points) fits."""
